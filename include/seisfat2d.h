@@ -1,0 +1,131 @@
+/*
+ * seisfat2d.h - C ABI of the GB300 first-arrival traveltime engine.
+ *
+ * A drop-in for the fast-sweeping eikonal path of phbastosa/SeisFAT2D:
+ * every entry point names the reference interface it replaces. Plain C: plain
+ * pointers and sizes, int status codes, no exceptions cross the boundary.
+ *
+ * Grid conventions (the reference's, src/modeling/modeling.cu:3-36):
+ *   model   nz x nx samples, z fastest: model[i + j*nz]
+ *   padded  nzz = nz + 2*nb rows, nxx = nx + 2*nb columns, nb = 3,
+ *           z fastest: T[i + j*nzz]; the pad replicates the edge samples
+ *   shots   source (sx, sz) in metres from the model origin
+ *
+ * Threading: one context per host thread; contexts are independent.
+ * Streams: `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ * Calls that take SF_MEM_HOST buffers synchronise the stream before returning.
+ */
+#ifndef SEISFAT2D_H
+#define SEISFAT2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SF_OK 0
+#define SF_ERR_ARG 1     /* bad argument (null pointer, size, layout)        */
+#define SF_ERR_CUDA 2    /* a CUDA runtime call or kernel launch failed      */
+#define SF_ERR_TIMEOUT 3 /* a bounded in-kernel wait gave up (results void)  */
+#define SF_ERR_RANGE 4   /* source or window outside the grid                */
+#define SF_ERR_STATE 5   /* call out of order (e.g. adjoint without a tape)  */
+#define SF_ERR_NOMEM 6   /* device allocation failed                          */
+
+/* memory kinds for buffer arguments */
+#define SF_MEM_HOST 0
+#define SF_MEM_DEVICE 1
+
+/* slowness layouts */
+#define SF_LAYOUT_MODEL 0  /* nz x nx, expanded to the padded grid on device */
+#define SF_LAYOUT_PADDED 1 /* nzz x nxx, taken as is                          */
+
+/* sf_batch_forward flags */
+#define SF_KEEP_TAPE 1   /* record the update tape for sf_batch_adjoint      */
+#define SF_KEEP_TABLES 2 /* keep every shot's traveltime window on device   */
+
+typedef struct sf_ctx sf_ctx;
+
+/* One shot of a batch. The solve runs on padded columns [c0, c0+ncols)
+ * (ncols <= 0: the whole width), with that window's first and last columns
+ * held fixed like the grid's outer ring. */
+typedef struct {
+    float sx, sz;
+    int c0, ncols;
+} sf_shot;
+
+const char* sf_status_string(int status);
+const char* sf_ctx_last_error(const sf_ctx* ctx);
+
+/* Modeling::set_parameters (modeling.cu:3-36) + set_eikonal (:62-102):
+ * grid sizes, spacing and device buffers. nb is fixed at 3. */
+int sf_ctx_create(sf_ctx** out, int nx, int nz, float dx, float dz, int device);
+int sf_ctx_destroy(sf_ctx* ctx);
+int sf_ctx_dims(const sf_ctx* ctx, int* nxx, int* nzz, int* nb);
+
+/* Modeling::set_properties + expand_boundary (modeling.cu:47-60, :204-232)
+ * and copy_slowness_to_device (:281-284). */
+int sf_set_slowness(sf_ctx* ctx, const float* s, int layout, int mem);
+/* padded slowness back (nzz x nxx) */
+int sf_get_slowness(sf_ctx* ctx, float* out, int mem);
+
+/* Eikonal_ANI::set_conditions / set_stiffness_element (eikonal_ani.cu:3-31)
+ * with Modeling::compression (modeling.cu:264-279): six nz x nx fields
+ * C11,C13,C15,C33,C35,C55, padded and quantised to uint16 with a
+ * deterministic min/max. */
+int sf_set_stiffness(sf_ctx* ctx, const float* const cij[6], int mem);
+/* Same with already quantised padded codes (nzz x nxx each) and their
+ * (min, max) pairs, for inputs quantised elsewhere. */
+int sf_set_stiffness_codes(sf_ctx* ctx, const uint16_t* const codes[6], const float minmax[12],
+                           int mem);
+
+/* Eikonal_ISO::time_propagation / Eikonal_ANI::time_propagation
+ * (eikonal_iso.cu:9-12, eikonal_ani.cu:33-45): initialization() +
+ * eikonal_solver() [+ get_quasi_slowness + second solve] for one source on
+ * the whole padded grid. T receives nzz x nxx traveltimes. One CTA. */
+int sf_time_propagation(sf_ctx* ctx, int ani, float sx, float sz, float* T, int T_mem,
+                        void* stream);
+
+/* Modeling::compute_seismogram (modeling.cu:161-194): 4x4 Catmull-Rom picks
+ * of a padded traveltime field (device pointer, nzz x nxx) at nrec receivers
+ * (host coordinates). Receivers whose stencil leaves the grid give NaN. */
+int sf_compute_seismogram(sf_ctx* ctx, const float* T_dev, const float* rx, const float* rz,
+                          int nrec, float* picks, int picks_mem, void* stream);
+
+/* Batched forward: the shot loop of modeling_main.cpp:21-29 (and the
+ * traveltime-table loops of migration.cu:116-171) in one persistent launch.
+ * shots/rx/rz are host arrays; picks is nshots x nrec (shot-major). */
+int sf_batch_forward(sf_ctx* ctx, int ani, const sf_shot* shots, int nshots, const float* rx,
+                     const float* rz, int nrec, float* picks, int picks_mem, int flags,
+                     void* stream);
+
+/* Traveltime window of shot `shot` of the last batch run with
+ * SF_KEEP_TABLES: nzz x ncols values, z fastest. */
+int sf_batch_table(sf_ctx* ctx, int shot, float* T, int mem, void* stream);
+
+/* Adjoint-state gradient (no counterpart in the reference, whose tomography
+ * traced rays on the host: inversion.cpp:95-177). Needs the last batch run
+ * with SF_KEEP_TAPE. pick_grad: dJ/dpicks, nshots x nrec (NaN picks are
+ * ignored); grad receives dJ/dS on the padded grid (nzz x nxx, overwritten). */
+int sf_batch_adjoint(sf_ctx* ctx, const float* pick_grad, int pg_mem, float* grad, int grad_mem,
+                     void* stream);
+
+/* Misfit J = 1/2 sum (pick - t_obs)^2 over valid picks (FP64) and its
+ * gradient dJ/dS, from the last SF_KEEP_TAPE batch. Replaces
+ * Inversion::check_convergence + optimization (inversion.cpp:179-345). */
+int sf_batch_misfit_gradient(sf_ctx* ctx, const float* t_obs, int obs_mem, double* misfit,
+                             float* grad, int grad_mem, void* stream);
+
+/* Waits for `stream` and reports in-kernel failures (SF_ERR_TIMEOUT). */
+int sf_synchronize(sf_ctx* ctx, void* stream);
+
+/* Launch shape: warps per CTA (4..16) and CTAs per SM for batches (1..4);
+ * 0 keeps the current value. */
+int sf_set_launch(sf_ctx* ctx, int warps, int ctas_per_sm);
+int sf_get_launch(const sf_ctx* ctx, int* warps, int* ctas_per_sm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,841 @@
+/*
+ * CPU oracle for the SeisFAT2D fast-sweeping eikonal path (test infrastructure;
+ * see eikonal_oracle.h for what each function restates). Build with
+ * -ffp-contract=off so that every FP32 operation rounds once, in source order.
+ */
+#include "eikonal_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define SF_BIG 1e6f
+#define NTHREADS_REF 256 /* modeling.cuh:11 */
+
+/* ---------------------------------------------------------------- padding */
+
+/* modeling.cu:204-232 */
+void orc_expand_boundary(const float* in, int nx, int nz, int nb, float* out)
+{
+    int nxx = nx + 2 * nb, nzz = nz + 2 * nb;
+    for (int j = 0; j < nx; j++)
+        for (int i = 0; i < nz; i++) out[(i + nb) + (j + nb) * nzz] = in[i + j * nz];
+    for (int i = 0; i < nb; i++)
+        for (int j = nb; j < nxx - nb; j++) {
+            out[i + j * nzz] = out[nb + j * nzz];
+            out[(nzz - i - 1) + j * nzz] = out[(nzz - nb - 1) + j * nzz];
+        }
+    for (int i = 0; i < nzz; i++)
+        for (int j = 0; j < nb; j++) {
+            out[i + j * nzz] = out[i + nb * nzz];
+            out[i + (nxx - j - 1) * nzz] = out[i + (nxx - nb - 1) * nzz];
+        }
+}
+
+/* modeling.cu:234-244 */
+void orc_reduce_boundary(const float* in, int nx, int nz, int nb, float* out)
+{
+    int nzz = nz + 2 * nb;
+    for (int j = 0; j < nx; j++)
+        for (int i = 0; i < nz; i++) out[i + j * nz] = in[(i + nb) + (j + nb) * nzz];
+}
+
+/* ------------------------------------------------ reference launch schedule */
+
+/* The per-level offsets of modeling.cu:137-148, restated. */
+static void level_offsets(int sweep, int level, int nxx, int nzz, int* zo, int* xo)
+{
+    switch (sweep) {
+    case 0:
+        *zo = (level < nxx) ? 0 : level - nxx + 1;
+        *xo = (level < nxx) ? level : nxx - 1;
+        break;
+    case 1:
+        *zo = (level < nzz) ? nzz - level - 1 : 0;
+        *xo = (level < nzz) ? 0 : level - nzz + 1;
+        break;
+    case 2:
+        *zo = (level < nzz) ? level : nzz - 1;
+        *xo = (level < nzz) ? nxx - 1 : nxx - 1 - (level - nzz + 1);
+        break;
+    default:
+        *zo = (level < nxx) ? nzz - 1 : nzz - 1 - (level - nxx + 1);
+        *xo = (level < nxx) ? nxx - level - 1 : 0;
+        break;
+    }
+}
+
+/* modeling.cu:150-154: threads launched for a level (the middle-band count is
+ * level-2, which can fall one short of the diagonal; the bound check at
+ * modeling.cu:319 hides the excess). */
+static int level_threads(int level, int nxx, int nzz)
+{
+    int total = nxx + nzz - 2, mn = nxx < nzz ? nxx : nzz, mx = nxx < nzz ? nzz : nxx;
+    int n = (level < mn) ? level + 1 : (level >= mx) ? total - level : total - mn - mx + level;
+    int nblk = (n + NTHREADS_REF - 1) / NTHREADS_REF;
+    return nblk * NTHREADS_REF;
+}
+
+static void sweep_dirs(int sweep, int* zd, int* xd)
+{
+    *zd = (sweep == 2 || sweep == 3) ? -1 : 1; /* modeling.cu:132-133 */
+    *xd = (sweep == 0 || sweep == 2) ? -1 : 1;
+}
+
+static int imax(int a, int b) { return a > b ? a : b; }
+static int imin(int a, int b) { return a < b ? a : b; }
+
+void orc_skip_cells(int ncols, int nzz, int skip_i[4], int skip_j[4])
+{
+    int nxx = ncols, total = nxx + nzz - 2;
+    for (int s = 0; s < 4; s++) {
+        skip_i[s] = -1;
+        skip_j[s] = -1;
+        int zd, xd;
+        sweep_dirs(s, &zd, &xd);
+        for (int level = 0; level < total; level++) {
+            int zo, xo;
+            level_offsets(s, level, nxx, nzz, &zo, &xo);
+            /* element range e >= 0 whose node is interior */
+            int lo = 0, hi = 1 << 30;
+            if (zd > 0) { lo = imax(lo, 1 - zo); hi = imin(hi, nzz - 2 - zo); }
+            else        { lo = imax(lo, zo - (nzz - 2)); hi = imin(hi, zo - 1); }
+            if (xd > 0) { lo = imax(lo, 1 - xo); hi = imin(hi, nxx - 2 - xo); }
+            else        { lo = imax(lo, xo - (nxx - 2)); hi = imin(hi, xo - 1); }
+            int nl = level_threads(level, nxx, nzz);
+            for (int e = imax(lo, nl); e <= hi; e++) {
+                /* at most one per sweep for any shape (checked by the tests) */
+                skip_i[s] = zo + zd * e;
+                skip_j[s] = xo + xd * e;
+            }
+        }
+    }
+}
+
+/* ----------------------------------------------------------- source / init */
+
+/* modeling.cu:112-113 */
+void orc_source_index(float sx, float sz, float dx, float dz, int nb, int* sIdx, int* sIdz)
+{
+    *sIdx = (int)((sx + 0.5f * dx) / dx) + nb;
+    *sIdz = (int)((sz + 0.5f * dz) / dz) + nb;
+}
+
+/* modeling.cu:293-306, evaluated in FP64. */
+void orc_init_block_f64(const float* S, int nzz, float sx, float sz, float dx, float dz,
+                        int nb, int sIdx, int sIdz, double vals[9])
+{
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) {
+            int zi = sIdz + a - 1, xi = sIdx + b - 1;
+            double ddx = (double)(xi - nb) * (double)dx - (double)sx;
+            double ddz = (double)(zi - nb) * (double)dz - (double)sz;
+            vals[a + 3 * b] = (double)S[zi + (size_t)xi * nzz] * sqrt(ddx * ddx + ddz * ddz);
+        }
+}
+
+static void init_dist_f64(int nb, float sx, float sz, float dx, float dz, int sIdx, int sIdz,
+                          double dist[9])
+{
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) {
+            int zi = sIdz + a - 1, xi = sIdx + b - 1;
+            double ddx = (double)(xi - nb) * (double)dx - (double)sx;
+            double ddz = (double)(zi - nb) * (double)dz - (double)sz;
+            dist[a + 3 * b] = sqrt(ddx * ddx + ddz * ddz);
+        }
+}
+
+/* ------------------------------------------------------------- the update */
+
+typedef struct {
+    float dx, dz, dx2i, dz2i, hyp;
+} k32;
+
+typedef struct {
+    double dx, dz, dx2i, dz2i, hyp;
+} k64;
+
+static k32 make_k32(float dx, float dz)
+{
+    k32 k;
+    k.dx = dx;
+    k.dz = dz;
+    k.dz2i = 1.0f / (dz * dz); /* modeling.cu:64-65 */
+    k.dx2i = 1.0f / (dx * dx);
+    k.hyp = sqrtf(dx * dx + dz * dz);
+    return k;
+}
+
+static k64 make_k64(double dx, double dz)
+{
+    k64 k;
+    k.dx = dx;
+    k.dz = dz;
+    k.dz2i = 1.0 / (dz * dz);
+    k.dx2i = 1.0 / (dx * dx);
+    k.hyp = sqrt(dx * dx + dz * dz);
+    return k;
+}
+
+/* Tape record of one node update. */
+typedef struct {
+    int code;
+    double c1, c2;
+} rec_t;
+
+/*
+ * inner_sweep's per-node arithmetic (modeling.cu:319-356). s1a/s1b are the two
+ * cells of the vertical upwind edge (row i1, columns max(j-1,1) and j), s2a/s2b
+ * of the horizontal one (rows max(i-1,1) and i, column j1), sref = S[i1][j1].
+ * dc1a: column offset code (0 -> j-1, 1 -> j) of s1a, dr2a: row code of s2a;
+ * dr1 / dc2: row code of the vertical edge's cells / column code of the
+ * horizontal edge's cells; those describe where a candidate read its slowness.
+ */
+static float upd32(float told, float tv, float te, float tev, float s1a, float s1b, float s2a,
+                   float s2b, float sref, const k32* k, int dr1, int dc1a, int dc2, int dr2a,
+                   rec_t* rec)
+{
+    float m1 = fminf(s1a, s1b);
+    float m2 = fminf(s2a, s2b);
+    float t1d1 = tv + k->dz * m1;
+    float t1d2 = te + k->dx * m2;
+    float t1D = fminf(t1d1, t1d2);
+    float t1 = SF_BIG, t2 = SF_BIG, t3 = SF_BIG;
+    int br = 0;
+    float rr = 0.0f, dd = 0.0f, q = 0.0f, qq = 0.0f;
+    if ((tv <= te + k->dx * sref) && (te <= tv + k->dz * sref) && (te - tev >= 0.0f) &&
+        (tv - tev >= 0.0f)) {
+        float ta = tev + te - tv;
+        float tb = tev - te + tv;
+        dd = ta - tb;
+        rr = sqrtf(4.0f * sref * sref * (k->dz2i + k->dx2i) - k->dz2i * k->dx2i * dd * dd);
+        t1 = ((tb * k->dz2i + ta * k->dx2i) + rr) / (k->dz2i + k->dx2i);
+        br = 3;
+    } else if ((te - tev <= sref * k->dz * k->dz / k->hyp) && (te - tev > 0.0f)) {
+        q = (te - tev) / k->dz;
+        qq = sqrtf(sref * sref - q * q);
+        t2 = te + k->dx * qq;
+        br = 4;
+    } else if ((tv - tev <= sref * k->dx * k->dx / k->hyp) && (tv - tev > 0.0f)) {
+        q = (tv - tev) / k->dx;
+        qq = sqrtf(sref * sref - q * q);
+        t3 = tv + k->dz * qq;
+        br = 5;
+    }
+    float t2D = fminf(t1, fminf(t2, t3));
+    float cand = fminf(t1D, t2D);
+    float tnew = fminf(told, cand);
+    if (rec) {
+        rec->code = 0;
+        rec->c1 = 0.0;
+        rec->c2 = 0.0;
+        if (cand < told) {
+            if (t1D <= t2D) {
+                if (t1d1 <= t1d2) {
+                    int dc = (s1a <= s1b) ? dc1a : 1;
+                    rec->code = 1 | (dr1 << 3) | (dc << 4);
+                    rec->c2 = k->dz;
+                } else {
+                    int dr = (s2a <= s2b) ? dr2a : 1;
+                    rec->code = 2 | (dr << 3) | (dc2 << 4);
+                    rec->c2 = k->dx;
+                }
+            } else if (br != 0) {
+                int pos = (dr1 << 3) | (dc2 << 4); /* Sref = S[i1][j1] */
+                rec->code = br | pos;
+                if (br == 3) {
+                    float D = k->dz2i + k->dx2i;
+                    float kA = k->dz2i - k->dx2i;
+                    float k2K = 2.0f * (k->dz2i * k->dx2i);
+                    if (rr > 0.0f) {
+                        rec->c1 = (kA + (k2K * dd) / rr) / D;
+                        rec->c2 = (4.0f * sref) / rr;
+                    } else {
+                        rec->c1 = kA / D;
+                        rec->c2 = 0.0f;
+                    }
+                } else {
+                    float hx = (br == 4) ? k->dx : k->dz; /* multiplies the sqrt */
+                    float hq = (br == 4) ? k->dz : k->dx; /* divides the difference */
+                    if (qq > 0.0f) {
+                        rec->c1 = (hx * q) / (hq * qq);
+                        rec->c2 = (hx * sref) / qq;
+                    } else {
+                        rec->c1 = 0.0f;
+                        rec->c2 = 0.0f;
+                    }
+                }
+            }
+        }
+    }
+    return tnew;
+}
+
+static double upd64(double told, double tv, double te, double tev, double s1a, double s1b,
+                    double s2a, double s2b, double sref, const k64* k, int dr1, int dc1a, int dc2,
+                    int dr2a, rec_t* rec)
+{
+    double m1 = fmin(s1a, s1b);
+    double m2 = fmin(s2a, s2b);
+    double t1d1 = tv + k->dz * m1;
+    double t1d2 = te + k->dx * m2;
+    double t1D = fmin(t1d1, t1d2);
+    double t1 = 1e6, t2 = 1e6, t3 = 1e6;
+    int br = 0;
+    double rr = 0.0, dd = 0.0, q = 0.0, qq = 0.0;
+    if ((tv <= te + k->dx * sref) && (te <= tv + k->dz * sref) && (te - tev >= 0.0) &&
+        (tv - tev >= 0.0)) {
+        double ta = tev + te - tv;
+        double tb = tev - te + tv;
+        dd = ta - tb;
+        rr = sqrt(4.0 * sref * sref * (k->dz2i + k->dx2i) - k->dz2i * k->dx2i * dd * dd);
+        t1 = ((tb * k->dz2i + ta * k->dx2i) + rr) / (k->dz2i + k->dx2i);
+        br = 3;
+    } else if ((te - tev <= sref * k->dz * k->dz / k->hyp) && (te - tev > 0.0)) {
+        q = (te - tev) / k->dz;
+        qq = sqrt(sref * sref - q * q);
+        t2 = te + k->dx * qq;
+        br = 4;
+    } else if ((tv - tev <= sref * k->dx * k->dx / k->hyp) && (tv - tev > 0.0)) {
+        q = (tv - tev) / k->dx;
+        qq = sqrt(sref * sref - q * q);
+        t3 = tv + k->dz * qq;
+        br = 5;
+    }
+    double t2D = fmin(t1, fmin(t2, t3));
+    double cand = fmin(t1D, t2D);
+    double tnew = fmin(told, cand);
+    if (rec) {
+        rec->code = 0;
+        rec->c1 = 0.0;
+        rec->c2 = 0.0;
+        if (cand < told) {
+            if (t1D <= t2D) {
+                if (t1d1 <= t1d2) {
+                    int dc = (s1a <= s1b) ? dc1a : 1;
+                    rec->code = 1 | (dr1 << 3) | (dc << 4);
+                    rec->c2 = k->dz;
+                } else {
+                    int dr = (s2a <= s2b) ? dr2a : 1;
+                    rec->code = 2 | (dr << 3) | (dc2 << 4);
+                    rec->c2 = k->dx;
+                }
+            } else if (br != 0) {
+                rec->code = br | (dr1 << 3) | (dc2 << 4);
+                if (br == 3) {
+                    double D = k->dz2i + k->dx2i;
+                    if (rr > 0.0) {
+                        rec->c1 = ((k->dz2i - k->dx2i) + 2.0 * k->dz2i * k->dx2i * dd / rr) / D;
+                        rec->c2 = 4.0 * sref / rr;
+                    } else {
+                        rec->c1 = (k->dz2i - k->dx2i) / D;
+                    }
+                } else {
+                    double hx = (br == 4) ? k->dx : k->dz;
+                    double hq = (br == 4) ? k->dz : k->dx;
+                    if (qq > 0.0) {
+                        rec->c1 = hx * q / (hq * qq);
+                        rec->c2 = hx * sref / qq;
+                    }
+                }
+            }
+        }
+    }
+    return tnew;
+}
+
+/* ------------------------------------------------------------- the solvers */
+
+#define SAT(i, j) S[(size_t)(i) + (size_t)(j) * ldS]
+#define TAT(i, j) T[(size_t)(i) + (size_t)(j) * nzz]
+
+static void sweep_signs(int sweep, int* sz, int* sx)
+{
+    /* sgnt of modeling.cu:68: {1,1},{-1,1},{1,-1},{-1,-1} (z, x) */
+    *sz = (sweep == 1 || sweep == 3) ? -1 : 1;
+    *sx = (sweep >= 2) ? -1 : 1;
+}
+
+/* Node (i, j) of sweep `sweep` in FP32; returns the new value. */
+static float node32(int sweep, int i, int j, int nzz, int ncols, const float* S, int ldS,
+                    const float* T, const k32* k, rec_t* rec)
+{
+    int sz, sx;
+    sweep_signs(sweep, &sz, &sx);
+    int i1 = (sz > 0) ? i - 1 : i; /* i - sgnv[sgni] */
+    int j1 = (sx > 0) ? j - 1 : j;
+    float tv = TAT(i - sz, j);
+    float te = TAT(i, j - sx);
+    float tev = TAT(i - sz, j - sx);
+    float s1a = SAT(i1, imax(j - 1, 1)), s1b = SAT(i1, imin(j, ncols - 1));
+    float s2a = SAT(imax(i - 1, 1), j1), s2b = SAT(imin(i, nzz - 1), j1);
+    float sref = SAT(i1, j1);
+    int dr1 = (sz > 0) ? 0 : 1, dc2 = (sx > 0) ? 0 : 1;
+    int dc1a = (j - 1 >= 1) ? 0 : 1, dr2a = (i - 1 >= 1) ? 0 : 1;
+    return upd32(TAT(i, j), tv, te, tev, s1a, s1b, s2a, s2b, sref, k, dr1, dc1a, dc2, dr2a, rec);
+}
+
+static double node64(int sweep, int i, int j, int nzz, int ncols, const float* S, int ldS,
+                     const double* T, const k64* k, rec_t* rec)
+{
+    int sz, sx;
+    sweep_signs(sweep, &sz, &sx);
+    int i1 = (sz > 0) ? i - 1 : i;
+    int j1 = (sx > 0) ? j - 1 : j;
+    double tv = TAT(i - sz, j);
+    double te = TAT(i, j - sx);
+    double tev = TAT(i - sz, j - sx);
+    double s1a = SAT(i1, imax(j - 1, 1)), s1b = SAT(i1, imin(j, ncols - 1));
+    double s2a = SAT(imax(i - 1, 1), j1), s2b = SAT(imin(i, nzz - 1), j1);
+    double sref = SAT(i1, j1);
+    int dr1 = (sz > 0) ? 0 : 1, dc2 = (sx > 0) ? 0 : 1;
+    int dc1a = (j - 1 >= 1) ? 0 : 1, dr2a = (i - 1 >= 1) ? 0 : 1;
+    return upd64(TAT(i, j), tv, te, tev, s1a, s1b, s2a, s2b, sref, k, dr1, dc1a, dc2, dr2a, rec);
+}
+
+static void init_field_f32(float* T, int nzz, int ncols, int sIdz, int sIdx_loc, const float init[9])
+{
+    for (size_t n = 0; n < (size_t)nzz * ncols; n++) T[n] = SF_BIG; /* time_set */
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) TAT(sIdz + a - 1, sIdx_loc + b - 1) = init[a + 3 * b];
+}
+
+static void init_field_f64(double* T, int nzz, int ncols, int sIdz, int sIdx_loc, const double init[9])
+{
+    for (size_t n = 0; n < (size_t)nzz * ncols; n++) T[n] = 1e6;
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) TAT(sIdz + a - 1, sIdx_loc + b - 1) = init[a + 3 * b];
+}
+
+static int is_skip(int s, int i, int j, const int si[4], const int sj[4])
+{
+    return i == si[s] && j == sj[s];
+}
+
+void orc_solve_f32(int nzz, int ncols, const float* S, int ldS, float dx, float dz, int sIdz,
+                   int sIdx_loc, const float init[9], float* T, int passes, int order)
+{
+    k32 k = make_k32(dx, dz);
+    int si[4], sj[4];
+    orc_skip_cells(ncols, nzz, si, sj);
+    init_field_f32(T, nzz, ncols, sIdz, sIdx_loc, init);
+    int nxx = ncols, total = nxx + nzz - 2;
+    for (int p = 0; p < passes; p++)
+        for (int s = 0; s < 4; s++) {
+            if (order == 0) {
+                int zd, xd;
+                sweep_dirs(s, &zd, &xd);
+                for (int level = 0; level < total; level++) {
+                    int zo, xo;
+                    level_offsets(s, level, nxx, nzz, &zo, &xo);
+                    int nl = level_threads(level, nxx, nzz);
+                    /* cells of one level are independent: update in place */
+                    for (int e = 0; e < nl; e++) {
+                        int i = zo + zd * e, j = xo + xd * e;
+                        if (i > 0 && i < nzz - 1 && j > 0 && j < nxx - 1)
+                            TAT(i, j) = node32(s, i, j, nzz, ncols, S, ldS, T, &k, NULL);
+                    }
+                }
+            } else {
+                int sz, sx;
+                sweep_signs(s, &sz, &sx);
+                for (int jj = 1; jj <= ncols - 2; jj++) {
+                    int j = (sx > 0) ? jj : ncols - 1 - jj;
+                    for (int ii = 1; ii <= nzz - 2; ii++) {
+                        int i = (sz > 0) ? ii : nzz - 1 - ii;
+                        if (is_skip(s, i, j, si, sj)) continue;
+                        TAT(i, j) = node32(s, i, j, nzz, ncols, S, ldS, T, &k, NULL);
+                    }
+                }
+            }
+        }
+}
+
+int orc_solve_f64(int nzz, int ncols, const float* S, int ldS, double dx, double dz, int sIdz,
+                  int sIdx_loc, const double init[9], double* T, int passes, double tol,
+                  int max_passes)
+{
+    k64 k = make_k64(dx, dz);
+    int si[4], sj[4];
+    orc_skip_cells(ncols, nzz, si, sj);
+    init_field_f64(T, nzz, ncols, sIdz, sIdx_loc, init);
+    int npass = passes > 0 ? passes : max_passes;
+    int run = 0;
+    for (int p = 0; p < npass; p++) {
+        double change = 0.0;
+        for (int s = 0; s < 4; s++) {
+            int sz, sx;
+            sweep_signs(s, &sz, &sx);
+            for (int jj = 1; jj <= ncols - 2; jj++) {
+                int j = (sx > 0) ? jj : ncols - 1 - jj;
+                for (int ii = 1; ii <= nzz - 2; ii++) {
+                    int i = (sz > 0) ? ii : nzz - 1 - ii;
+                    if (is_skip(s, i, j, si, sj)) continue;
+                    double old = TAT(i, j);
+                    double nv = node64(s, i, j, nzz, ncols, S, ldS, T, &k, NULL);
+                    TAT(i, j) = nv;
+                    if (old < 1e6 && old - nv > change) change = old - nv;
+                    if (old >= 1e6 && nv < 1e6) change = 1e30;
+                }
+            }
+        }
+        run++;
+        if (passes <= 0 && change <= tol) break;
+    }
+    return run;
+}
+
+/* ------------------------------------------------------------- anisotropy */
+
+/* modeling.cu:264-279 with a deterministic min/max (the reference's OpenMP
+ * loop races on min_value/max_value). max == min gives code 1 (decodes to min
+ * exactly, as the reference's NaN-derived code does). */
+void orc_compress(const float* in, int n, uint16_t* out, float* vmax, float* vmin)
+{
+    float mx = -1e20f, mn = 1e20f;
+    for (int i = 0; i < n; i++) {
+        mn = fminf(in[i], mn);
+        mx = fmaxf(in[i], mx);
+    }
+    *vmax = mx;
+    *vmin = mn;
+    for (int i = 0; i < n; i++) {
+        if (mx == mn) {
+            out[i] = 1;
+            continue;
+        }
+        float v = 1.0f + (float)(65535 - 1) * (in[i] - mn) / (mx - mn);
+        out[i] = (uint16_t)v;
+    }
+}
+
+static float decode_c(uint16_t c, float mn, float mx)
+{
+    /* eikonal_ani.cu:76-83 */
+    return (mn + ((float)c - 1.0f) * (mx - mn) / (float)(65535 - 1));
+}
+
+/* eikonal_ani.cu:47-111 */
+void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* Sin, int ldS,
+                       float dx, float dz, int sIdz, int sIdx_loc,
+                       const uint16_t* const codes[6], const float mm[12], float* Sout)
+{
+    for (int j = 0; j < ncols; j++)
+        for (int i = 0; i < nzz; i++) {
+            size_t is = (size_t)i + (size_t)j * ldS;
+            size_t it = (size_t)i + (size_t)j * nzz;
+            float s = Sin[is];
+            Sout[it] = s;
+            if (!((i >= nb) && (i < nzz - nb) && (j >= nb) && (j < ncols - nb))) continue;
+            if ((i == sIdz) && (j == sIdx_loc)) continue;
+            float dTz = 0.5f * (T[it + 1] - T[it - 1]) / dz;
+            float dTx = 0.5f * (T[it + nzz] - T[it - nzz]) / dx;
+            float norm = sqrtf(dTx * dTx + dTz * dTz);
+            float p0 = dTx / norm, p1 = dTz / norm;
+            float c11 = decode_c(codes[0][is], mm[0], mm[1]);
+            float c13 = decode_c(codes[1][is], mm[2], mm[3]);
+            float c15 = decode_c(codes[2][is], mm[4], mm[5]);
+            float c33 = decode_c(codes[3][is], mm[6], mm[7]);
+            float c35 = decode_c(codes[4][is], mm[8], mm[9]);
+            float c55 = decode_c(codes[5][is], mm[10], mm[11]);
+            float C[9];
+            C[0] = c11; C[3] = c13; C[6] = c15;
+            C[1] = c13; C[4] = c33; C[7] = c35;
+            C[2] = c15; C[5] = c35; C[8] = c55;
+            float Ro = c33 * s * s;
+            for (int q = 0; q < 9; q++) C[q] = C[q] / Ro / Ro;
+            float Gxx = C[0] * p0 * p0 + C[8] * p1 * p1 + 2.0f * C[6] * p0 * p1;
+            float Gzz = C[8] * p0 * p0 + C[4] * p1 * p1 + 2.0f * C[7] * p0 * p1;
+            float Gxz = C[6] * p0 * p0 + C[7] * p1 * p1 + (C[3] + C[8]) * p0 * p1;
+            float coeff1 = Gxx + Gzz;
+            float coeff2 = Gxx - Gzz;
+            float det = sqrtf((coeff2 * coeff2) / 4.0f + Gxz * Gxz);
+            /* coeff1 / 2.0 is a double expression in the reference */
+            float g0 = (float)((double)coeff1 / 2.0 + (double)det);
+            float g1 = (float)((double)coeff1 / 2.0 - (double)det);
+            if (g0 < g1) g0 = g1;
+            Sout[it] = 1.0f / sqrtf(g0 * Ro);
+        }
+}
+
+/* ------------------------------------------------------------------ picks */
+
+/* admin.cpp:121-133 */
+static float cubic1d(const float P[4], float t)
+{
+    return P[1] + 0.5f * t *
+                      (P[2] - P[0] +
+                       t * (2.0f * P[0] - 5.0f * P[1] + 4.0f * P[2] - P[3] +
+                            t * (3.0f * (P[1] - P[2]) + P[3] - P[0])));
+}
+
+static int pick_geom(float x, float z, float dx, float dz, int nb, int nzz, int ncols, int c0,
+                     int* pi, int* pj, float* pxd, float* pzd)
+{
+    /* modeling.cu:170-181 */
+    float x0 = floorf((x + 0.5f * dx) / dx) * dx;
+    float z0 = floorf((z + 0.5f * dz) / dz) * dz;
+    float x1 = floorf((x + 0.5f * dx) / dx) * dx + dx;
+    float z1 = floorf((z + 0.5f * dz) / dz) * dz + dz;
+    *pxd = (x - x0) / (x1 - x0);
+    *pzd = (z - z0) / (z1 - z0);
+    int i = (int)((z + 0.5f * dz) / dz) + nb;
+    int j = (int)((x + 0.5f * dx) / dx) + nb - c0;
+    *pi = i;
+    *pj = j;
+    if (i - 1 < 1 || i + 2 > nzz - 2 || j - 1 < 1 || j + 2 > ncols - 2) return -1;
+    return 0;
+}
+
+void orc_picks_f32(const float* T, int nzz, int ncols, int c0, float dx, float dz, int nb,
+                   const float* rx, const float* rz, int nrec, float* out)
+{
+    for (int r = 0; r < nrec; r++) {
+        int i, j;
+        float xd, zd;
+        if (pick_geom(rx[r], rz[r], dx, dz, nb, nzz, ncols, c0, &i, &j, &xd, &zd)) {
+            out[r] = NAN;
+            continue;
+        }
+        float P[4][4], p[4];
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++) P[a][b] = TAT(i + b - 1, j + a - 1);
+        for (int a = 0; a < 4; a++) p[a] = cubic1d(P[a], zd);
+        out[r] = cubic1d(p, xd);
+    }
+}
+
+static void cubic_w(double t, double w[4])
+{
+    /* cubic1d is linear in P: coefficients of P[0..3] */
+    w[0] = -0.5 * t + t * t - 0.5 * t * t * t;
+    w[1] = 1.0 - 2.5 * t * t + 1.5 * t * t * t;
+    w[2] = 0.5 * t + 2.0 * t * t - 1.5 * t * t * t;
+    w[3] = -0.5 * t * t + 0.5 * t * t * t;
+}
+
+int orc_pick_weights_f64(float x, float z, float dx, float dz, int nb, int nzz, int ncols, int c0,
+                         int* i, int* j, double w[16])
+{
+    float xd, zd;
+    if (pick_geom(x, z, dx, dz, nb, nzz, ncols, c0, i, j, &xd, &zd)) return -1;
+    double wx[4], wz[4];
+    cubic_w(xd, wx);
+    cubic_w(zd, wz);
+    for (int a = 0; a < 4; a++)
+        for (int b = 0; b < 4; b++) w[a * 4 + b] = wx[a] * wz[b];
+    return 0;
+}
+
+/* -------------------------------------------------------------- full shot */
+
+int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int c0, int ncols,
+                 float sx, float sz, int ani, const uint16_t* const codes[6], const float mm[12],
+                 float* T, const float* rx, const float* rz, int nrec, float* picks)
+{
+    int sIdx, sIdz;
+    orc_source_index(sx, sz, dx, dz, nb, &sIdx, &sIdz);
+    int sloc = sIdx - c0;
+    if (sIdz < 1 || sIdz > nzz - 2 || sloc < 1 || sloc > ncols - 2 || c0 < 0 || c0 + ncols > nxx)
+        return -1;
+    size_t n = (size_t)nzz * ncols;
+    float* Tw = T ? T : (float*)malloc(n * sizeof(float));
+    const float* Sw = S + (size_t)c0 * nzz;
+    double iv[9];
+    float init[9];
+    orc_init_block_f64(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, iv);
+    for (int q = 0; q < 9; q++) init[q] = (float)iv[q];
+    orc_solve_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sloc, init, Tw, 1, 1);
+    if (ani) {
+        float* Sq = (float*)malloc(n * sizeof(float));
+        const uint16_t* cw[6];
+        for (int c = 0; c < 6; c++) cw[c] = codes[c] + (size_t)c0 * nzz;
+        orc_qslowness_f32(nzz, ncols, nb, Tw, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
+        /* second initialisation reads the qP slowness (eikonal_ani.cu:40-41) */
+        for (int b = 0; b < 3; b++)
+            for (int a = 0; a < 3; a++) {
+                int zi = sIdz + a - 1, xl = sloc + b - 1;
+                double ddx = (double)(xl + c0 - nb) * (double)dx - (double)sx;
+                double ddz = (double)(zi - nb) * (double)dz - (double)sz;
+                init[a + 3 * b] = (float)((double)Sq[zi + (size_t)xl * nzz] * sqrt(ddx * ddx + ddz * ddz));
+            }
+        orc_solve_f32(nzz, ncols, Sq, nzz, dx, dz, sIdz, sloc, init, Tw, 1, 1);
+        free(Sq);
+    }
+    if (picks) orc_picks_f32(Tw, nzz, ncols, c0, dx, dz, nb, rx, rz, nrec, picks);
+    if (!T) free(Tw);
+    return 0;
+}
+
+int orc_batch_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots,
+                  const float* sx, const float* sz, const int* c0, const int* ncols, int ani,
+                  const uint16_t* const codes[6], const float mm[12], const float* rx,
+                  const float* rz, int nrec, float* picks, int nthreads)
+{
+    int used = 1;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (int b = 0; b < nshots; b++) {
+        orc_shot_f32(nzz, nxx, nb, S, dx, dz, c0[b], ncols[b], sx[b], sz[b], ani, codes, mm, NULL,
+                     rx, rz, nrec, picks + (size_t)b * nrec);
+    }
+#ifdef _OPENMP
+    used = nthreads;
+#endif
+    return used;
+}
+
+/* ---------------------------------------------------------------- adjoint */
+
+#define TP(k, i, j) (((size_t)(k) * ncols + (size_t)(j)) * nzz + (size_t)(i))
+
+void orc_solve_tape_f32(int nzz, int ncols, const float* S, int ldS, float dx, float dz, int sIdz,
+                        int sIdx_loc, const float init[9], float* T, uint8_t* code, float* c1,
+                        float* c2)
+{
+    k32 k = make_k32(dx, dz);
+    int si[4], sj[4];
+    orc_skip_cells(ncols, nzz, si, sj);
+    init_field_f32(T, nzz, ncols, sIdz, sIdx_loc, init);
+    memset(code, 0, (size_t)4 * ncols * nzz);
+    for (size_t n = 0; n < (size_t)4 * ncols * nzz; n++) c1[n] = c2[n] = 0.0f;
+    for (int s = 0; s < 4; s++) {
+        int sz, sx;
+        sweep_signs(s, &sz, &sx);
+        for (int jj = 1; jj <= ncols - 2; jj++) {
+            int j = (sx > 0) ? jj : ncols - 1 - jj;
+            for (int ii = 1; ii <= nzz - 2; ii++) {
+                int i = (sz > 0) ? ii : nzz - 1 - ii;
+                if (is_skip(s, i, j, si, sj)) continue;
+                rec_t r;
+                TAT(i, j) = node32(s, i, j, nzz, ncols, S, ldS, T, &k, &r);
+                code[TP(s, i, j)] = (uint8_t)r.code;
+                c1[TP(s, i, j)] = (float)r.c1;
+                c2[TP(s, i, j)] = (float)r.c2;
+            }
+        }
+    }
+}
+
+void orc_solve_tape_f64(int nzz, int ncols, const float* S, int ldS, double dx, double dz, int sIdz,
+                        int sIdx_loc, const double init[9], double* T, uint8_t* code, double* c1,
+                        double* c2)
+{
+    k64 k = make_k64(dx, dz);
+    int si[4], sj[4];
+    orc_skip_cells(ncols, nzz, si, sj);
+    init_field_f64(T, nzz, ncols, sIdz, sIdx_loc, init);
+    memset(code, 0, (size_t)4 * ncols * nzz);
+    for (size_t n = 0; n < (size_t)4 * ncols * nzz; n++) c1[n] = c2[n] = 0.0;
+    for (int s = 0; s < 4; s++) {
+        int sz, sx;
+        sweep_signs(s, &sz, &sx);
+        for (int jj = 1; jj <= ncols - 2; jj++) {
+            int j = (sx > 0) ? jj : ncols - 1 - jj;
+            for (int ii = 1; ii <= nzz - 2; ii++) {
+                int i = (sz > 0) ? ii : nzz - 1 - ii;
+                if (is_skip(s, i, j, si, sj)) continue;
+                rec_t r;
+                TAT(i, j) = node64(s, i, j, nzz, ncols, S, ldS, T, &k, &r);
+                code[TP(s, i, j)] = (uint8_t)r.code;
+                c1[TP(s, i, j)] = r.c1;
+                c2[TP(s, i, j)] = r.c2;
+            }
+        }
+    }
+}
+
+/*
+ * Reverse sweeps in pull form: for sweep k (signs sz, sx), node n = (i, j)
+ *   mu(n) = ((lam(n) + pv(i+sz, j)) + pe(i, j+sx)) + pev(i+sz, j+sx)
+ * where pv/pe/pev(d) = mu(d) * dT(d)/d{tv,te,tev}; then lam(n) = mu(n) if the
+ * node kept its old value (code 0), else 0, and the node's slowness term
+ * v = mu(n) * c2 goes to the cell named by the code. Cells gather their terms
+ * in the order sweep 0..3, corner (dr,dc) = (0,0),(0,1),(1,0),(1,1), then the
+ * 3x3 initialisation term lam_init * dist.
+ */
+#define ADJ_BODY(REAL)                                                                          \
+    size_t npl = (size_t)nzz * ncols;                                                           \
+    REAL* pv = (REAL*)calloc(npl, sizeof(REAL));                                                \
+    REAL* pe = (REAL*)calloc(npl, sizeof(REAL));                                                \
+    REAL* pev = (REAL*)calloc(npl, sizeof(REAL));                                               \
+    REAL* vr = (REAL*)calloc(4 * npl, sizeof(REAL));                                            \
+    for (int s = 3; s >= 0; s--) {                                                              \
+        int sz, sx;                                                                             \
+        sweep_signs(s, &sz, &sx);                                                               \
+        memset(pv, 0, npl * sizeof(REAL));                                                      \
+        memset(pe, 0, npl * sizeof(REAL));                                                      \
+        memset(pev, 0, npl * sizeof(REAL));                                                     \
+        for (int jj = ncols - 1; jj >= 0; jj--) {                                               \
+            int j = (sx > 0) ? jj : ncols - 1 - jj;                                             \
+            for (int ii = nzz - 1; ii >= 0; ii--) {                                             \
+                int i = (sz > 0) ? ii : nzz - 1 - ii;                                           \
+                REAL mu = lam[(size_t)i + (size_t)j * nzz];                                     \
+                int id = i + sz, jd = j + sx;                                                   \
+                if (id >= 0 && id < nzz) mu = mu + pv[(size_t)id + (size_t)j * nzz];            \
+                if (jd >= 0 && jd < ncols) mu = mu + pe[(size_t)i + (size_t)jd * nzz];          \
+                if (id >= 0 && id < nzz && jd >= 0 && jd < ncols)                               \
+                    mu = mu + pev[(size_t)id + (size_t)jd * nzz];                               \
+                int cd = code[TP(s, i, j)];                                                     \
+                int br = cd & 7;                                                                \
+                size_t here = (size_t)i + (size_t)j * nzz;                                      \
+                if (br == 0) {                                                                  \
+                    lam[here] = mu;                                                             \
+                    continue;                                                                   \
+                }                                                                               \
+                lam[here] = 0;                                                                  \
+                REAL a = c1[TP(s, i, j)];                                                       \
+                REAL one = 1;                                                                   \
+                switch (br) {                                                                   \
+                case 1: pv[here] = mu; break;                                                   \
+                case 2: pe[here] = mu; break;                                                   \
+                case 3: pv[here] = mu * a; pe[here] = mu * (-a); pev[here] = mu; break;         \
+                case 4: pe[here] = mu * (one - a); pev[here] = mu * a; break;                   \
+                default: pv[here] = mu * (one - a); pev[here] = mu * a; break;                  \
+                }                                                                               \
+                vr[(size_t)s * npl + here] = mu * c2[TP(s, i, j)];                              \
+            }                                                                                   \
+        }                                                                                       \
+    }                                                                                           \
+    for (int b = 0; b < ncols; b++)                                                             \
+        for (int a = 0; a < nzz; a++) {                                                         \
+            REAL g = grad[(size_t)a + (size_t)b * nzz];                                         \
+            for (int s = 0; s < 4; s++)                                                         \
+                for (int dr = 0; dr < 2; dr++)                                                  \
+                    for (int dc = 0; dc < 2; dc++) {                                            \
+                        int i = a + 1 - dr, j = b + 1 - dc;                                     \
+                        if (i >= nzz || j >= ncols) continue;                                   \
+                        int cd = code[TP(s, i, j)];                                             \
+                        if ((cd & 7) && ((cd >> 3) & 1) == dr && ((cd >> 4) & 1) == dc)         \
+                            g = g + vr[(size_t)s * npl + (size_t)i + (size_t)j * nzz];          \
+                    }                                                                           \
+            grad[(size_t)a + (size_t)b * nzz] = g;                                              \
+        }                                                                                       \
+    for (int b = 0; b < 3; b++)                                                                 \
+        for (int a = 0; a < 3; a++) {                                                           \
+            size_t n = (size_t)(sIdz + a - 1) + (size_t)(sIdx_loc + b - 1) * nzz;               \
+            grad[n] = grad[n] + lam[n] * (REAL)dist[a + 3 * b];                                 \
+        }                                                                                       \
+    free(pv);                                                                                   \
+    free(pe);                                                                                   \
+    free(pev);                                                                                  \
+    free(vr);
+
+void orc_adjoint_f32(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* code,
+                     const float* c1, const float* c2, const float dist[9], float* lam, float* grad)
+{
+    ADJ_BODY(float)
+}
+
+void orc_adjoint_f64(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* code,
+                     const double* c1, const double* c2, const double dist[9], double* lam,
+                     double* grad)
+{
+    ADJ_BODY(double)
+}

@@ -1,0 +1,279 @@
+"""ctypes view of the CPU oracle (test infrastructure: tests/, the smoke entry
+and the bench's CPU-baseline leg only).
+
+Arrays follow the reference's layout: a padded field of ``nzz`` rows (z) by
+``nxx`` columns (x) is stored z-fastest, i.e. a numpy array of shape
+``(nxx, nzz)`` in C order (``a[j, i]`` is row ``i``, column ``j``).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+IP = C.POINTER(C.c_int)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            path = _build.build()
+        L = C.CDLL(path)
+        L.orc_expand_boundary.argtypes = [f32p, C.c_int, C.c_int, C.c_int, f32p]
+        L.orc_reduce_boundary.argtypes = [f32p, C.c_int, C.c_int, C.c_int, f32p]
+        L.orc_skip_cells.argtypes = [C.c_int, C.c_int, i32p, i32p]
+        L.orc_source_index.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, IP, IP]
+        L.orc_init_block_f64.argtypes = [f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                         C.c_int, C.c_int, C.c_int, f64p]
+        L.orc_solve_f32.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_float, C.c_float, C.c_int,
+                                    C.c_int, f32p, f32p, C.c_int, C.c_int]
+        L.orc_solve_f64.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_double, C.c_double, C.c_int,
+                                    C.c_int, f64p, f64p, C.c_int, C.c_double, C.c_int]
+        L.orc_solve_f64.restype = C.c_int
+        L.orc_compress.argtypes = [f32p, C.c_int, u16p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_qslowness_f32.argtypes = [C.c_int, C.c_int, C.c_int, f32p, f32p, C.c_int, C.c_float,
+                                        C.c_float, C.c_int, C.c_int, C.c_void_p * 6, f32p, f32p]
+        L.orc_picks_f32.argtypes = [f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
+                                    f32p, f32p, C.c_int, f32p]
+        L.orc_shot_f32.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float, C.c_int,
+                                   C.c_int, C.c_float, C.c_float, C.c_int, C.c_void_p * 6, f32p,
+                                   C.c_void_p, f32p, f32p, C.c_int, C.c_void_p]
+        L.orc_shot_f32.restype = C.c_int
+        L.orc_batch_f32.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float, C.c_int,
+                                    f32p, f32p, i32p, i32p, C.c_int, C.c_void_p * 6, f32p, f32p,
+                                    f32p, C.c_int, f32p, C.c_int]
+        L.orc_batch_f32.restype = C.c_int
+        L.orc_solve_tape_f32.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_float, C.c_float,
+                                         C.c_int, C.c_int, f32p, f32p, u8p, f32p, f32p]
+        L.orc_solve_tape_f64.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_double, C.c_double,
+                                         C.c_int, C.c_int, f64p, f64p, u8p, f64p, f64p]
+        L.orc_adjoint_f32.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, u8p, f32p, f32p, f32p,
+                                      f32p, f32p]
+        L.orc_adjoint_f64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, u8p, f64p, f64p, f64p,
+                                      f64p, f64p]
+        L.orc_pick_weights_f64.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, IP, IP, f64p]
+        L.orc_pick_weights_f64.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def expand_boundary(model, nb=3):
+    """model: (nx, nz) float32 -> padded (nx+2nb, nz+2nb)."""
+    model = _f32(model)
+    nx, nz = model.shape
+    out = np.zeros((nx + 2 * nb, nz + 2 * nb), np.float32)
+    lib().orc_expand_boundary(model, nx, nz, nb, out)
+    return out
+
+
+def reduce_boundary(padded, nb=3):
+    padded = _f32(padded)
+    nxx, nzz = padded.shape
+    out = np.zeros((nxx - 2 * nb, nzz - 2 * nb), np.float32)
+    lib().orc_reduce_boundary(padded, nxx - 2 * nb, nzz - 2 * nb, nb, out)
+    return out
+
+
+def skip_cells(ncols, nzz):
+    si = np.zeros(4, np.int32)
+    sj = np.zeros(4, np.int32)
+    lib().orc_skip_cells(ncols, nzz, si, sj)
+    return si, sj
+
+
+def source_index(sx, sz, dx, dz, nb=3):
+    a, b = C.c_int(), C.c_int()
+    lib().orc_source_index(sx, sz, dx, dz, nb, C.byref(a), C.byref(b))
+    return a.value, b.value
+
+
+def init_block(S, sx, sz, dx, dz, nb=3):
+    S = _f32(S)
+    nzz = S.shape[1]
+    sIdx, sIdz = source_index(sx, sz, dx, dz, nb)
+    v = np.zeros(9, np.float64)
+    lib().orc_init_block_f64(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, v)
+    return v, sIdx, sIdz
+
+
+def solve_f32(S, dx, dz, sx, sz, nb=3, passes=1, order=1, c0=0, ncols=None):
+    """FP32 restatement of one isotropic solve on window [c0, c0+ncols)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ncols = nxx - c0 if ncols is None else ncols
+    v, sIdx, sIdz = init_block(S, sx, sz, dx, dz, nb)
+    init = v.astype(np.float32)
+    Sw = np.ascontiguousarray(S[c0:c0 + ncols])
+    T = np.zeros((ncols, nzz), np.float32)
+    lib().orc_solve_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0, init, T, passes, order)
+    return T
+
+
+def solve_f64(S, dx, dz, sx, sz, nb=3, passes=1, tol=0.0, max_passes=50, c0=0, ncols=None):
+    """FP64 solve: passes>0 runs that many passes; passes<=0 iterates to tol."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ncols = nxx - c0 if ncols is None else ncols
+    v, sIdx, sIdz = init_block(S, sx, sz, dx, dz, nb)
+    Sw = np.ascontiguousarray(S[c0:c0 + ncols])
+    T = np.zeros((ncols, nzz), np.float64)
+    n = lib().orc_solve_f64(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0, v, T, passes, tol,
+                            max_passes)
+    return T, n
+
+
+def compress(field):
+    """Quantise a padded field to uint16; returns (codes, vmin, vmax)."""
+    field = _f32(field)
+    out = np.zeros(field.shape, np.uint16)
+    mx, mn = C.c_float(), C.c_float()
+    lib().orc_compress(field.ravel(), field.size, out.ravel(), C.byref(mx), C.byref(mn))
+    return out, mn.value, mx.value
+
+
+def _codes_arg(codes):
+    arr = (C.c_void_p * 6)()
+    keep = []
+    for k in range(6):
+        c = np.ascontiguousarray(codes[k], dtype=np.uint16)
+        keep.append(c)
+        arr[k] = c.ctypes.data
+    return arr, keep
+
+
+def qslowness(T, S, dx, dz, sIdz, sIdx, codes, mm, nb=3):
+    T = _f32(T)
+    S = _f32(S)
+    ncols, nzz = T.shape
+    arr, keep = _codes_arg(codes)
+    out = np.zeros_like(T)
+    lib().orc_qslowness_f32(nzz, ncols, nb, T, S, nzz, dx, dz, sIdz, sIdx, arr,
+                            _f32(mm), out)
+    return out
+
+
+def picks(T, dx, dz, rx, rz, nb=3, c0=0):
+    T = _f32(T)
+    ncols, nzz = T.shape
+    rx, rz = _f32(rx), _f32(rz)
+    out = np.zeros(len(rx), np.float32)
+    lib().orc_picks_f32(T, nzz, ncols, c0, dx, dz, nb, rx, rz, len(rx), out)
+    return out
+
+
+def shot(S, dx, dz, sx, sz, rx=None, rz=None, nb=3, c0=0, ncols=None, ani=None, want_T=True):
+    """Full shot as the C-ABI runs it. ani: (codes[6], mm[12]) or None.
+    Returns (T or None, picks or None)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ncols = nxx - c0 if ncols is None else ncols
+    T = np.zeros((ncols, nzz), np.float32) if want_T else None
+    nrec = 0 if rx is None else len(rx)
+    pk = np.zeros(nrec, np.float32) if nrec else None
+    if ani is not None:
+        arr, keep = _codes_arg(ani[0])
+        mm = _f32(ani[1])
+    else:
+        arr, keep = (C.c_void_p * 6)(), []
+        mm = np.zeros(12, np.float32)
+    rxa = _f32(rx if nrec else np.zeros(1))
+    rza = _f32(rz if nrec else np.zeros(1))
+    rc = lib().orc_shot_f32(nzz, nxx, nb, S, dx, dz, c0, ncols, sx, sz, 1 if ani is not None else 0,
+                            arr, mm, T.ctypes.data if T is not None else None, rxa, rza, nrec,
+                            pk.ctypes.data if pk is not None else None)
+    if rc != 0:
+        raise ValueError("source outside the window")
+    return T, pk
+
+
+def batch_picks(S, dx, dz, sx, sz, c0, ncols, rx, rz, nb=3, ani=None, nthreads=0):
+    """CPU baseline: all shots, picks only. Returns (picks, threads_used)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ns = len(sx)
+    out = np.zeros((ns, len(rx)), np.float32)
+    if ani is not None:
+        arr, keep = _codes_arg(ani[0])
+        mm = _f32(ani[1])
+    else:
+        arr, keep = (C.c_void_p * 6)(), []
+        mm = np.zeros(12, np.float32)
+    used = lib().orc_batch_f32(nzz, nxx, nb, S, dx, dz, ns, _f32(sx), _f32(sz),
+                               np.ascontiguousarray(c0, np.int32),
+                               np.ascontiguousarray(ncols, np.int32), 1 if ani is not None else 0,
+                               arr, mm, _f32(rx), _f32(rz), len(rx), out, nthreads)
+    return out, used
+
+
+def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):
+    """Forward with tape. Returns (T, code, c1, c2, sIdz, sIdx_loc); tape arrays
+    have shape (4, ncols, nzz)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ncols = nxx - c0 if ncols is None else ncols
+    v, sIdx, sIdz = init_block(S, sx, sz, dx, dz, nb)
+    Sw = np.ascontiguousarray(S[c0:c0 + ncols])
+    code = np.zeros((4, ncols, nzz), np.uint8)
+    if fp64:
+        T = np.zeros((ncols, nzz), np.float64)
+        c1 = np.zeros((4, ncols, nzz), np.float64)
+        c2 = np.zeros_like(c1)
+        lib().orc_solve_tape_f64(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0, v, T, code, c1, c2)
+    else:
+        T = np.zeros((ncols, nzz), np.float32)
+        c1 = np.zeros((4, ncols, nzz), np.float32)
+        c2 = np.zeros_like(c1)
+        lib().orc_solve_tape_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0,
+                                 v.astype(np.float32), T, code, c1, c2)
+    return T, code, c1, c2, sIdz, sIdx - c0
+
+
+def init_dist(sx, sz, dx, dz, nb=3):
+    sIdx, sIdz = source_index(sx, sz, dx, dz, nb)
+    d = np.zeros(9)
+    for b in range(3):
+        for a in range(3):
+            zi, xi = sIdz + a - 1, sIdx + b - 1
+            ddx = float(xi - nb) * float(np.float32(dx)) - float(np.float32(sx))
+            ddz = float(zi - nb) * float(np.float32(dz)) - float(np.float32(sz))
+            d[a + 3 * b] = np.sqrt(ddx * ddx + ddz * ddz)
+    return d
+
+
+def adjoint(tape, lam, dist, fp64=False, grad=None):
+    """Reverse sweeps. tape = (code, c1, c2, sIdz, sIdx_loc); lam: adjoint of the
+    final T (ncols, nzz). Returns (grad, lam_init)."""
+    code, c1, c2, sIdz, sloc = tape
+    ncols, nzz = code.shape[1], code.shape[2]
+    dt = np.float64 if fp64 else np.float32
+    lam = np.ascontiguousarray(lam, dtype=dt).copy()
+    g = np.zeros((ncols, nzz), dt) if grad is None else np.ascontiguousarray(grad, dtype=dt)
+    fn = lib().orc_adjoint_f64 if fp64 else lib().orc_adjoint_f32
+    fn(nzz, ncols, sIdz, sloc, np.ascontiguousarray(code), np.ascontiguousarray(c1, dt),
+       np.ascontiguousarray(c2, dt), np.ascontiguousarray(dist, dt), lam, g)
+    return g, lam
+
+
+def pick_weights(x, z, dx, dz, nzz, ncols, nb=3, c0=0):
+    """Returns (i, j_local, w[4,4]) or None; w[a, b] weights node (i-1+b, j-1+a)."""
+    i, j = C.c_int(), C.c_int()
+    w = np.zeros(16)
+    rc = lib().orc_pick_weights_f64(x, z, dx, dz, nb, nzz, ncols, c0, C.byref(i), C.byref(j), w)
+    if rc:
+        return None
+    return i.value, j.value, w.reshape(4, 4)

@@ -1,0 +1,198 @@
+// Runs the reference's own modeling kernels (compiled from the reference
+// sources into cubins by build_ref.py) through the CUDA driver API, replaying
+// the reference's host launch sequence. TEST INFRASTRUCTURE ONLY: it is the
+// checker that pins the oracle and the engine to the reference's arithmetic.
+//
+// Host sequence restated from phbastosa/SeisFAT2D:
+//   Modeling::set_eikonal        src/modeling/modeling.cu:62-102 (sign tables)
+//   Modeling::initialization     src/modeling/modeling.cu:110-121
+//   Modeling::eikonal_solver     src/modeling/modeling.cu:123-159
+//   Eikonal_ANI::time_propagation src/modeling/eikonal_ani.cu:33-45
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace {
+CUmodule g_mod = nullptr, g_ani = nullptr;
+CUfunction f_set = nullptr, f_init = nullptr, f_sweep = nullptr, f_qs = nullptr;
+CUcontext g_ctx = nullptr;
+CUdevice g_dev = 0;
+
+#define DR(call)                                       \
+    do {                                               \
+        CUresult _r = (call);                          \
+        if (_r != CUDA_SUCCESS) {                      \
+            const char* s = nullptr;                   \
+            cuGetErrorString(_r, &s);                  \
+            fprintf(stderr, "%s: %s\n", #call, s ? s : "?"); \
+            return -(int)_r - 1000;                    \
+        }                                              \
+    } while (0)
+
+CUresult get_fn(CUmodule m, const char* const* names, CUfunction* f)
+{
+    CUresult r = CUDA_ERROR_NOT_FOUND;
+    for (int k = 0; names[k]; k++) {
+        r = cuModuleGetFunction(f, m, names[k]);
+        if (r == CUDA_SUCCESS) return r;
+    }
+    return r;
+}
+}  // namespace
+
+extern "C" int ref_open(const char* modeling_cubin, const char* ani_cubin, int device)
+{
+    DR(cuInit(0));
+    DR(cuDeviceGet(&g_dev, device));
+    DR(cuDevicePrimaryCtxRetain(&g_ctx, g_dev));
+    DR(cuCtxSetCurrent(g_ctx));
+    DR(cuModuleLoad(&g_mod, modeling_cubin));
+    DR(cuModuleLoad(&g_ani, ani_cubin));
+    const char* n_set[] = {"_Z8time_setPfi", nullptr};
+    const char* n_init[] = {"_Z9time_initPfS_ffffiiii", nullptr};
+    const char* n_sweep[] = {"_Z11inner_sweepPfS_PiS0_iiiiiiiiffff", nullptr};
+    const char* n_qs[] = {"_Z18get_quasi_slownessPfS_ffiiiiiPtS0_S0_S0_S0_S0_ffffffffffff", nullptr};
+    DR(get_fn(g_mod, n_set, &f_set));
+    DR(get_fn(g_mod, n_init, &f_init));
+    DR(get_fn(g_mod, n_sweep, &f_sweep));
+    DR(get_fn(g_ani, n_qs, &f_qs));
+    return 0;
+}
+
+extern "C" int ref_close()
+{
+    if (g_mod) cuModuleUnload(g_mod);
+    if (g_ani) cuModuleUnload(g_ani);
+    g_mod = g_ani = nullptr;
+    if (g_ctx) cuDevicePrimaryCtxRelease(g_dev);
+    g_ctx = nullptr;
+    return 0;
+}
+
+namespace {
+int initialization(CUdeviceptr dT, CUdeviceptr dS, int matsize, int nzz, int nb, float sx, float sz,
+                   float dx, float dz, int* sIdx_out, int* sIdz_out)
+{
+    int sIdx = (int)((sx + 0.5f * dx) / dx) + nb;
+    int sIdz = (int)((sz + 0.5f * dz) / dz) + nb;
+    *sIdx_out = sIdx;
+    *sIdz_out = sIdz;
+    int nBlocks = (matsize + 256 - 1) / 256;
+    void* a1[] = {&dT, &matsize};
+    DR(cuLaunchKernel(f_set, nBlocks, 1, 1, 256, 1, 1, 0, 0, a1, nullptr));
+    void* a2[] = {&dT, &dS, &sx, &sz, &dx, &dz, &sIdx, &sIdz, &nzz, &nb};
+    DR(cuLaunchKernel(f_init, 1, 1, 1, 3, 3, 1, 0, 0, a2, nullptr));
+    return 0;
+}
+
+int eikonal_solver(CUdeviceptr dT, CUdeviceptr dS, CUdeviceptr dsgnv, CUdeviceptr dsgnt, int nxx, int nzz,
+                   float dx, float dz)
+{
+    float dz2i = 1.0f / (dz * dz);
+    float dx2i = 1.0f / (dx * dx);
+    int total_levels = (nxx - 1) + (nzz - 1);
+    int min_level = std::min(nxx, nzz), max_level = std::max(nxx, nzz);
+    for (int sweep = 0; sweep < 4; sweep++) {
+        int zd = (sweep == 2 || sweep == 3) ? -1 : 1;
+        int xd = (sweep == 0 || sweep == 2) ? -1 : 1;
+        int sgni = sweep + 0 * 4;
+        int sgnj = sweep + 1 * 4;
+        for (int level = 0; level < total_levels; level++) {
+            int z_offset = (sweep == 0) ? ((level < nxx) ? 0 : level - nxx + 1)
+                         : (sweep == 1) ? ((level < nzz) ? nzz - level - 1 : 0)
+                         : (sweep == 2) ? ((level < nzz) ? level : nzz - 1)
+                                        : ((level < nxx) ? nzz - 1 : nzz - 1 - (level - nxx + 1));
+            int x_offset = (sweep == 0) ? ((level < nxx) ? level : nxx - 1)
+                         : (sweep == 1) ? ((level < nzz) ? 0 : level - nzz + 1)
+                         : (sweep == 2) ? ((level < nzz) ? nxx - 1 : nxx - 1 - (level - nzz + 1))
+                                        : ((level < nxx) ? nxx - level - 1 : 0);
+            int n_elements = (level < min_level) ? level + 1
+                           : (level >= max_level) ? total_levels - level
+                                                  : total_levels - min_level - max_level + level;
+            int nblk = (n_elements + 256 - 1) / 256;
+            void* a[] = {&dT, &dS, &dsgnv, &dsgnt, &sgni, &sgnj, &x_offset, &z_offset, &xd, &zd,
+                         &nxx, &nzz, &dx, &dz, &dx2i, &dz2i};
+            DR(cuLaunchKernel(f_sweep, nblk, 1, 1, 256, 1, 1, 0, 0, a, nullptr));
+        }
+    }
+    return 0;
+}
+}  // namespace
+
+// One shot on the padded grid (host buffers). ani != 0 runs the two-pass
+// anisotropic solve with the quantised codes. ms_out: GPU time of the
+// time_propagation sequence (CUDA events), excluding the copies.
+extern "C" int ref_solve(int nxx, int nzz, int nb, const float* S, float dx, float dz, float sx, float sz,
+                         int ani, const uint16_t* const* codes, const float* mm, float* T_out, double* ms_out,
+                         int repeats)
+{
+    DR(cuCtxSetCurrent(g_ctx));
+    const int matsize = nxx * nzz;
+    CUdeviceptr dT, dS, dsgnv, dsgnt;
+    CUdeviceptr dC[6] = {0, 0, 0, 0, 0, 0};
+    DR(cuMemAlloc(&dT, sizeof(float) * matsize));
+    DR(cuMemAlloc(&dS, sizeof(float) * matsize));
+    DR(cuMemAlloc(&dsgnv, sizeof(int) * 8));
+    DR(cuMemAlloc(&dsgnt, sizeof(int) * 8));
+    // modeling.cu:69-82: sgnv = {{1,1},{0,1},{1,0},{0,0}}, sgnt = {{1,1},{-1,1},{1,-1},{-1,-1}}
+    const int sgnv[4][2] = {{1, 1}, {0, 1}, {1, 0}, {0, 0}};
+    const int sgnt[4][2] = {{1, 1}, {-1, 1}, {1, -1}, {-1, -1}};
+    int hv[8], ht[8];
+    for (int index = 0; index < 8; index++) {
+        int j = index / 4, i = index % 4;
+        hv[i + j * 4] = sgnv[i][j];
+        ht[i + j * 4] = sgnt[i][j];
+    }
+    DR(cuMemcpyHtoD(dsgnv, hv, sizeof(hv)));
+    DR(cuMemcpyHtoD(dsgnt, ht, sizeof(ht)));
+    if (ani) {
+        for (int q = 0; q < 6; q++) {
+            DR(cuMemAlloc(&dC[q], sizeof(uint16_t) * matsize));
+            DR(cuMemcpyHtoD(dC[q], codes[q], sizeof(uint16_t) * matsize));
+        }
+    }
+    CUevent e0, e1;
+    DR(cuEventCreate(&e0, CU_EVENT_DEFAULT));
+    DR(cuEventCreate(&e1, CU_EVENT_DEFAULT));
+    double best = 1e30;
+    if (repeats < 1) repeats = 1;
+    for (int rep = 0; rep < repeats; rep++) {
+        DR(cuMemcpyHtoD(dS, S, sizeof(float) * matsize));
+        DR(cuCtxSynchronize());
+        DR(cuEventRecord(e0, 0));
+        int sIdx, sIdz, rc;
+        if ((rc = initialization(dT, dS, matsize, nzz, nb, sx, sz, dx, dz, &sIdx, &sIdz))) return rc;
+        if ((rc = eikonal_solver(dT, dS, dsgnv, dsgnt, nxx, nzz, dx, dz))) return rc;
+        if (ani) {
+            int nBlocks = (matsize + 256 - 1) / 256;
+            float m[12];
+            std::memcpy(m, mm, sizeof(m));  // (min, max) pairs C11..C55
+            void* a[] = {&dT, &dS, &dx, &dz, &sIdx, &sIdz, &nxx, &nzz, &nb,
+                         &dC[0], &dC[1], &dC[2], &dC[3], &dC[4], &dC[5],
+                         &m[0], &m[1], &m[2], &m[3], &m[4], &m[5], &m[6], &m[7], &m[8], &m[9], &m[10], &m[11]};
+            DR(cuLaunchKernel(f_qs, nBlocks, 1, 1, 256, 1, 1, 0, 0, a, nullptr));
+            if ((rc = initialization(dT, dS, matsize, nzz, nb, sx, sz, dx, dz, &sIdx, &sIdz))) return rc;
+            if ((rc = eikonal_solver(dT, dS, dsgnv, dsgnt, nxx, nzz, dx, dz))) return rc;
+        }
+        DR(cuEventRecord(e1, 0));
+        DR(cuEventSynchronize(e1));
+        float ms = 0.0f;
+        DR(cuEventElapsedTime(&ms, e0, e1));
+        best = std::min(best, (double)ms);
+    }
+    DR(cuMemcpyDtoH(T_out, dT, sizeof(float) * matsize));
+    if (ms_out) *ms_out = best;
+    cuEventDestroy(e0);
+    cuEventDestroy(e1);
+    cuMemFree(dT);
+    cuMemFree(dS);
+    cuMemFree(dsgnv);
+    cuMemFree(dsgnt);
+    for (int q = 0; q < 6; q++)
+        if (dC[q]) cuMemFree(dC[q]);
+    return 0;
+}

@@ -1,0 +1,52 @@
+"""Run the reference's own kernels (test infrastructure; see build_ref.py)."""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_ref
+
+_h = None
+
+
+def available():
+    return build_ref.available()
+
+
+def _handle(device=0):
+    global _h
+    if _h is None:
+        path = build_ref.build_harness()
+        h = C.CDLL(path)
+        h.ref_open.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+        h.ref_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                                C.c_float, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.POINTER(C.c_double), C.c_int]
+        rc = h.ref_open(build_ref.cubin_path("modeling").encode(),
+                        build_ref.cubin_path("eikonal_ani").encode(), device)
+        if rc != 0:
+            raise RuntimeError(f"ref_open failed ({rc})")
+        _h = h
+    return _h
+
+
+def solve(S_padded, dx, dz, sx, sz, ani=None, nb=3, repeats=1):
+    """Reference time_propagation on a padded (nxx, nzz) slowness.
+    ani: (codes[6] padded uint16, mm[12]) or None. Returns (T, ms)."""
+    h = _handle()
+    S = np.ascontiguousarray(S_padded, np.float32)
+    nxx, nzz = S.shape
+    T = np.zeros_like(S)
+    ms = C.c_double()
+    if ani is not None:
+        codes = [np.ascontiguousarray(c, np.uint16) for c in ani[0]]
+        arr = (C.c_void_p * 6)(*[c.ctypes.data for c in codes])
+        mm = np.ascontiguousarray(ani[1], np.float32)
+        cp, mp = C.cast(arr, C.c_void_p), C.c_void_p(mm.ctypes.data)
+    else:
+        cp, mp = None, None
+    rc = h.ref_solve(nxx, nzz, nb, C.c_void_p(S.ctypes.data), dx, dz, sx, sz, 1 if ani is not None else 0,
+                     cp, mp, C.c_void_p(T.ctypes.data), C.byref(ms), repeats)
+    if rc != 0:
+        raise RuntimeError(f"ref_solve failed ({rc})")
+    return T, ms.value

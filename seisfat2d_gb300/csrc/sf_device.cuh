@@ -1,0 +1,213 @@
+// Device-side building blocks of the GB300 eikonal engine: the per-node
+// fast-sweeping update, the anisotropic qP slowness, the receiver rule and the
+// FP64 near-source initialisation.
+//
+// Every FP32 operation is written with an explicit round-to-nearest intrinsic
+// (__fadd_rn, __fmul_rn, ...). Those are never contracted into FMAs, so the
+// result of each node is exactly the IEEE evaluation of the reference source
+// expression in source order (src/modeling/modeling.cu:319-356), independent
+// of compiler flags and identical to the CPU oracle built with
+// -ffp-contract=off.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sf {
+
+constexpr float kBig = 1e6f;  // time_set sentinel (modeling.cu:290)
+
+struct Consts {
+    float dx, dz;
+    float dx2i, dz2i;  // 1/(dx*dx), 1/(dz*dz) rounded as modeling.cu:64-65
+    float hyp;         // sqrtf(dx*dx + dz*dz)
+    float D;           // dz2i + dx2i
+    float K;           // dz2i * dx2i
+    float kA;          // dz2i - dx2i      (tape coefficient)
+    float k2K;         // 2 * (dz2i*dx2i)  (tape coefficient)
+};
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// Tape record of one node (adjoint bookkeeping; see the tape description in
+// include/seisfat2d.h). code bits 0-2 candidate, 3 row code, 4 column code.
+struct Rec {
+    uint8_t code;
+    float c1, c2;
+};
+
+// One node update. s1a/s1b: cells of the vertical upwind edge (row i1,
+// columns max(j-1,1) and j); s2a/s2b: cells of the horizontal edge (rows
+// max(i-1,1) and i, column j1); sref = S[i1][j1]. dr1/dc2 locate i1/j1 in the
+// 2x2 block around the node, dc1a/dr2a locate the clamped first cells.
+template <bool TAPE>
+__device__ __forceinline__ float node_update(float told, float tv, float te, float tev, float s1a,
+                                             float s1b, float s2a, float s2b, float sref,
+                                             const Consts& k, int dr1, int dc1a, int dc2, int dr2a,
+                                             Rec& rec)
+{
+    float m1 = fminf(s1a, s1b);
+    float m2 = fminf(s2a, s2b);
+    float t1d1 = fadd(tv, fmul(k.dz, m1));
+    float t1d2 = fadd(te, fmul(k.dx, m2));
+    float t1D = fminf(t1d1, t1d2);
+    float t1 = kBig, t2 = kBig, t3 = kBig;
+    float dte = fsub(te, tev);
+    float dtv = fsub(tv, tev);
+    int br = 0;
+    float rr = 0.0f, dd = 0.0f, q = 0.0f, qq = 0.0f;
+    if ((tv <= fadd(te, fmul(k.dx, sref))) && (te <= fadd(tv, fmul(k.dz, sref))) &&
+        (dte >= 0.0f) && (dtv >= 0.0f)) {
+        float ta = fsub(fadd(tev, te), tv);
+        float tb = fadd(fsub(tev, te), tv);
+        dd = fsub(ta, tb);
+        rr = fsqrt(fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd)));
+        t1 = fdiv(fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr), k.D);
+        br = 3;
+    } else if ((dte <= fdiv(fmul(fmul(sref, k.dz), k.dz), k.hyp)) && (dte > 0.0f)) {
+        q = fdiv(dte, k.dz);
+        qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
+        t2 = fadd(te, fmul(k.dx, qq));
+        br = 4;
+    } else if ((dtv <= fdiv(fmul(fmul(sref, k.dx), k.dx), k.hyp)) && (dtv > 0.0f)) {
+        q = fdiv(dtv, k.dx);
+        qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
+        t3 = fadd(tv, fmul(k.dz, qq));
+        br = 5;
+    }
+    float t2D = fminf(t1, fminf(t2, t3));
+    float cand = fminf(t1D, t2D);
+    float tnew = fminf(told, cand);
+    if (TAPE) {
+        rec.code = 0;
+        rec.c1 = 0.0f;
+        rec.c2 = 0.0f;
+        if (cand < told) {
+            if (t1D <= t2D) {
+                if (t1d1 <= t1d2) {
+                    int dc = (s1a <= s1b) ? dc1a : 1;
+                    rec.code = (uint8_t)(1 | (dr1 << 3) | (dc << 4));
+                    rec.c2 = k.dz;
+                } else {
+                    int dr = (s2a <= s2b) ? dr2a : 1;
+                    rec.code = (uint8_t)(2 | (dr << 3) | (dc2 << 4));
+                    rec.c2 = k.dx;
+                }
+            } else if (br != 0) {
+                rec.code = (uint8_t)(br | (dr1 << 3) | (dc2 << 4));
+                if (br == 3) {
+                    if (rr > 0.0f) {
+                        rec.c1 = fdiv(fadd(k.kA, fdiv(fmul(k.k2K, dd), rr)), k.D);
+                        rec.c2 = fdiv(fmul(4.0f, sref), rr);
+                    } else {
+                        rec.c1 = fdiv(k.kA, k.D);
+                    }
+                } else {
+                    float hx = (br == 4) ? k.dx : k.dz;
+                    float hq = (br == 4) ? k.dz : k.dx;
+                    if (qq > 0.0f) {
+                        rec.c1 = fdiv(fmul(hx, q), fmul(hq, qq));
+                        rec.c2 = fdiv(fmul(hx, sref), qq);
+                    }
+                }
+            }
+        }
+    }
+    return tnew;
+}
+
+// Near-source value of node (zi, xi) (global padded indices), FP64 then one
+// rounding: S * |x_node - x_src| (modeling.cu:293-306).
+__device__ __forceinline__ double src_dist(int zi, int xi, int nb, float dx, float dz, float sx,
+                                           float sz)
+{
+    double ddx = __dsub_rn(__dmul_rn((double)(xi - nb), (double)dx), (double)sx);
+    double ddz = __dsub_rn(__dmul_rn((double)(zi - nb), (double)dz), (double)sz);
+    return __dsqrt_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddz, ddz)));
+}
+
+// Catmull-Rom 1D rule of admin.cpp:121-124, each operation rounded once.
+__device__ __forceinline__ float cubic1d(float p0, float p1, float p2, float p3, float t)
+{
+    float inner = fsub(fadd(fmul(3.0f, fsub(p1, p2)), p3), p0);
+    float mid = fadd(fsub(fadd(fsub(fmul(2.0f, p0), fmul(5.0f, p1)), fmul(4.0f, p2)), p3),
+                     fmul(t, inner));
+    float outer = fadd(fsub(p2, p0), fmul(t, mid));
+    return fadd(p1, fmul(fmul(0.5f, t), outer));
+}
+
+// Receiver stencil geometry (modeling.cu:170-181). Returns false when the
+// 4x4 stencil leaves rows [1, nzz-2] or window columns [1, ncols-2].
+__device__ __forceinline__ bool pick_geom(float x, float z, float dx, float dz, int nb, int nzz,
+                                          int ncols, int c0, int& i, int& j, float& xd, float& zd)
+{
+    float ax = fdiv(fadd(x, fmul(0.5f, dx)), dx);
+    float az = fdiv(fadd(z, fmul(0.5f, dz)), dz);
+    float x0 = fmul(floorf(ax), dx);
+    float z0 = fmul(floorf(az), dz);
+    float x1 = fadd(fmul(floorf(ax), dx), dx);
+    float z1 = fadd(fmul(floorf(az), dz), dz);
+    xd = fdiv(fsub(x, x0), fsub(x1, x0));
+    zd = fdiv(fsub(z, z0), fsub(z1, z0));
+    i = __float2int_rz(az) + nb;
+    j = __float2int_rz(ax) + nb - c0;
+    return !(i - 1 < 1 || i + 2 > nzz - 2 || j - 1 < 1 || j + 2 > ncols - 2);
+}
+
+// cubic2d of admin.cpp:126-133 over the padded window T (column stride nzz).
+__device__ __forceinline__ float pick_value(const float* T, int nzz, int i, int j, float xd,
+                                            float zd)
+{
+    float p[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const float* col = T + (size_t)(j + a - 1) * nzz + (i - 1);
+        p[a] = cubic1d(col[0], col[1], col[2], col[3], zd);
+    }
+    return cubic1d(p[0], p[1], p[2], p[3], xd);
+}
+
+// Cij decompression (eikonal_ani.cu:76-83).
+__device__ __forceinline__ float decode_c(uint16_t c, float mn, float mx)
+{
+    return fadd(mn, fdiv(fmul(fsub((float)c, 1.0f), fsub(mx, mn)), 65534.0f));
+}
+
+// qP phase slowness of one node (eikonal_ani.cu:59-108). T, S: window
+// pointers at the node; codes already decoded.
+__device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, float txm, float s,
+                                             float dx, float dz, float c11, float c13, float c15,
+                                             float c33, float c35, float c55)
+{
+    float dTz = fdiv(fmul(0.5f, fsub(tzp, tzm)), dz);
+    float dTx = fdiv(fmul(0.5f, fsub(txp, txm)), dx);
+    float norm = fsqrt(fadd(fmul(dTx, dTx), fmul(dTz, dTz)));
+    float p0 = fdiv(dTx, norm), p1 = fdiv(dTz, norm);
+    float Ro = fmul(fmul(c33, s), s);
+    // C[q] / Ro / Ro
+    float C0 = fdiv(fdiv(c11, Ro), Ro);   // c11
+    float C3 = fdiv(fdiv(c13, Ro), Ro);   // c13
+    float C6 = fdiv(fdiv(c15, Ro), Ro);   // c15
+    float C4 = fdiv(fdiv(c33, Ro), Ro);   // c33
+    float C7 = fdiv(fdiv(c35, Ro), Ro);   // c35
+    float C8 = fdiv(fdiv(c55, Ro), Ro);   // c55
+    float Gxx = fadd(fadd(fmul(fmul(C0, p0), p0), fmul(fmul(C8, p1), p1)),
+                     fmul(fmul(fmul(2.0f, C6), p0), p1));
+    float Gzz = fadd(fadd(fmul(fmul(C8, p0), p0), fmul(fmul(C4, p1), p1)),
+                     fmul(fmul(fmul(2.0f, C7), p0), p1));
+    float Gxz = fadd(fadd(fmul(fmul(C6, p0), p0), fmul(fmul(C7, p1), p1)),
+                     fmul(fmul(fadd(C3, C8), p0), p1));
+    float coeff1 = fadd(Gxx, Gzz);
+    float coeff2 = fsub(Gxx, Gzz);
+    float det = fsqrt(fadd(fdiv(fmul(coeff2, coeff2), 4.0f), fmul(Gxz, Gxz)));
+    // coeff1 / 2.0 is a double expression in the reference
+    float g0 = __double2float_rn(__dadd_rn(__ddiv_rn((double)coeff1, 2.0), (double)det));
+    float g1 = __double2float_rn(__dsub_rn(__ddiv_rn((double)coeff1, 2.0), (double)det));
+    if (g0 < g1) g0 = g1;
+    return fdiv(1.0f, fsqrt(fmul(g0, Ro)));
+}
+
+}  // namespace sf

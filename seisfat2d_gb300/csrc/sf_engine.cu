@@ -1,0 +1,609 @@
+// C ABI of the GB300 eikonal engine (include/seisfat2d.h): context, buffers,
+// launches of the forward kernels. Compiled for sm_103a only.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/seisfat2d.h"
+#include "sf_engine.h"
+
+using namespace sf;
+
+// ------------------------------------------------------------------ helpers
+
+const char* sf_status_string(int s)
+{
+    switch (s) {
+    case SF_OK: return "ok";
+    case SF_ERR_ARG: return "invalid argument";
+    case SF_ERR_CUDA: return "CUDA error";
+    case SF_ERR_TIMEOUT: return "in-kernel wait timed out";
+    case SF_ERR_RANGE: return "source or window outside the grid";
+    case SF_ERR_STATE: return "call out of order";
+    case SF_ERR_NOMEM: return "device allocation failed";
+    default: return "unknown status";
+    }
+}
+
+int sf_fail(sf_ctx* c, int status, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return status;
+}
+
+int sf_cuda_check(sf_ctx* c, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return SF_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return sf_fail(c, SF_ERR_NOMEM, m);
+    return sf_fail(c, SF_ERR_CUDA, m);
+}
+
+#define CK(call)                                                          \
+    do {                                                                  \
+        int _st = sf_cuda_check(c, (call), #call);                        \
+        if (_st != SF_OK) return _st;                                     \
+    } while (0)
+
+int sf_dev_reserve(sf_ctx* c, void** p, size_t* cap, size_t bytes)
+{
+    if (bytes <= *cap && *p) return SF_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(p, want);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return sf_cuda_check(c, e, "cudaMalloc");
+    }
+    *cap = want;
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+
+namespace {
+
+// expand_boundary (modeling.cu:204-232): clamp-to-edge copy of the model.
+__global__ void k_expand(const float* __restrict__ in, int nx, int nz, int nb, float* __restrict__ out)
+{
+    const int nzz = nz + 2 * nb, nxx = nx + 2 * nb;
+    const size_t n = (size_t)nzz * nxx;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(idx % nzz), j = (int)(idx / nzz);
+        int si = min(max(i - nb, 0), nz - 1), sj = min(max(j - nb, 0), nx - 1);
+        out[idx] = in[si + (size_t)sj * nz];
+    }
+}
+
+// compute_seismogram on a device field (modeling.cu:161-194).
+__global__ void k_picks(const float* __restrict__ T, int nzz, int ncols, int c0, int nb, float dx,
+                        float dz, const float* __restrict__ rx, const float* __restrict__ rz,
+                        int nrec, float* __restrict__ out)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    int i, j;
+    float xd, zd;
+    float v = __int_as_float(0x7fc00000);
+    if (pick_geom(rx[r], rz[r], dx, dz, nb, nzz, ncols, c0, i, j, xd, zd))
+        v = pick_value(T, nzz, i, j, xd, zd);
+    out[r] = v;
+}
+
+}  // namespace
+
+size_t sf_fwd_smem_bytes(int warps)
+{
+    return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * sizeof(WarpRing);
+}
+
+// ------------------------------------------------------------------ context
+
+extern "C" const char* sf_ctx_last_error(const sf_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int sf_ctx_create(sf_ctx** out, int nx, int nz, float dx, float dz, int device)
+{
+    if (!out) return SF_ERR_ARG;
+    *out = nullptr;
+    if (nx < 2 || nz < 2 || !(dx > 0.0f) || !(dz > 0.0f)) return SF_ERR_ARG;
+    sf_ctx* c = new sf_ctx();
+    c->dev = device;
+    c->nx = nx;
+    c->nz = nz;
+    c->nb = 3;
+    c->nxx = nx + 2 * c->nb;
+    c->nzz = nz + 2 * c->nb;
+    c->dx = dx;
+    c->dz = dz;
+    Consts& k = c->kc;
+    k.dx = dx;
+    k.dz = dz;
+    k.dz2i = 1.0f / (dz * dz);  // modeling.cu:64-65 (host, no contraction)
+    k.dx2i = 1.0f / (dx * dx);
+    k.hyp = sqrtf(dx * dx + dz * dz);
+    k.D = k.dz2i + k.dx2i;
+    k.K = k.dz2i * k.dx2i;
+    k.kA = k.dz2i - k.dx2i;
+    k.k2K = 2.0f * k.K;
+    int st = sf_cuda_check(c, cudaSetDevice(device), "cudaSetDevice");
+    if (st == SF_OK) {
+        cudaDeviceProp prop;
+        st = sf_cuda_check(c, cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+        if (st == SF_OK) c->sms = prop.multiProcessorCount;
+    }
+    size_t cap = 0;
+    if (st == SF_OK) st = sf_dev_reserve(c, (void**)&c->d_S, &cap, sizeof(float) * (size_t)c->nxx * c->nzz);
+    cap = 0;
+    if (st == SF_OK) st = sf_dev_reserve(c, (void**)&c->d_flags, &cap, 256);
+    if (st == SF_OK) st = sf_cuda_check(c, cudaMemset(c->d_flags, 0, 256), "cudaMemset");
+    if (st == SF_OK) st = sf_fwd_setup(c);
+    if (st != SF_OK) {
+        sf_ctx_destroy(c);
+        return st;
+    }
+    *out = c;
+    return SF_OK;
+}
+
+extern "C" int sf_ctx_destroy(sf_ctx* c)
+{
+    if (!c) return SF_OK;
+    cudaSetDevice(c->dev);
+    sf_adjoint_release(c);
+    void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
+                    c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    delete c;
+    return SF_OK;
+}
+
+extern "C" int sf_ctx_dims(const sf_ctx* c, int* nxx, int* nzz, int* nb)
+{
+    if (!c) return SF_ERR_ARG;
+    if (nxx) *nxx = c->nxx;
+    if (nzz) *nzz = c->nzz;
+    if (nb) *nb = c->nb;
+    return SF_OK;
+}
+
+extern "C" int sf_set_launch(sf_ctx* c, int warps, int ctas_per_sm)
+{
+    if (!c) return SF_ERR_ARG;
+    if (warps && (warps < 2 || warps > kMaxWarps)) return sf_fail(c, SF_ERR_ARG, "warps must be 2..16");
+    if (ctas_per_sm && (ctas_per_sm < 1 || ctas_per_sm > 4))
+        return sf_fail(c, SF_ERR_ARG, "ctas_per_sm must be 1..4");
+    if (warps) c->warps = warps;
+    if (ctas_per_sm) c->ctas_per_sm = ctas_per_sm;
+    return SF_OK;
+}
+
+extern "C" int sf_get_launch(const sf_ctx* c, int* warps, int* ctas_per_sm)
+{
+    if (!c) return SF_ERR_ARG;
+    if (warps) *warps = c->warps;
+    if (ctas_per_sm) *ctas_per_sm = c->ctas_per_sm;
+    return SF_OK;
+}
+
+int sf_fwd_setup(sf_ctx* c)
+{
+    size_t mx = sf_fwd_smem_bytes(kMaxWarps);
+    CK(cudaFuncSetAttribute(k_shots<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_shots<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ models
+
+extern "C" int sf_set_slowness(sf_ctx* c, const float* s, int layout, int mem)
+{
+    if (!c || !s) return SF_ERR_ARG;
+    CK(cudaSetDevice(c->dev));
+    const size_t npad = (size_t)c->nxx * c->nzz;
+    if (layout == SF_LAYOUT_PADDED) {
+        CK(cudaMemcpy(c->d_S, s, npad * sizeof(float),
+                      mem == SF_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+        return SF_OK;
+    }
+    if (layout != SF_LAYOUT_MODEL) return sf_fail(c, SF_ERR_ARG, "unknown layout");
+    const size_t nm = (size_t)c->nx * c->nz;
+    int st = sf_dev_reserve(c, (void**)&c->d_model, &c->cap_model, nm * sizeof(float));
+    if (st) return st;
+    CK(cudaMemcpy(c->d_model, s, nm * sizeof(float),
+                  mem == SF_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    k_expand<<<std::min<size_t>((npad + 255) / 256, 4096), 256>>>(c->d_model, c->nx, c->nz, c->nb, c->d_S);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    return SF_OK;
+}
+
+extern "C" int sf_get_slowness(sf_ctx* c, float* out, int mem)
+{
+    if (!c || !out) return SF_ERR_ARG;
+    CK(cudaSetDevice(c->dev));
+    CK(cudaMemcpy(out, c->d_S, sizeof(float) * (size_t)c->nxx * c->nzz,
+                  mem == SF_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+    return SF_OK;
+}
+
+// Deterministic quantisation of one padded field (modeling.cu:264-279).
+static void compress_field(const float* in, size_t n, uint16_t* out, float* vmax, float* vmin)
+{
+    float mx = -1e20f, mn = 1e20f;
+    for (size_t i = 0; i < n; i++) {
+        mn = std::fmin(in[i], mn);
+        mx = std::fmax(in[i], mx);
+    }
+    *vmax = mx;
+    *vmin = mn;
+    for (size_t i = 0; i < n; i++) {
+        if (mx == mn) {
+            out[i] = 1;
+            continue;
+        }
+        float v = 1.0f + (float)(65535 - 1) * (in[i] - mn) / (mx - mn);
+        out[i] = (uint16_t)v;
+    }
+}
+
+static int upload_codes(sf_ctx* c, const uint16_t* const codes[6], int mem)
+{
+    const size_t npad = (size_t)c->nxx * c->nzz;
+    int st = sf_dev_reserve(c, (void**)&c->d_cij_all, &c->cap_cij, 6 * npad * sizeof(uint16_t));
+    if (st) return st;
+    for (int q = 0; q < 6; q++) {
+        CK(cudaMemcpy(c->d_cij_all + q * npad, codes[q], npad * sizeof(uint16_t),
+                      mem == SF_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    }
+    c->have_cij = true;
+    return SF_OK;
+}
+
+extern "C" int sf_set_stiffness(sf_ctx* c, const float* const cij[6], int mem)
+{
+    if (!c || !cij) return SF_ERR_ARG;
+    for (int q = 0; q < 6; q++)
+        if (!cij[q]) return SF_ERR_ARG;
+    CK(cudaSetDevice(c->dev));
+    const int nx = c->nx, nz = c->nz, nb = c->nb, nzz = c->nzz, nxx = c->nxx;
+    const size_t nm = (size_t)nx * nz, npad = (size_t)nxx * nzz;
+    std::vector<float> model(nm), padded(npad);
+    std::vector<std::vector<uint16_t>> codes(6, std::vector<uint16_t>(npad));
+    for (int q = 0; q < 6; q++) {
+        if (mem == SF_MEM_DEVICE) CK(cudaMemcpy(model.data(), cij[q], nm * sizeof(float), cudaMemcpyDeviceToHost));
+        else std::memcpy(model.data(), cij[q], nm * sizeof(float));
+        for (int j = 0; j < nxx; j++)
+            for (int i = 0; i < nzz; i++) {
+                int si = std::min(std::max(i - nb, 0), nz - 1), sj = std::min(std::max(j - nb, 0), nx - 1);
+                padded[i + (size_t)j * nzz] = model[si + (size_t)sj * nz];
+            }
+        compress_field(padded.data(), npad, codes[q].data(), &c->mm[2 * q + 1], &c->mm[2 * q]);
+    }
+    const uint16_t* ptrs[6];
+    for (int q = 0; q < 6; q++) ptrs[q] = codes[q].data();
+    return upload_codes(c, ptrs, SF_MEM_HOST);
+}
+
+extern "C" int sf_set_stiffness_codes(sf_ctx* c, const uint16_t* const codes[6], const float mm[12], int mem)
+{
+    if (!c || !codes || !mm) return SF_ERR_ARG;
+    for (int q = 0; q < 6; q++)
+        if (!codes[q]) return SF_ERR_ARG;
+    CK(cudaSetDevice(c->dev));
+    std::memcpy(c->mm, mm, sizeof(c->mm));
+    return upload_codes(c, codes, mem);
+}
+
+// ------------------------------------------------------------------ shots
+
+// Interior cells the reference's launch schedule (modeling.cu:123-159) never
+// updates, for a grid of nzz x ncols, per sweep: the middle-band thread count
+// (level-2) can fall one short of the diagonal when min(n)-2 is a multiple of
+// the 256-thread block.
+void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4])
+{
+    const int nxx = ncols, total = nxx + nzz - 2, mn = std::min(nxx, nzz), mxl = std::max(nxx, nzz);
+    for (int s = 0; s < 4; s++) {
+        si[s] = sj[s] = -1;
+        const int zd = (s == 2 || s == 3) ? -1 : 1;
+        const int xd = (s == 0 || s == 2) ? -1 : 1;
+        for (int level = 0; level < total; level++) {
+            int zo, xo;
+            switch (s) {
+            case 0: zo = (level < nxx) ? 0 : level - nxx + 1; xo = (level < nxx) ? level : nxx - 1; break;
+            case 1: zo = (level < nzz) ? nzz - level - 1 : 0; xo = (level < nzz) ? 0 : level - nzz + 1; break;
+            case 2: zo = (level < nzz) ? level : nzz - 1; xo = (level < nzz) ? nxx - 1 : nxx - 1 - (level - nzz + 1); break;
+            default: zo = (level < nxx) ? nzz - 1 : nzz - 1 - (level - nxx + 1); xo = (level < nxx) ? nxx - level - 1 : 0; break;
+            }
+            int n = (level < mn) ? level + 1 : (level >= mxl) ? total - level : total - mn - mxl + level;
+            int nl = ((n + 255) / 256) * 256;
+            int lo = 0, hi = 1 << 30;
+            if (zd > 0) { lo = std::max(lo, 1 - zo); hi = std::min(hi, nzz - 2 - zo); }
+            else { lo = std::max(lo, zo - (nzz - 2)); hi = std::min(hi, zo - 1); }
+            if (xd > 0) { lo = std::max(lo, 1 - xo); hi = std::min(hi, nxx - 2 - xo); }
+            else { lo = std::max(lo, xo - (nxx - 2)); hi = std::min(hi, xo - 1); }
+            for (int e = std::max(lo, nl); e <= hi; e++) {
+                si[s] = zo + zd * e;
+                sj[s] = xo + xd * e;
+            }
+        }
+    }
+}
+
+// Builds the device shot table (sorted widest window first for the work
+// queue). Returns SF_ERR_RANGE for a source outside its window.
+int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape)
+{
+    c->hshots.resize(nshots);
+    std::vector<int> order(nshots);
+    std::vector<std::pair<int, std::array<int, 8>>> skip_cache;
+    long long toff = 0, tape_off = 0;
+    const int nstrips = (c->nzz + 31) / 32;
+    int maxcols = 0;
+    for (int b = 0; b < nshots; b++) {
+        const sf_shot& s = shots[b];
+        ShotDev d;
+        std::memset(&d, 0, sizeof(d));
+        d.c0 = s.c0;
+        d.ncols = (s.ncols <= 0) ? c->nxx - s.c0 : s.ncols;
+        if (d.c0 < 0 || d.ncols < 3 || d.c0 + d.ncols > c->nxx)
+            return sf_fail(c, SF_ERR_RANGE, "shot " + std::to_string(b) + ": window outside the grid");
+        // modeling.cu:112-113 (host float arithmetic, no contraction)
+        float fx = (s.sx + 0.5f * c->dx) / c->dx;
+        float fz = (s.sz + 0.5f * c->dz) / c->dz;
+        if (!(fx > -1e9f && fx < 1e9f && fz > -1e9f && fz < 1e9f))
+            return sf_fail(c, SF_ERR_RANGE, "shot " + std::to_string(b) + ": source not finite");
+        d.sIdx = (int)fx + c->nb;
+        d.sIdz = (int)fz + c->nb;
+        d.sx = s.sx;
+        d.sz = s.sz;
+        const int sloc = d.sIdx - d.c0;
+        if (d.sIdz < 1 || d.sIdz > c->nzz - 2 || sloc < 1 || sloc > d.ncols - 2)
+            return sf_fail(c, SF_ERR_RANGE, "shot " + std::to_string(b) + ": source outside its window");
+        bool found = false;
+        for (auto& e : skip_cache)
+            if (e.first == d.ncols) {
+                for (int q = 0; q < 4; q++) { d.skip_i[q] = e.second[q]; d.skip_j[q] = e.second[4 + q]; }
+                found = true;
+                break;
+            }
+        if (!found) {
+            sf_skip_cells(d.ncols, c->nzz, d.skip_i, d.skip_j);
+            std::array<int, 8> v;
+            for (int q = 0; q < 4; q++) { v[q] = d.skip_i[q]; v[4 + q] = d.skip_j[q]; }
+            skip_cache.push_back({d.ncols, v});
+        }
+        d.orig = b;
+        d.t_off = toff;
+        if (keep_tables) toff += (long long)c->nzz * d.ncols;
+        d.tape_off = tape_off;
+        if (tape) tape_off += 4LL * nstrips * (d.ncols + 31) * 32;
+        maxcols = std::max(maxcols, d.ncols);
+        c->hshots[b] = d;
+    }
+    std::stable_sort(c->hshots.begin(), c->hshots.end(),
+                     [](const ShotDev& a, const ShotDev& b) { return a.ncols > b.ncols; });
+    c->batch_T_floats = toff;
+    c->batch_tape_entries = tape_off;
+    c->batch_maxcols = maxcols;
+    c->tables_index.assign(nshots, 0);
+    for (int q = 0; q < nshots; q++) c->tables_index[c->hshots[q].orig] = q;
+    return SF_OK;
+}
+
+int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape,
+                    int grid, cudaStream_t st)
+{
+    const int nshots = (int)c->hshots.size();
+    const size_t nzz = c->nzz;
+    int rc;
+    rc = sf_dev_reserve(c, (void**)&c->d_shots, &c->cap_shots, nshots * sizeof(ShotDev));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->d_shots, c->hshots.data(), nshots * sizeof(ShotDev), cudaMemcpyHostToDevice, st));
+    const long long t_per_cta = keep_tables ? 0 : (long long)nzz * c->batch_maxcols;
+    const size_t tfloats = keep_tables ? (size_t)c->batch_T_floats : (size_t)grid * t_per_cta;
+    rc = sf_dev_reserve(c, (void**)&c->d_T, &c->cap_T, tfloats * sizeof(float));
+    if (rc) return rc;
+    if (ani) {
+        rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)grid * nzz * c->batch_maxcols * sizeof(float));
+        if (rc) return rc;
+    }
+    if (tape) {
+        size_t n = (size_t)c->batch_tape_entries;
+        rc = sf_dev_reserve(c, (void**)&c->d_tcode, &c->cap_tcode, n);
+        if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc1, &c->cap_tc1, n * sizeof(float));
+        if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc2, &c->cap_tc2, n * sizeof(float));
+        if (rc) return rc;
+    }
+    FwdParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.S = c->d_S;
+    p.nzz = c->nzz;
+    p.nxx = c->nxx;
+    p.nb = c->nb;
+    p.kc = c->kc;
+    p.shots = c->d_shots;
+    p.nshots = nshots;
+    p.Tpool = c->d_T;
+    p.t_per_cta = t_per_cta;
+    p.counter = c->d_flags;          // flags[0]: work counter
+    p.err = c->d_flags + 1;          // flags[1]: error flag
+    p.ani = ani;
+    if (ani) {
+        const size_t npad = (size_t)c->nxx * c->nzz;
+        for (int q = 0; q < 6; q++) p.cij[q] = c->d_cij_all + q * npad;
+        std::memcpy(p.mm, c->mm, sizeof(p.mm));
+        p.Sq = c->d_Sq;
+        p.sq_per_cta = (long long)nzz * c->batch_maxcols;
+    }
+    if (tape) {
+        p.tcode = c->d_tcode;
+        p.tc1 = c->d_tc1;
+        p.tc2 = c->d_tc2;
+    }
+    p.rx = c->d_rx;
+    p.rz = c->d_rz;
+    p.nrec = nrec;
+    p.picks = d_picks;
+    CK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
+    const size_t smem = sf_fwd_smem_bytes(c->warps);
+    if (tape) k_shots<true><<<grid, c->warps * 32, smem, st>>>(p);
+    else k_shots<false><<<grid, c->warps * 32, smem, st>>>(p);
+    CK(cudaGetLastError());
+    c->tables_valid = keep_tables;
+    c->tape_valid = tape;
+    c->batch_nrec = nrec;
+    return SF_OK;
+}
+
+static int upload_receivers(sf_ctx* c, const float* rx, const float* rz, int nrec, cudaStream_t st)
+{
+    if (nrec <= 0) return SF_OK;
+    int rc = sf_dev_reserve(c, (void**)&c->d_rx, &c->cap_rx, nrec * sizeof(float));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_rz, &c->cap_rz, nrec * sizeof(float));
+    if (rc) return rc;
+    if (c->h_rx.size() == (size_t)nrec && std::equal(rx, rx + nrec, c->h_rx.begin()) &&
+        std::equal(rz, rz + nrec, c->h_rz.begin()))
+        return SF_OK;  // unchanged receivers stay on the device
+    c->h_rx.assign(rx, rx + nrec);
+    c->h_rz.assign(rz, rz + nrec);
+    CK(cudaMemcpyAsync(c->d_rx, c->h_rx.data(), nrec * sizeof(float), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_rz, c->h_rz.data(), nrec * sizeof(float), cudaMemcpyHostToDevice, st));
+    return SF_OK;
+}
+
+int sf_check_flags(sf_ctx* c, cudaStream_t st)
+{
+    CK(cudaStreamSynchronize(st));
+    int err = 0;
+    CK(cudaMemcpy(&err, c->d_flags + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        cudaMemset(c->d_flags + 1, 0, sizeof(int));
+        return sf_fail(c, SF_ERR_TIMEOUT, "an in-kernel wait gave up; results of the launch are void");
+    }
+    return SF_OK;
+}
+
+extern "C" int sf_synchronize(sf_ctx* c, void* stream)
+{
+    if (!c) return SF_ERR_ARG;
+    CK(cudaSetDevice(c->dev));
+    return sf_check_flags(c, (cudaStream_t)stream);
+}
+
+extern "C" int sf_batch_forward(sf_ctx* c, int ani, const sf_shot* shots, int nshots, const float* rx,
+                                const float* rz, int nrec, float* picks, int picks_mem, int flags,
+                                void* stream)
+{
+    if (!c || !shots || nshots <= 0 || nrec < 0 || (nrec > 0 && (!rx || !rz || !picks)))
+        return sf_fail(c, SF_ERR_ARG, "bad batch arguments");
+    if (ani && !c->have_cij) return sf_fail(c, SF_ERR_STATE, "anisotropic solve needs sf_set_stiffness");
+    const bool tape = (flags & SF_KEEP_TAPE) != 0, tables = (flags & SF_KEEP_TABLES) != 0;
+    if (ani && tape) return sf_fail(c, SF_ERR_ARG, "the adjoint tape is isotropic only");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    c->tape_valid = false;
+    c->tables_valid = false;
+    int rc = sf_prepare_shots(c, shots, nshots, tables, tape);
+    if (rc) return rc;
+    rc = upload_receivers(c, rx, rz, nrec, st);
+    if (rc) return rc;
+    float* dp = nullptr;
+    if (nrec > 0) {
+        if (picks_mem == SF_MEM_DEVICE) dp = picks;
+        else {
+            rc = sf_dev_reserve(c, (void**)&c->d_picks, &c->cap_picks, (size_t)nshots * nrec * sizeof(float));
+            if (rc) return rc;
+            dp = c->d_picks;
+        }
+    }
+    const int grid = std::max(1, std::min(nshots, c->sms * c->ctas_per_sm));
+    rc = sf_launch_shots(c, ani, nrec, dp, tables, tape, grid, st);
+    if (rc) return rc;
+    c->batch_nshots = nshots;
+    c->batch_picks = dp;
+    if (nrec > 0 && picks_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(picks, dp, (size_t)nshots * nrec * sizeof(float), cudaMemcpyDeviceToHost, st));
+        return sf_check_flags(c, st);
+    }
+    return SF_OK;
+}
+
+extern "C" int sf_batch_table(sf_ctx* c, int shot, float* T, int mem, void* stream)
+{
+    if (!c || !T) return SF_ERR_ARG;
+    if (!c->tables_valid) return sf_fail(c, SF_ERR_STATE, "last batch did not keep tables");
+    if (shot < 0 || shot >= (int)c->hshots.size()) return sf_fail(c, SF_ERR_ARG, "shot out of range");
+    CK(cudaSetDevice(c->dev));
+    const ShotDev& d = c->hshots[c->tables_index[shot]];
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(T, c->d_T + d.t_off, sizeof(float) * (size_t)c->nzz * d.ncols,
+                       mem == SF_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (mem == SF_MEM_HOST) return sf_check_flags(c, st);
+    return SF_OK;
+}
+
+extern "C" int sf_time_propagation(sf_ctx* c, int ani, float sx, float sz, float* T, int T_mem, void* stream)
+{
+    if (!c || !T) return sf_fail(c, SF_ERR_ARG, "null argument");
+    if (ani && !c->have_cij) return sf_fail(c, SF_ERR_STATE, "anisotropic solve needs sf_set_stiffness");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    sf_shot s{sx, sz, 0, c->nxx};
+    int rc = sf_prepare_shots(c, &s, 1, true, false);
+    if (rc) return rc;
+    const size_t npad = (size_t)c->nxx * c->nzz;
+    // the whole-grid table is written straight into the caller's device buffer
+    float* keepT = c->d_T;
+    size_t keepcap = c->cap_T;
+    if (T_mem == SF_MEM_DEVICE) {
+        c->d_T = T;
+        c->cap_T = npad * sizeof(float);
+    }
+    rc = sf_launch_shots(c, ani, 0, nullptr, true, false, 1, st);
+    if (T_mem == SF_MEM_DEVICE) {
+        c->d_T = keepT;
+        c->cap_T = keepcap;
+        c->tables_valid = false;
+    }
+    if (rc) return rc;
+    if (T_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(T, c->d_T, npad * sizeof(float), cudaMemcpyDeviceToHost, st));
+        return sf_check_flags(c, st);
+    }
+    return SF_OK;
+}
+
+extern "C" int sf_compute_seismogram(sf_ctx* c, const float* T_dev, const float* rx, const float* rz,
+                                     int nrec, float* picks, int picks_mem, void* stream)
+{
+    if (!c || !T_dev || nrec < 0 || (nrec > 0 && (!rx || !rz || !picks))) return SF_ERR_ARG;
+    if (nrec == 0) return SF_OK;
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = upload_receivers(c, rx, rz, nrec, st);
+    if (rc) return rc;
+    float* dp = picks;
+    if (picks_mem == SF_MEM_HOST) {
+        rc = sf_dev_reserve(c, (void**)&c->d_picks, &c->cap_picks, (size_t)nrec * sizeof(float));
+        if (rc) return rc;
+        dp = c->d_picks;
+    }
+    k_picks<<<(nrec + 127) / 128, 128, 0, st>>>(T_dev, c->nzz, c->nxx, 0, c->nb, c->dx, c->dz, c->d_rx,
+                                                c->d_rz, nrec, dp);
+    CK(cudaGetLastError());
+    if (picks_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(picks, dp, (size_t)nrec * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return SF_OK;
+}

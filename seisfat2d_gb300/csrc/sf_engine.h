@@ -1,0 +1,68 @@
+// Internal state of an engine context (not part of the public ABI).
+#pragma once
+#include <array>
+#include <string>
+#include <vector>
+
+#include "../../include/seisfat2d.h"
+#include "sf_forward.cuh"
+
+struct sf_ctx {
+    int dev = 0;
+    int nx = 0, nz = 0, nb = 3, nxx = 0, nzz = 0;
+    float dx = 0.0f, dz = 0.0f;
+    sf::Consts kc{};
+    int sms = 1;
+    int warps = 8;
+    int ctas_per_sm = 2;
+    std::string err;
+
+    float* d_S = nullptr;       // padded slowness
+    int* d_flags = nullptr;     // [0] work counter, [1] error flag, [2..] adjoint counters
+    float* d_model = nullptr;
+    size_t cap_model = 0;
+    uint16_t* d_cij_all = nullptr;  // six padded code fields
+    size_t cap_cij = 0;
+    float mm[12] = {};
+    bool have_cij = false;
+
+    // batch state
+    std::vector<sf::ShotDev> hshots;  // sorted widest first
+    std::vector<int> tables_index;    // caller index -> hshots index
+    long long batch_T_floats = 0, batch_tape_entries = 0;
+    int batch_maxcols = 0, batch_nshots = 0, batch_nrec = 0;
+    float* batch_picks = nullptr;
+    bool tables_valid = false, tape_valid = false;
+    std::vector<float> h_rx, h_rz;
+
+    sf::ShotDev* d_shots = nullptr; size_t cap_shots = 0;
+    float* d_T = nullptr; size_t cap_T = 0;
+    float* d_rx = nullptr; size_t cap_rx = 0;
+    float* d_rz = nullptr; size_t cap_rz = 0;
+    float* d_picks = nullptr; size_t cap_picks = 0;
+    float* d_Sq = nullptr; size_t cap_Sq = 0;
+    uint8_t* d_tcode = nullptr; size_t cap_tcode = 0;
+    float* d_tc1 = nullptr; size_t cap_tc1 = 0;
+    float* d_tc2 = nullptr; size_t cap_tc2 = 0;
+
+    // adjoint state
+    float* d_lam = nullptr; size_t cap_lam = 0;
+    float* d_vrec = nullptr; size_t cap_vrec = 0;
+    float* d_gshot = nullptr; size_t cap_gshot = 0;
+    float* d_pg = nullptr; size_t cap_pg = 0;
+    double* d_misfit = nullptr; size_t cap_misfit = 0;
+    int* d_colshots = nullptr; size_t cap_colshots = 0;
+    int* d_colptr = nullptr; size_t cap_colptr = 0;
+};
+
+int sf_fail(sf_ctx* c, int status, const std::string& msg);
+int sf_cuda_check(sf_ctx* c, cudaError_t e, const char* what);
+int sf_dev_reserve(sf_ctx* c, void** p, size_t* cap, size_t bytes);
+int sf_check_flags(sf_ctx* c, cudaStream_t st);
+int sf_fwd_setup(sf_ctx* c);
+size_t sf_fwd_smem_bytes(int warps);
+void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4]);
+int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape);
+int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int grid,
+                    cudaStream_t st);
+void sf_adjoint_release(sf_ctx* c);

@@ -1,0 +1,200 @@
+"""Python mirror of the engine's C ABI (used by the tests, the bench and the
+autograd wrapper). Every call goes through ``libseisfat2d.so``.
+
+Arrays use the reference layout: a padded field of ``nzz`` rows by ``nxx``
+columns, z fastest, is a ``(nxx, nzz)`` array (``a[j, i]`` = row i, column j);
+a model is ``(nx, nz)``. numpy arrays are host buffers, CUDA torch tensors are
+device buffers.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import (SF_KEEP_TABLES, SF_KEEP_TAPE, SF_LAYOUT_MODEL, SF_LAYOUT_PADDED, SF_MEM_DEVICE,
+                   SF_MEM_HOST, EngineError, sf_shot)
+
+try:  # torch is optional for host-buffer use
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_dev(a):
+    return torch is not None and isinstance(a, torch.Tensor) and a.is_cuda
+
+
+def _ptr(a, dtype=np.float32):
+    """(pointer, mem kind, keepalive) of a numpy array or torch tensor."""
+    if _is_dev(a):
+        if not a.is_contiguous():
+            raise ValueError("device tensor must be contiguous")
+        return C.c_void_p(a.data_ptr()), SF_MEM_DEVICE, a
+    if torch is not None and isinstance(a, torch.Tensor):
+        a = a.detach().numpy()
+    arr = np.ascontiguousarray(a, dtype=dtype)
+    return C.c_void_p(arr.ctypes.data), SF_MEM_HOST, arr
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if torch is not None and isinstance(stream, torch.cuda.Stream):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class Engine:
+    """One padded model grid on one device (``sf_ctx``)."""
+
+    def __init__(self, nx, nz, dx, dz, device=0):
+        self.L = _lib.load()
+        self._ctx = C.c_void_p()
+        st = self.L.sf_ctx_create(C.byref(self._ctx), int(nx), int(nz), float(dx), float(dz),
+                                  int(device))
+        if st != 0:
+            raise EngineError(st, "sf_ctx_create: " + self.L.sf_status_string(st).decode())
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self.L.sf_ctx_dims(self._ctx, C.byref(a), C.byref(b), C.byref(c))
+        self.nx, self.nz, self.dx, self.dz = int(nx), int(nz), float(dx), float(dz)
+        self.nxx, self.nzz, self.nb = a.value, b.value, c.value
+        self.device = device
+
+    def close(self):
+        if self._ctx:
+            self.L.sf_ctx_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.L.sf_ctx_last_error(self._ctx)
+            raise EngineError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    # -------------------------------------------------------------- models
+    def set_slowness(self, s, padded=False):
+        p, mem, keep = _ptr(s)
+        self._check(self.L.sf_set_slowness(self._ctx, p, SF_LAYOUT_PADDED if padded else SF_LAYOUT_MODEL,
+                                           mem), "sf_set_slowness")
+
+    def get_slowness(self):
+        out = np.zeros((self.nxx, self.nzz), np.float32)
+        self._check(self.L.sf_get_slowness(self._ctx, C.c_void_p(out.ctypes.data), SF_MEM_HOST),
+                    "sf_get_slowness")
+        return out
+
+    def set_stiffness(self, cij):
+        arr = (C.c_void_p * 6)()
+        keep = []
+        mem = None
+        for q in range(6):
+            p, m, k = _ptr(cij[q])
+            arr[q] = p.value
+            keep.append(k)
+            mem = m
+        self._check(self.L.sf_set_stiffness(self._ctx, arr, mem), "sf_set_stiffness")
+
+    def set_stiffness_codes(self, codes, minmax):
+        arr = (C.c_void_p * 6)()
+        keep = []
+        for q in range(6):
+            c = np.ascontiguousarray(codes[q], dtype=np.uint16)
+            keep.append(c)
+            arr[q] = c.ctypes.data
+        mm = np.ascontiguousarray(minmax, dtype=np.float32)
+        self._check(self.L.sf_set_stiffness_codes(self._ctx, arr, C.c_void_p(mm.ctypes.data),
+                                                  SF_MEM_HOST), "sf_set_stiffness_codes")
+
+    # -------------------------------------------------------------- per shot
+    def time_propagation(self, sx, sz, ani=False, out=None, stream=None):
+        """One shot on the whole grid; returns (nxx, nzz) traveltimes."""
+        if out is None:
+            out = np.zeros((self.nxx, self.nzz), np.float32)
+        p, mem, keep = _ptr(out)
+        self._check(self.L.sf_time_propagation(self._ctx, 1 if ani else 0, float(sx), float(sz), p, mem,
+                                               _stream_ptr(stream)), "sf_time_propagation")
+        return out
+
+    def compute_seismogram(self, T_dev, rx, rz, out=None, stream=None):
+        rx = np.ascontiguousarray(rx, np.float32)
+        rz = np.ascontiguousarray(rz, np.float32)
+        if out is None:
+            out = np.zeros(len(rx), np.float32)
+        p, mem, keep = _ptr(out)
+        self._check(self.L.sf_compute_seismogram(self._ctx, C.c_void_p(T_dev.data_ptr()),
+                                                 C.c_void_p(rx.ctypes.data), C.c_void_p(rz.ctypes.data),
+                                                 len(rx), p, mem, _stream_ptr(stream)),
+                    "sf_compute_seismogram")
+        return out
+
+    # -------------------------------------------------------------- batches
+    @staticmethod
+    def shot_table(shots):
+        """shots: iterable of (sx, sz) or (sx, sz, c0, ncols)."""
+        shots = list(shots)
+        arr = (sf_shot * len(shots))()
+        for k, s in enumerate(shots):
+            sx, sz = float(s[0]), float(s[1])
+            c0 = int(s[2]) if len(s) > 2 else 0
+            nc = int(s[3]) if len(s) > 3 else 0
+            arr[k] = sf_shot(sx, sz, c0, nc)
+        return arr
+
+    def batch_forward(self, shots, rx, rz, ani=False, keep_tape=False, keep_tables=False, out=None,
+                      stream=None):
+        """All shots in one persistent launch; returns picks (nshots, nrec)."""
+        tab = shots if isinstance(shots, C.Array) else self.shot_table(shots)
+        rx = np.ascontiguousarray(rx, np.float32)
+        rz = np.ascontiguousarray(rz, np.float32)
+        ns, nr = len(tab), len(rx)
+        if out is None:
+            out = np.zeros((ns, nr), np.float32)
+        p, mem, keep = _ptr(out)
+        flags = (SF_KEEP_TAPE if keep_tape else 0) | (SF_KEEP_TABLES if keep_tables else 0)
+        self._check(self.L.sf_batch_forward(self._ctx, 1 if ani else 0, tab, ns,
+                                            C.c_void_p(rx.ctypes.data), C.c_void_p(rz.ctypes.data), nr,
+                                            p, mem, flags, _stream_ptr(stream)), "sf_batch_forward")
+        return out
+
+    def batch_table(self, shot, ncols, out=None, stream=None):
+        if out is None:
+            out = np.zeros((ncols, self.nzz), np.float32)
+        p, mem, keep = _ptr(out)
+        self._check(self.L.sf_batch_table(self._ctx, int(shot), p, mem, _stream_ptr(stream)),
+                    "sf_batch_table")
+        return out
+
+    def batch_adjoint(self, pick_grad, out=None, stream=None):
+        if out is None:
+            out = np.zeros((self.nxx, self.nzz), np.float32)
+        pg, pmem, k1 = _ptr(pick_grad)
+        p, mem, k2 = _ptr(out)
+        self._check(self.L.sf_batch_adjoint(self._ctx, pg, pmem, p, mem, _stream_ptr(stream)),
+                    "sf_batch_adjoint")
+        return out
+
+    def misfit_gradient(self, t_obs, out=None, stream=None):
+        if out is None:
+            out = np.zeros((self.nxx, self.nzz), np.float32)
+        po, omem, k1 = _ptr(t_obs)
+        p, mem, k2 = _ptr(out)
+        mis = C.c_double()
+        self._check(self.L.sf_batch_misfit_gradient(self._ctx, po, omem, C.byref(mis), p, mem,
+                                                    _stream_ptr(stream)), "sf_batch_misfit_gradient")
+        return mis.value, out
+
+    def synchronize(self, stream=None):
+        self._check(self.L.sf_synchronize(self._ctx, _stream_ptr(stream)), "sf_synchronize")
+
+    def set_launch(self, warps=0, ctas_per_sm=0):
+        self._check(self.L.sf_set_launch(self._ctx, int(warps), int(ctas_per_sm)), "sf_set_launch")
+
+    def get_launch(self):
+        a, b = C.c_int(), C.c_int()
+        self.L.sf_get_launch(self._ctx, C.byref(a), C.byref(b))
+        return a.value, b.value

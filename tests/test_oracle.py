@@ -1,0 +1,174 @@
+"""CPU checks of the oracle itself: the restated launch schedule, the FP64
+modes, analytic known answers and the quantisation."""
+import numpy as np
+import pytest
+
+from helpers import layered, rel_err, smooth_model
+
+
+def coverage(nxx, nzz, nthreads=256):
+    """Which interior cells the reference's per-level launches reach
+    (modeling.cu:123-159, restated with numpy for the test)."""
+    total = nxx + nzz - 2
+    mn, mx = min(nxx, nzz), max(nxx, nzz)
+    res = []
+    for sweep in range(4):
+        zd = -1 if sweep in (2, 3) else 1
+        xd = -1 if sweep in (0, 2) else 1
+        cov = np.zeros((nzz, nxx), np.int32)
+        for level in range(total):
+            if sweep == 0:
+                zo = 0 if level < nxx else level - nxx + 1
+                xo = level if level < nxx else nxx - 1
+            elif sweep == 1:
+                zo = nzz - level - 1 if level < nzz else 0
+                xo = 0 if level < nzz else level - nzz + 1
+            elif sweep == 2:
+                zo = level if level < nzz else nzz - 1
+                xo = nxx - 1 if level < nzz else nxx - 1 - (level - nzz + 1)
+            else:
+                zo = nzz - 1 if level < nxx else nzz - 1 - (level - nxx + 1)
+                xo = nxx - level - 1 if level < nxx else 0
+            n = level + 1 if level < mn else (total - level if level >= mx else total - mn - mx + level)
+            e = np.arange(((n + nthreads - 1) // nthreads) * nthreads)
+            i, j = zo + zd * e, xo + xd * e
+            m = (i > 0) & (i < nzz - 1) & (j > 0) & (j < nxx - 1)
+            np.add.at(cov, (i[m], j[m]), 1)
+        res.append(cov)
+    return res
+
+
+@pytest.mark.parametrize("nxx,nzz", [(26, 16), (16, 26), (23, 23), (300, 258), (258, 300), (514, 258)])
+def test_skip_cells_match_launch_coverage(oracle, nxx, nzz):
+    si, sj = oracle.skip_cells(nxx, nzz)
+    cov = coverage(nxx, nzz)
+    for s in range(4):
+        inner = cov[s][1:-1, 1:-1]
+        assert inner.max() <= 1, "a level launch never updates a cell twice"
+        miss = np.argwhere(inner == 0) + 1
+        assert len(miss) <= 1
+        if len(miss):
+            assert (si[s], sj[s]) == tuple(miss[0])
+        else:
+            assert si[s] == -1 and sj[s] == -1
+    has_skip = (min(nxx, nzz) - 2) % 256 == 0
+    assert (si >= 0).any() == has_skip
+
+
+@pytest.mark.parametrize("nx,nz", [(40, 20), (20, 40), (57, 33), (252, 20), (20, 252)])
+def test_launch_order_equals_loop_order(oracle, nx, nz):
+    S = oracle.expand_boundary(smooth_model(nx, nz, 10.0, seed=nx + nz, noise=0.02))
+    for (sx, sz) in [(0.0, 0.0), ((nx - 1) * 10.0, (nz - 1) * 10.0), (nx * 4.3, nz * 6.1)]:
+        Ta = oracle.solve_f32(S, 10.0, 10.0, sx, sz, order=0)
+        Tb = oracle.solve_f32(S, 10.0, 10.0, sx, sz, order=1)
+        assert np.array_equal(Ta, Tb)
+
+
+def test_launch_order_equals_loop_order_with_skipped_cells(oracle):
+    nx, nz = 252, 30  # nzz = 36, nxx = 258: min-2 = 34 (no skip) -> use nzz = 258 below
+    S = oracle.expand_boundary(smooth_model(40, 252, 10.0, seed=3))  # nxx = 46, nzz = 258
+    si, sj = oracle.skip_cells(S.shape[0], S.shape[1])
+    assert (si < 0).all()
+    S = oracle.expand_boundary(smooth_model(300, 252, 10.0, seed=4))  # nzz = 258 -> skips
+    si, sj = oracle.skip_cells(S.shape[0], S.shape[1])
+    assert (si >= 0).all()
+    Ta = oracle.solve_f32(S, 10.0, 10.0, 1234.0, 20.0, order=0)
+    Tb = oracle.solve_f32(S, 10.0, 10.0, 1234.0, 20.0, order=1)
+    assert np.array_equal(Ta, Tb)
+
+
+def test_fp32_matches_fp64_schedule(oracle):
+    S = oracle.expand_boundary(smooth_model(201, 81, 10.0, seed=7))
+    T32 = oracle.solve_f32(S, 10.0, 10.0, 1000.0, 0.0)
+    T64, n = oracle.solve_f64(S, 10.0, 10.0, 1000.0, 0.0, passes=1)
+    assert n == 1
+    inner = (slice(3, -3), slice(3, -3))
+    assert rel_err(T32[inner], T64[inner]).max() < 1e-5
+
+
+def test_homogeneous_first_order_error_bound(oracle):
+    nx, nz, h, v = 121, 61, 10.0, 2000.0
+    S = oracle.expand_boundary(np.full((nx, nz), 1.0 / v, np.float32))
+    sx, sz = 600.0, 0.0
+    T, _ = oracle.solve_f64(S, h, h, sx, sz, passes=1)
+    x = (np.arange(nx + 6) - 3) * h
+    z = (np.arange(nz + 6) - 3) * h
+    Ta = np.hypot(x[:, None] - sx, z[None, :] - sz) / v
+    inner = (slice(3, -3), slice(3, -3))
+    err = np.abs(T[inner] - Ta[inner])
+    # first-order scheme: error grows like log(r) * h / v at most a few cells' time
+    assert err.max() < 4 * h / v
+    far = Ta[inner] > 20 * h / v
+    assert (err[far] / Ta[inner][far]).max() < 0.05
+
+
+def analytic_head_wave(v, z, x):
+    """Flat-layer refraction times (src/functions.py:23-33, restated)."""
+    out = np.zeros((len(z), len(x)))
+    for n in range(len(z)):
+        out[n] = x / v[n + 1]
+        for i in range(n + 1):
+            ang = np.arcsin(v[i] / v[n + 1])
+            out[n] += 2.0 * z[i] * np.cos(ang) / v[i]
+    return out
+
+
+def test_two_layer_head_wave(oracle):
+    nx, nz, h = 401, 61, 10.0
+    v = [1500.0, 3000.0]
+    S = oracle.expand_boundary(layered(nx, nz, h, v, [200.0]))
+    T, _ = oracle.solve_f64(S, h, h, 0.0, 0.0, passes=0, tol=0.0)
+    x = np.arange(nx) * h
+    head = analytic_head_wave(np.array(v), np.array([200.0]), x)[0]
+    direct = x / v[0]
+    first = np.minimum(head, direct)
+    Tsurf = T[3:-3, 3]
+    far = x > 1500.0
+    assert (np.abs(Tsurf[far] - first[far]) / first[far]).max() < 0.02
+
+
+def test_compress_deterministic_and_decodes_within_step(oracle):
+    rng = np.random.default_rng(0)
+    f = rng.uniform(1e9, 9e9, (50, 40)).astype(np.float32)
+    c1, mn1, mx1 = oracle.compress(f)
+    c2, mn2, mx2 = oracle.compress(f)
+    assert np.array_equal(c1, c2) and mn1 == mn2 and mx1 == mx2
+    assert mn1 == f.min() and mx1 == f.max()
+    dec = mn1 + (c1.astype(np.float32) - 1.0) * (mx1 - mn1) / 65534.0
+    assert np.abs(dec - f).max() <= (mx1 - mn1) / 65534.0 * 1.01
+    z = np.zeros((10, 10), np.float32)
+    cz, mnz, mxz = oracle.compress(z)
+    assert (cz == 1).all() and mnz == 0.0 and mxz == 0.0
+
+
+def numpy_cubic2d(T, i, j, xd, zd):
+    def c1d(P, t):
+        return P[1] + 0.5 * t * (P[2] - P[0] + t * (2 * P[0] - 5 * P[1] + 4 * P[2] - P[3] +
+                                                    t * (3 * (P[1] - P[2]) + P[3] - P[0])))
+    p = [c1d([T[j + a - 1, i + b - 1] for b in range(4)], zd) for a in range(4)]
+    return c1d(p, xd)
+
+
+def test_picks_match_independent_cubic(oracle):
+    S = oracle.expand_boundary(smooth_model(80, 40, 10.0, seed=9))
+    T = oracle.solve_f32(S, 10.0, 10.0, 300.0, 0.0)
+    rng = np.random.default_rng(1)
+    rx = rng.uniform(0, 790.0, 50).astype(np.float32)
+    rz = rng.uniform(0, 390.0, 50).astype(np.float32)
+    pk = oracle.picks(T, 10.0, 10.0, rx, rz)
+    for r in range(50):
+        i = int((rz[r] + 5.0) / 10.0) + 3
+        j = int((rx[r] + 5.0) / 10.0) + 3
+        x0 = np.floor((rx[r] + 5.0) / 10.0) * 10.0
+        z0 = np.floor((rz[r] + 5.0) / 10.0) * 10.0
+        ref = numpy_cubic2d(T.astype(np.float64), i, j, (rx[r] - x0) / 10.0, (rz[r] - z0) / 10.0)
+        assert abs(pk[r] - ref) <= 1e-5 * abs(ref) + 1e-6
+
+
+def test_window_solve_is_crop_solve(oracle):
+    S = oracle.expand_boundary(smooth_model(120, 40, 10.0, seed=5))
+    c0, nc = 30, 60
+    Tw = oracle.solve_f32(S, 10.0, 10.0, 600.0, 0.0, c0=c0, ncols=nc)
+    assert Tw.shape == (nc, S.shape[1])
+    T, pk = oracle.shot(S, 10.0, 10.0, 600.0, 0.0, c0=c0, ncols=nc)
+    assert np.array_equal(T, Tw)
