@@ -53,6 +53,10 @@ __device__ __forceinline__ size_t tape_strip_base(long long tape_off, int sweep,
     return (size_t)tape_off + ((size_t)sweep * nstrips + k) * (size_t)(ncols + 31) * 32;
 }
 
+// Position of strip p (p >= 1) among the strips fed through handoff channel
+// p % W: channel 0 carries W, 2W, ..., channel w > 0 carries w, w+W, ...
+__device__ __forceinline__ int chan_entry(int p, int W) { return p / W - ((p % W == 0) ? 1 : 0); }
+
 // The four sweeps of one solve on the window held by this CTA.
 template <bool TAPE>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float* Sw, int ldS,
@@ -91,10 +95,11 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float*
 #pragma unroll 1
         for (int pidx = warp; pidx < nstrips; pidx += W) {
             a.k = szpos ? pidx : nstrips - 1 - pidx;
+            // channel w carries strips p = w, w+W, ... (p >= 1) back to back
             a.w_in = (pidx > 0) ? warp : -1;
-            a.e_in = (pidx / W) * ncols;
+            a.e_in = chan_entry(pidx, W) * ncols;
             a.w_out = (pidx < nstrips - 1) ? (pidx + 1) % W : -1;
-            a.e_out = ((pidx + 1) / W) * ncols;
+            a.e_out = chan_entry(pidx + 1, W) * ncols;
             if (TAPE) {
                 size_t base = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
                 a.tcode = p.tcode + base;

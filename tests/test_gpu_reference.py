@@ -65,3 +65,53 @@ def test_anisotropic_matches_reference_kernels(oracle, engine_lib, cuda):
     err = rel_err(T, Tr).max()
     print(f"ANI: max rel diff vs reference kernels = {err:.3e}")
     assert err <= 1e-5
+
+
+def test_engine_matches_golden_vectors(oracle, engine_lib, cuda):
+    import glob
+    import os
+    from seisfat2d_gb300 import Engine
+    files = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz")))
+    assert files
+    for f in files:
+        d = np.load(f)
+        S = d["S"]
+        nxx, nzz = S.shape
+        e = Engine(nxx - 6, nzz - 6, float(d["dx"]), float(d["dz"]))
+        e.set_slowness(S, padded=True)
+        ani = "codes" in d
+        if ani:
+            e.set_stiffness_codes(list(d["codes"]), d["mm"])
+        T = e.time_propagation(float(d["sx"]), float(d["sz"]), ani=ani)
+        err = rel_err(T, d["T_ref"]).max()
+        print(os.path.basename(f), f"max rel diff vs reference kernels {err:.2e}")
+        assert err <= 1e-5
+
+
+def test_reference_solver_timing_config2(oracle, engine_lib, cuda):
+    """Times the reference's own per-shot solver (its kernels, its launch
+    sequence) and the engine's per-shot drop-in on the 2007 x 507 padded grid;
+    prints ms/shot for the record and checks the two agree to 1e-5."""
+    ref = _ref()
+    import time
+
+    from seisfat2d_gb300 import Engine
+    from seisfat2d_gb300.synthetic import config2
+    w = config2()
+    S = oracle.expand_boundary(w.slowness)
+    Tr, ms_ref = ref.solve(S, w.dx, w.dz, 10000.0, 0.0, repeats=3)
+    e = Engine(w.nx, w.nz, w.dx, w.dz)
+    e.set_slowness(w.slowness)
+    Td = cuda.empty((e.nxx, e.nzz), dtype=cuda.float32, device="cuda")
+    e.time_propagation(10000.0, 0.0, out=Td)
+    cuda.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        e.time_propagation(10000.0, 0.0, out=Td)
+    cuda.cuda.synchronize()
+    ms_ours = (time.perf_counter() - t0) / 3 * 1e3
+    T = Td.cpu().numpy()
+    err = rel_err(T, Tr).max()
+    print(f"\nREFERENCE_TIMING cfg2 2007x507: reference solver {ms_ref:.3f} ms/shot, "
+          f"engine per-shot drop-in {ms_ours:.3f} ms/shot, max rel diff {err:.2e}")
+    assert err <= 1e-5

@@ -172,3 +172,25 @@ def test_window_solve_is_crop_solve(oracle):
     assert Tw.shape == (nc, S.shape[1])
     T, pk = oracle.shot(S, 10.0, 10.0, 600.0, 0.0, c0=c0, ncols=nc)
     assert np.array_equal(T, Tw)
+
+
+def golden_cases():
+    import glob
+    import os
+    return sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: p.split("/")[-1][:-4])
+def test_oracle_matches_reference_kernel_golden_vectors(oracle, path):
+    """Golden vectors: the reference's own kernels run on a GB300 (see
+    tests/golden/make_golden.py). The reference contracts mul+add into FMAs and
+    initialises in FP32; the oracle rounds every operation and initialises in
+    FP64, so agreement is to the 1e-5 relative tolerance, not bitwise."""
+    d = np.load(path)
+    S, dx, dz, sx, sz = d["S"], float(d["dx"]), float(d["dz"]), float(d["sx"]), float(d["sz"])
+    if "codes" in d:
+        T, _ = oracle.shot(S, dx, dz, sx, sz, ani=(list(d["codes"]), d["mm"]))
+    else:
+        T = oracle.solve_f32(S, dx, dz, sx, sz, order=0)
+    assert rel_err(T, d["T_ref"]).max() <= 1e-5
+    assert len(golden_cases()) >= 7
