@@ -159,7 +159,7 @@ extern "C" int sf_ctx_destroy(sf_ctx* c)
     cudaSetDevice(c->dev);
     sf_adjoint_release(c);
     void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
-                    c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all};
+                    c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete c;
@@ -417,6 +417,9 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
         rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)grid * nzz * c->batch_maxcols * sizeof(float));
         if (rc) return rc;
     }
+    const long long hand_per_cta = (long long)((nzz + 31) / 32) * c->batch_maxcols;
+    rc = sf_dev_reserve(c, (void**)&c->d_hand, &c->cap_hand, (size_t)grid * hand_per_cta * sizeof(float));
+    if (rc) return rc;
     if (tape) {
         size_t n = (size_t)c->batch_tape_entries;
         rc = sf_dev_reserve(c, (void**)&c->d_tcode, &c->cap_tcode, n);
@@ -437,6 +440,8 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     p.t_per_cta = t_per_cta;
     p.counter = c->d_flags;          // flags[0]: work counter
     p.err = c->d_flags + 1;          // flags[1]: error flag
+    p.hand = c->d_hand;
+    p.hand_per_cta = hand_per_cta;
     p.ani = ani;
     if (ani) {
         const size_t npad = (size_t)c->nxx * c->nzz;

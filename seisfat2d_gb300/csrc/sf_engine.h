@@ -41,6 +41,7 @@ struct sf_ctx {
     float* d_rz = nullptr; size_t cap_rz = 0;
     float* d_picks = nullptr; size_t cap_picks = 0;
     float* d_Sq = nullptr; size_t cap_Sq = 0;
+    float* d_hand = nullptr; size_t cap_hand = 0;
     uint8_t* d_tcode = nullptr; size_t cap_tcode = 0;
     float* d_tc1 = nullptr; size_t cap_tc1 = 0;
     float* d_tc2 = nullptr; size_t cap_tc2 = 0;

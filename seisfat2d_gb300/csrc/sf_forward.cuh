@@ -30,6 +30,8 @@ struct FwdParams {
     long long t_per_cta;  // > 0: each CTA reuses Tpool + blockIdx.x * t_per_cta
     int* counter;
     int* err;
+    float* hand;          // strip handoff buffer, hand + blockIdx.x * hand_per_cta
+    long long hand_per_cta;  // >= nstrips * widest window
     // anisotropy
     int ani;
     const uint16_t* cij[6];
@@ -82,12 +84,10 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float*
     a.tcode = nullptr;
     a.tc1 = nullptr;
     a.tc2 = nullptr;
+    float* hb = p.hand + (size_t)blockIdx.x * p.hand_per_cta;
 #pragma unroll 1
     for (int sw = 0; sw < 4; sw++) {
-        if (threadIdx.x < kMaxWarps) {
-            cs->prod[threadIdx.x] = 0;
-            cs->cons[threadIdx.x] = 0;
-        }
+        if (threadIdx.x < kMaxWarps) cs->prod[threadIdx.x] = 0;
         __syncthreads();
         const bool szpos = !(sw == 1 || sw == 3);
         a.skip_i = sh.skip_i[sw];
@@ -100,6 +100,8 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float*
             a.e_in = chan_entry(pidx, W) * ncols;
             a.w_out = (pidx < nstrips - 1) ? (pidx + 1) % W : -1;
             a.e_out = chan_entry(pidx + 1, W) * ncols;
+            a.h_in = hb + (size_t)pidx * ncols;
+            a.h_out = hb + (size_t)(pidx + 1) * ncols;
             if (TAPE) {
                 size_t base = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
                 a.tcode = p.tcode + base;

@@ -7,8 +7,12 @@
 // values of the reference update (modeling.cu:324-326) are: the lane above's
 // result of the previous step (shfl), the lane's own previous result, and the
 // lane's own previous upwind value. Consecutive strips are chained through a
-// small shared-memory ring (the last lane of strip p feeds lane 0 of strip p+1)
-// with bounded spin waits.
+// per-CTA global buffer: the last lane of strip p writes its row, column by
+// column, and publishes a counter in shared memory; lane 0 of strip p+1
+// prefetches those values through the same cp.async pipeline as its own
+// columns (bounded spin on the counter). Producers never wait on consumers, so
+// every wait points to a lower strip and the schedule cannot deadlock however
+// many strips share a warp.
 //
 // Column chunks are staged into a per-warp shared-memory ring by cp.async:
 // at step s the warp fetches march column s+LOOK (32 consecutive rows = one
@@ -27,11 +31,11 @@ namespace sf {
 
 constexpr int kRing = 48;   // column slots per warp ring (>= 32 + kLook + 1)
 constexpr int kLook = 12;   // prefetch distance in march columns
-constexpr int kSP = 34;     // S slot pitch: rows rb-1 .. rb+32 (33 used)
+constexpr int kSP = 34;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff at 33
 constexpr int kTP = 32;     // T slot pitch
-constexpr int kHR = 64;     // handoff ring entries between consecutive strips
 constexpr int kMaxWarps = 16;
-constexpr long long kSpinLimit = 1ll << 26;
+constexpr long long kSpinLimit = 1ll << 30;          // iterations
+constexpr unsigned long long kSpinNs = 2000000000ull;  // and at most ~2 s
 
 struct WarpRing {
     float S[kRing * kSP];
@@ -41,9 +45,7 @@ struct WarpRing {
 // Per-CTA shared state (static part), followed by kMaxWarps WarpRing blocks in
 // dynamic shared memory (only the CTA's warps are used).
 struct CtaShared {
-    float hand[kMaxWarps][kHR];      // hand[w]: entries consumed by warp w
-    int prod[kMaxWarps];             // entries published into hand[w]
-    int cons[kMaxWarps];             // entries consumed from hand[w]
+    int prod[kMaxWarps];             // handoff entries published on channel w
     int abort_flag;
     int item;
     float init[9];
@@ -75,8 +77,10 @@ struct StripArgs {
     const float* init;  // 9 values in shared memory
     WarpRing* ring;
     CtaShared* sh;
-    int w_in, e_in;     // consumer side: ring index and entry base (-1: first strip)
+    int w_in, e_in;     // consumer side: channel and entry base (-1: first strip)
     int w_out, e_out;   // producer side (-1: last strip)
+    const float* h_in;  // handoff values of this strip's upwind row, by march column
+    float* h_out;       // handoff values this strip feeds to the next one
     // tape (TAPE only): base of this sweep/strip, entries [step*32 + lane]
     uint8_t* tcode;
     float* tc1;
@@ -84,12 +88,28 @@ struct StripArgs {
     int* err;
 };
 
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for *p >= target. On timeout it raises the CTA's abort flag and
+// the launch's error flag, and every later wait returns at once, so the
+// kernel always finishes (its results are then void and the host reports
+// SF_ERR_TIMEOUT).
 __device__ __forceinline__ bool spin_until(const int* p, int target, CtaShared* sh, int* err)
 {
+    if (ld_volatile(p) >= target) {
+        __threadfence_block();
+        return true;
+    }
+    const unsigned long long t0 = global_ns();
     long long n = 0;
     while (ld_volatile(p) < target) {
         if (ld_volatile(&sh->abort_flag)) return false;
-        if (++n > kSpinLimit) {
+        if (++n > kSpinLimit || ((n & 1023) == 0 && global_ns() - t0 > kSpinNs)) {
             st_volatile(&sh->abort_flag, 1);
             atomicExch(err, 2);
             return false;
@@ -126,6 +146,8 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     float* Tg = a.T;
     const size_t ldS = (size_t)a.ldS;
 
+    CtaShared* sh = a.sh;
+    const bool consumer = (lane == 0) && (a.w_in >= 0);
     auto col_of = [&](int m) { return (SX > 0) ? m : ncols - 1 - m; };
     auto prefetch = [&](int q, int slot) {
         if (q < ncols) {
@@ -134,6 +156,11 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             if (lx_ok) cp_async4(&Sring[slot * kSP + 32], Sg + (size_t)(rb + 31) + (size_t)jq * ldS);
             if (!SW0 && lt_ok)
                 cp_async4(&Tring[slot * kTP + lane], Tg + (size_t)(rb + lane) + (size_t)jq * nzz);
+            if (consumer) {
+                // upwind-row value of march q, once the previous strip has published it
+                spin_until(&sh->prod[a.w_in], a.e_in + q + 1, sh, a.err);
+                cp_async4(&Sring[slot * kSP + 33], a.h_in + q);
+            }
         }
         cp_commit();
     };
@@ -147,9 +174,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     int wb_slot = (kRing - 31) % kRing;                   // slot of march s-31
     float tn = 0.0f, tvp = 0.0f;                          // own last result, last upwind value
     float cU = 0.0f, cI = 0.0f;                           // carried S of rows r-1, r
-    int hand_seen = 0, cons_seen = 0;
     const int nsteps = ncols + 31;
-    CtaShared* sh = a.sh;
 
 #pragma unroll 1
     for (int s = 0; s < nsteps; s++) {
@@ -167,17 +192,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
         // upwind value from the lane above (or the previous strip)
         float tv = __shfl_up_sync(0xffffffffu, tn, 1);
-        if (lane == 0 && a.w_in >= 0 && s < ncols) {
-            const int e = a.e_in + s;
-            if (e >= hand_seen) {
-                if (spin_until(&sh->prod[a.w_in], e + 1, sh, a.err))
-                    hand_seen = ld_volatile(&sh->prod[a.w_in]);
-                else
-                    hand_seen = e + 1;
-            }
-            tv = *(volatile float*)&sh->hand[a.w_in][e % kHR];
-            st_volatile(&sh->cons[a.w_in], e + 1);
-        }
+        if (consumer) tv = Sring[m_slot * kSP + 33];
         const float te = tn, tev = tvp;
 
         float told;
@@ -222,16 +237,9 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
         // feed the next strip: lane 31 just finished march s-31
         if (lane == 31 && a.w_out >= 0 && act) {
-            const int e = a.e_out + m;
-            if (e - kHR >= cons_seen) {
-                if (spin_until(&sh->cons[a.w_out], e - kHR + 1, sh, a.err))
-                    cons_seen = ld_volatile(&sh->cons[a.w_out]);
-                else
-                    cons_seen = e;
-            }
-            *(volatile float*)&sh->hand[a.w_out][e % kHR] = tnew;
+            a.h_out[m] = tnew;
             __threadfence_block();
-            st_volatile(&sh->prod[a.w_out], e + 1);
+            st_volatile(&sh->prod[a.w_out], a.e_out + m + 1);
         }
 
         // write back the column every lane has finished

@@ -105,10 +105,10 @@ def test_batched_windows_equal_plain_per_window(oracle, engine_lib, cuda):
     shots = []
     for k in range(23):
         sx = float(rng.uniform(0, (nx - 1) * 10.0))
-        w = int(rng.integers(20, 200))
-        c0 = max(0, int(sx / 10.0) + 3 - w // 2)
-        nc = min(e.nxx - c0, w)
-        shots.append((sx, float(rng.uniform(0, 200.0)), c0, nc))
+        sidx = int((sx + 5.0) / 10.0) + 3
+        c0 = max(0, sidx - int(rng.integers(5, 120)))
+        c1 = min(e.nxx, sidx + int(rng.integers(5, 120)))
+        shots.append((sx, float(rng.uniform(0, 200.0)), c0, c1 - c0))
     shots.append((1500.0, 0.0, 0, 0))  # full width
     rx, rz = surface_receivers(nx, 10.0, step=2)
     pk = e.batch_forward(shots, rx, rz, keep_tables=True)
