@@ -41,6 +41,10 @@ extern "C" {
 #define SF_LAYOUT_MODEL 0  /* nz x nx, expanded to the padded grid on device */
 #define SF_LAYOUT_PADDED 1 /* nzz x nxx, taken as is                          */
 
+/* arithmetic of the FP32 sweeps (sf_set_arithmetic) */
+#define SF_ARITH_REFERENCE 0 /* the reference build's: FP32 init, nvcc's FMAs (default) */
+#define SF_ARITH_IEEE 1      /* every operation rounded once, FP64 3x3 initialisation */
+
 /* sf_batch_forward flags */
 #define SF_KEEP_TAPE 1   /* record the update tape for sf_batch_adjoint      */
 #define SF_KEEP_TABLES 2 /* keep every shot's traveltime window on device   */
@@ -119,6 +123,15 @@ int sf_batch_misfit_gradient(sf_ctx* ctx, const float* t_obs, int obs_mem, doubl
 
 /* Waits for `stream` and reports in-kernel failures (SF_ERR_TIMEOUT). */
 int sf_synchronize(sf_ctx* ctx, void* stream);
+
+/* FP32 arithmetic of the solves. SF_ARITH_REFERENCE reproduces the
+ * reference build of inner_sweep/time_init (modeling.cu:293-357 compiled by
+ * nvcc with its default FMA contraction): FP32 initialisation and fused
+ * multiply-adds for t1d1, t1d2, the 2D numerator and the discriminant.
+ * SF_ARITH_IEEE rounds every operation once and evaluates the 3x3
+ * initialisation in FP64. */
+int sf_set_arithmetic(sf_ctx* ctx, int mode);
+int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
 
 /* Launch shape: warps per CTA (4..16) and CTAs per SM for batches (1..4);
  * 0 keeps the current value. */

@@ -13,6 +13,9 @@
 #endif
 
 #define SF_BIG 1e6f
+
+static int g_arith = 0; /* see orc_set_arith */
+void orc_set_arith(int mode) { g_arith = mode; }
 #define NTHREADS_REF 256 /* modeling.cuh:11 */
 
 /* ---------------------------------------------------------------- padding */
@@ -137,6 +140,20 @@ void orc_init_block_f64(const float* S, int nzz, float sx, float sz, float dx, f
         }
 }
 
+/* modeling.cu:293-306 in the reference build's FP32 arithmetic
+ * (powf(v, 2.0f) taken as v*v). */
+void orc_init_block_f32(const float* S, int nzz, float sx, float sz, float dx, float dz, int nb,
+                           int sIdx, int sIdz, float vals[9])
+{
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) {
+            int zi = sIdz + a - 1, xi = sIdx + b - 1;
+            float X = (float)(xi - nb) * dx - sx;
+            float Z = (float)(zi - nb) * dz - sz;
+            vals[a + 3 * b] = S[zi + (size_t)xi * nzz] * sqrtf(X * X + Z * Z);
+        }
+}
+
 static void init_dist_f64(int nb, float sx, float sz, float dx, float dz, int sIdx, int sIdz,
                           double dist[9])
 {
@@ -201,8 +218,9 @@ static float upd32(float told, float tv, float te, float tev, float s1a, float s
 {
     float m1 = fminf(s1a, s1b);
     float m2 = fminf(s2a, s2b);
-    float t1d1 = tv + k->dz * m1;
-    float t1d2 = te + k->dx * m2;
+    const int ref = g_arith == 1;
+    float t1d1 = ref ? fmaf(k->dz, m1, tv) : tv + k->dz * m1;
+    float t1d2 = ref ? fmaf(k->dx, m2, te) : te + k->dx * m2;
     float t1D = fminf(t1d1, t1d2);
     float t1 = SF_BIG, t2 = SF_BIG, t3 = SF_BIG;
     int br = 0;
@@ -212,8 +230,14 @@ static float upd32(float told, float tv, float te, float tev, float s1a, float s
         float ta = tev + te - tv;
         float tb = tev - te + tv;
         dd = ta - tb;
-        rr = sqrtf(4.0f * sref * sref * (k->dz2i + k->dx2i) - k->dz2i * k->dx2i * dd * dd);
-        t1 = ((tb * k->dz2i + ta * k->dx2i) + rr) / (k->dz2i + k->dx2i);
+        if (ref) {
+            float kd = k->dz2i * k->dx2i * dd;
+            rr = sqrtf(fmaf(4.0f * sref * sref, (k->dz2i + k->dx2i), -(kd * dd)));
+            t1 = (fmaf(tb, k->dz2i, ta * k->dx2i) + rr) / (k->dz2i + k->dx2i);
+        } else {
+            rr = sqrtf(4.0f * sref * sref * (k->dz2i + k->dx2i) - k->dz2i * k->dx2i * dd * dd);
+            t1 = ((tb * k->dz2i + ta * k->dx2i) + rr) / (k->dz2i + k->dx2i);
+        }
         br = 3;
     } else if ((te - tev <= sref * k->dz * k->dz / k->hyp) && (te - tev > 0.0f)) {
         q = (te - tev) / k->dz;
@@ -534,7 +558,8 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
             if ((i == sIdz) && (j == sIdx_loc)) continue;
             float dTz = 0.5f * (T[it + 1] - T[it - 1]) / dz;
             float dTx = 0.5f * (T[it + nzz] - T[it - nzz]) / dx;
-            float norm = sqrtf(dTx * dTx + dTz * dTz);
+            const int ref = g_arith == 1;
+            float norm = sqrtf(ref ? fmaf(dTz, dTz, dTx * dTx) : dTx * dTx + dTz * dTz);
             float p0 = dTx / norm, p1 = dTz / norm;
             float c11 = decode_c(codes[0][is], mm[0], mm[1]);
             float c13 = decode_c(codes[1][is], mm[2], mm[3]);
@@ -548,9 +573,16 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
             C[2] = c15; C[5] = c35; C[8] = c55;
             float Ro = c33 * s * s;
             for (int q = 0; q < 9; q++) C[q] = C[q] / Ro / Ro;
-            float Gxx = C[0] * p0 * p0 + C[8] * p1 * p1 + 2.0f * C[6] * p0 * p1;
-            float Gzz = C[8] * p0 * p0 + C[4] * p1 * p1 + 2.0f * C[7] * p0 * p1;
-            float Gxz = C[6] * p0 * p0 + C[7] * p1 * p1 + (C[3] + C[8]) * p0 * p1;
+            float Gxx, Gzz, Gxz;
+            if (ref) { /* nvcc's FMAs: ((a p0) p0 + (b p1) p1) + (c p0) p1 -> fma(c p0, p1, fma(a p0, p0, (b p1) p1)) */
+                Gxx = fmaf(2.0f * C[6] * p0, p1, fmaf(C[0] * p0, p0, C[8] * p1 * p1));
+                Gzz = fmaf(2.0f * C[7] * p0, p1, fmaf(C[8] * p0, p0, C[4] * p1 * p1));
+                Gxz = fmaf((C[3] + C[8]) * p0, p1, fmaf(C[6] * p0, p0, C[7] * p1 * p1));
+            } else {
+                Gxx = C[0] * p0 * p0 + C[8] * p1 * p1 + 2.0f * C[6] * p0 * p1;
+                Gzz = C[8] * p0 * p0 + C[4] * p1 * p1 + 2.0f * C[7] * p0 * p1;
+                Gxz = C[6] * p0 * p0 + C[7] * p1 * p1 + (C[3] + C[8]) * p0 * p1;
+            }
             float coeff1 = Gxx + Gzz;
             float coeff2 = Gxx - Gzz;
             float det = sqrtf((coeff2 * coeff2) / 4.0f + Gxz * Gxz);
@@ -631,6 +663,54 @@ int orc_pick_weights_f64(float x, float z, float dx, float dz, int nb, int nzz, 
     return 0;
 }
 
+static void cubic_w_ops(double t, double w[4])
+{
+    double t2 = t * t, t3 = t2 * t;
+    w[0] = (-0.5 * t + t2) - 0.5 * t3;
+    w[1] = (1.0 - 2.5 * t2) + 1.5 * t3;
+    w[2] = (0.5 * t + 2.0 * t2) - 1.5 * t3;
+    w[3] = -0.5 * t2 + 0.5 * t3;
+}
+
+void orc_seed_lambda_f32(int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
+                         const float* rz, int nrec, const float* pg, float* lam)
+{
+    memset(lam, 0, sizeof(float) * (size_t)nzz * ncols);
+    for (int r = 0; r < nrec; r++) {
+        int i, j;
+        float xd, zd;
+        float g = pg[r];
+        if (pick_geom(rx[r], rz[r], dx, dz, nb, nzz, ncols, c0, &i, &j, &xd, &zd) || g != g) continue;
+        double wx[4], wz[4];
+        cubic_w_ops((double)xd, wx);
+        cubic_w_ops((double)zd, wz);
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++) {
+                float w = (float)(wx[a] * wz[b]);
+                float* at = lam + (size_t)(i + b - 1) + (size_t)(j + a - 1) * nzz;
+                *at = *at + g * w;
+            }
+    }
+}
+
+void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
+                         const float* rz, int nrec, const double* pg, double* lam)
+{
+    memset(lam, 0, sizeof(double) * (size_t)nzz * ncols);
+    for (int r = 0; r < nrec; r++) {
+        int i, j;
+        float xd, zd;
+        double g = pg[r];
+        if (pick_geom(rx[r], rz[r], dx, dz, nb, nzz, ncols, c0, &i, &j, &xd, &zd) || g != g) continue;
+        double wx[4], wz[4];
+        cubic_w_ops((double)xd, wx);
+        cubic_w_ops((double)zd, wz);
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++)
+                lam[(size_t)(i + b - 1) + (size_t)(j + a - 1) * nzz] += g * (wx[a] * wz[b]);
+    }
+}
+
 /* -------------------------------------------------------------- full shot */
 
 int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int c0, int ncols,
@@ -647,8 +727,12 @@ int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, i
     const float* Sw = S + (size_t)c0 * nzz;
     double iv[9];
     float init[9];
-    orc_init_block_f64(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, iv);
-    for (int q = 0; q < 9; q++) init[q] = (float)iv[q];
+    if (g_arith == 1) {
+        orc_init_block_f32(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, init);
+    } else {
+        orc_init_block_f64(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, iv);
+        for (int q = 0; q < 9; q++) init[q] = (float)iv[q];
+    }
     orc_solve_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sloc, init, Tw, 1, 1);
     if (ani) {
         float* Sq = (float*)malloc(n * sizeof(float));
@@ -659,9 +743,15 @@ int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, i
         for (int b = 0; b < 3; b++)
             for (int a = 0; a < 3; a++) {
                 int zi = sIdz + a - 1, xl = sloc + b - 1;
-                double ddx = (double)(xl + c0 - nb) * (double)dx - (double)sx;
-                double ddz = (double)(zi - nb) * (double)dz - (double)sz;
-                init[a + 3 * b] = (float)((double)Sq[zi + (size_t)xl * nzz] * sqrt(ddx * ddx + ddz * ddz));
+                if (g_arith == 1) {
+                    float X = (float)(xl + c0 - nb) * dx - sx;
+                    float Z = (float)(zi - nb) * dz - sz;
+                    init[a + 3 * b] = Sq[zi + (size_t)xl * nzz] * sqrtf(X * X + Z * Z);
+                } else {
+                    double ddx = (double)(xl + c0 - nb) * (double)dx - (double)sx;
+                    double ddz = (double)(zi - nb) * (double)dz - (double)sz;
+                    init[a + 3 * b] = (float)((double)Sq[zi + (size_t)xl * nzz] * sqrt(ddx * ddx + ddz * ddz));
+                }
             }
         orc_solve_f32(nzz, ncols, Sq, nzz, dx, dz, sIdz, sloc, init, Tw, 1, 1);
         free(Sq);

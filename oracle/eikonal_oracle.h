@@ -44,6 +44,10 @@ void orc_source_index(float sx, float sz, float dx, float dz, int nb, int* sIdx,
 void orc_init_block_f64(const float* S, int nzz, float sx, float sz, float dx, float dz,
                         int nb, int sIdx, int sIdz, double vals[9]);
 
+/* The same in the reference build's FP32 arithmetic (orc_set_arith(1)). */
+void orc_init_block_f32(const float* S, int nzz, float sx, float sz, float dx, float dz, int nb,
+                        int sIdx, int sIdz, float vals[9]);
+
 /* One solve on a window of the padded grid: nzz rows x ncols columns.
  * S: slowness of the window, column stride ldS. T: output, column stride nzz.
  * sIdz / sIdx_loc: source node inside the window; init: 9 FP32 values.
@@ -121,6 +125,21 @@ void orc_adjoint_f32(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* 
 void orc_adjoint_f64(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* code,
                      const double* c1, const double* c2, const double dist[9], double* lam,
                      double* grad);
+
+/* Adjoint seed of one shot window from pick gradients pg[nrec] (NaN = no
+ * pick), receivers in order, 16 taps each: lam[node] += pg * w, w the
+ * Catmull-Rom weight product (FP64 weights, t^2 = t*t, t^3 = t^2*t, rounded
+ * once to FP32 in the _f32 variant). lam is zeroed first. */
+void orc_seed_lambda_f32(int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
+                         const float* rz, int nrec, const float* pg, float* lam);
+void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
+                         const float* rz, int nrec, const double* pg, double* lam);
+
+/* Arithmetic of the FP32 solvers: 0 = every operation rounded once and the
+ * 3x3 initialisation in FP64 (default); 1 = the reference build's arithmetic:
+ * FP32 initialisation and fused multiply-adds where nvcc forms them in
+ * inner_sweep (t1d1, t1d2, the 2D numerator and discriminant). */
+void orc_set_arith(int mode);
 
 /* Catmull-Rom weights of the pick rule: w[16], node (i-1+b, j-1+a) -> w[a*4+b]
  * (a along x, b along z); i, j padded node of the receiver; returns 0 when the

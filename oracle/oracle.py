@@ -64,8 +64,26 @@ def lib():
         L.orc_pick_weights_f64.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                                            C.c_int, C.c_int, C.c_int, IP, IP, f64p]
         L.orc_pick_weights_f64.restype = C.c_int
+        L.orc_init_block_f32.argtypes = [f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                         C.c_int, C.c_int, C.c_int, f32p]
+        L.orc_set_arith.argtypes = [C.c_int]
+        L.orc_seed_lambda_f32.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
+                                          f32p, f32p, C.c_int, f32p, f32p]
+        L.orc_seed_lambda_f64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
+                                          f32p, f32p, C.c_int, f64p, f64p]
         _lib = L
     return _lib
+
+
+_arith = 0
+
+
+def set_arith(mode):
+    """'ieee' (every operation rounded once, FP64 init) or 'reference' (the
+    reference build's FP32 init and FMAs)."""
+    global _arith
+    _arith = {"ieee": 0, "reference": 1}[mode] if isinstance(mode, str) else int(mode)
+    lib().orc_set_arith(_arith)
 
 
 def _f32(a):
@@ -111,13 +129,24 @@ def init_block(S, sx, sz, dx, dz, nb=3):
     return v, sIdx, sIdz
 
 
+def init_block_f32(S, sx, sz, dx, dz, nb=3):
+    """The 9 FP32 initial values of the current arithmetic mode."""
+    S = _f32(S)
+    if _arith == 1:
+        sIdx, sIdz = source_index(sx, sz, dx, dz, nb)
+        v = np.zeros(9, np.float32)
+        lib().orc_init_block_f32(S, S.shape[1], sx, sz, dx, dz, nb, sIdx, sIdz, v)
+        return v, sIdx, sIdz
+    v, sIdx, sIdz = init_block(S, sx, sz, dx, dz, nb)
+    return v.astype(np.float32), sIdx, sIdz
+
+
 def solve_f32(S, dx, dz, sx, sz, nb=3, passes=1, order=1, c0=0, ncols=None):
     """FP32 restatement of one isotropic solve on window [c0, c0+ncols)."""
     S = _f32(S)
     nxx, nzz = S.shape
     ncols = nxx - c0 if ncols is None else ncols
-    v, sIdx, sIdz = init_block(S, sx, sz, dx, dz, nb)
-    init = v.astype(np.float32)
+    init, sIdx, sIdz = init_block_f32(S, sx, sz, dx, dz, nb)
     Sw = np.ascontiguousarray(S[c0:c0 + ncols])
     T = np.zeros((ncols, nzz), np.float32)
     lib().orc_solve_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0, init, T, passes, order)
@@ -238,8 +267,8 @@ def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):
         T = np.zeros((ncols, nzz), np.float32)
         c1 = np.zeros((4, ncols, nzz), np.float32)
         c2 = np.zeros_like(c1)
-        lib().orc_solve_tape_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0,
-                                 v.astype(np.float32), T, code, c1, c2)
+        init, _, _ = init_block_f32(S, sx, sz, dx, dz, nb)
+        lib().orc_solve_tape_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0, init, T, code, c1, c2)
     return T, code, c1, c2, sIdz, sIdx - c0
 
 
@@ -277,3 +306,47 @@ def pick_weights(x, z, dx, dz, nzz, ncols, nb=3, c0=0):
     if rc:
         return None
     return i.value, j.value, w.reshape(4, 4)
+
+
+def seed_lambda(ncols, nzz, dx, dz, rx, rz, pg, c0=0, nb=3, fp64=False):
+    """Adjoint seed of one shot window from its pick gradients (receivers in
+    order, the engine's tap order and rounding)."""
+    rx, rz = _f32(rx), _f32(rz)
+    if fp64:
+        lam = np.zeros((ncols, nzz), np.float64)
+        lib().orc_seed_lambda_f64(nzz, ncols, c0, dx, dz, nb, rx, rz, len(rx),
+                                  np.ascontiguousarray(pg, np.float64), lam)
+    else:
+        lam = np.zeros((ncols, nzz), np.float32)
+        lib().orc_seed_lambda_f32(nzz, ncols, c0, dx, dz, nb, rx, rz, len(rx), _f32(pg), lam)
+    return lam
+
+
+def batch_gradient(S, dx, dz, shots, rx, rz, pick_grad, nb=3, fp64=False):
+    """Oracle of sf_batch_adjoint: per shot (window) tape + seed + reverse
+    sweeps, shot gradients summed in FP64 in shot order onto the padded grid.
+    Returns (grad (nxx, nzz), picks (nshots, nrec))."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    total = np.zeros((nxx, nzz), np.float64)
+    picks_out = np.zeros((len(shots), len(rx)), np.float64 if fp64 else np.float32)
+    for b, s in enumerate(shots):
+        sx, sz = s[0], s[1]
+        c0 = int(s[2]) if len(s) > 2 else 0
+        nc = int(s[3]) if len(s) > 3 and s[3] > 0 else nxx - c0
+        T, code, c1, c2, sIdz, sloc = solve_tape(S, dx, dz, sx, sz, nb, c0, nc, fp64=fp64)
+        if fp64:
+            pk = np.full(len(rx), np.nan)
+            for r in range(len(rx)):
+                pw = pick_weights(rx[r], rz[r], dx, dz, nzz, nc, nb, c0)
+                if pw is not None:
+                    i, j, w = pw
+                    pk[r] = sum(w[a, bb] * T[j + a - 1, i + bb - 1] for a in range(4) for bb in range(4))
+        else:
+            pk = picks(T, dx, dz, rx, rz, nb, c0)
+        picks_out[b] = pk
+        lam = seed_lambda(nc, nzz, dx, dz, rx, rz, pick_grad[b], c0, nb, fp64)
+        d = init_dist(sx, sz, dx, dz, nb)
+        g, _ = adjoint((code, c1, c2, sIdz, sloc), lam, d, fp64=fp64)
+        total[c0:c0 + nc] += g.astype(np.float64)
+    return (total if fp64 else total.astype(np.float32)), picks_out

@@ -20,6 +20,8 @@ SF_MEM_HOST = 0
 SF_MEM_DEVICE = 1
 SF_LAYOUT_MODEL = 0
 SF_LAYOUT_PADDED = 1
+SF_ARITH_REFERENCE = 0
+SF_ARITH_IEEE = 1
 SF_KEEP_TAPE = 1
 SF_KEEP_TABLES = 2
 
@@ -52,6 +54,8 @@ SIGNATURES = {
     "sf_batch_misfit_gradient": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_double), VP, C.c_int, VP]),
     "sf_synchronize": (C.c_int, [VP, VP]),
     "sf_set_launch": (C.c_int, [VP, C.c_int, C.c_int]),
+    "sf_set_arithmetic": (C.c_int, [VP, C.c_int]),
+    "sf_get_arithmetic": (C.c_int, [VP, IP]),
     "sf_get_launch": (C.c_int, [VP, IP, IP]),
 }
 

@@ -1,21 +1,203 @@
-// Adjoint-state gradient of the pick misfit (entry points; kernels follow).
+// Adjoint-state gradient of the pick misfit: C ABI entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "sf_adjoint.cuh"
 #include "sf_engine.h"
+
+using namespace sf;
+
+#define CK(call)                                                          \
+    do {                                                                  \
+        int _st = sf_cuda_check(c, (call), #call);                        \
+        if (_st != SF_OK) return _st;                                     \
+    } while (0)
 
 void sf_adjoint_release(sf_ctx* c)
 {
-    void* bufs[] = {c->d_lam, c->d_vrec, c->d_gshot, c->d_pg, c->d_misfit, c->d_colshots, c->d_colptr};
+    void* bufs[] = {c->d_lam, c->d_vrec, c->d_gshot, c->d_pg, c->d_misfit, c->d_colshots, c->d_colptr,
+                    c->d_lam_init, c->d_hand2, c->d_orig_map};
     for (void* b : bufs)
         if (b) cudaFree(b);
 }
 
-extern "C" int sf_batch_adjoint(sf_ctx* c, const float*, int, float*, int, void*)
+size_t sf_adj_smem_bytes(int warps)
 {
-    return sf_fail(c, SF_ERR_STATE, "adjoint not available");
+    return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * sizeof(AdjRing);
 }
 
-extern "C" int sf_batch_misfit_gradient(sf_ctx* c, const float*, int, double*, float*, int, void*)
+int sf_adj_setup(sf_ctx* c)
 {
-    return sf_fail(c, SF_ERR_STATE, "adjoint not available");
+    CK(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sf_adj_smem_bytes(kMaxWarps)));
+    return SF_OK;
+}
+
+// Device buffers of the gather (shots per column, caller order) for the last
+// taped batch; rebuilt when the batch changes.
+static int prepare_gather(sf_ctx* c, cudaStream_t st)
+{
+    const int ns = (int)c->hshots.size();
+    std::vector<int> cnt(c->nxx + 1, 0);
+    std::vector<const ShotDev*> by_orig(ns);
+    for (const ShotDev& d : c->hshots) by_orig[d.orig] = &d;
+    for (int o = 0; o < ns; o++)
+        for (int j = by_orig[o]->c0; j < by_orig[o]->c0 + by_orig[o]->ncols; j++) cnt[j + 1]++;
+    for (int j = 0; j < c->nxx; j++) cnt[j + 1] += cnt[j];
+    std::vector<int> shots_of_col(cnt[c->nxx]);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int o = 0; o < ns; o++)
+        for (int j = by_orig[o]->c0; j < by_orig[o]->c0 + by_orig[o]->ncols; j++) shots_of_col[fill[j]++] = o;
+    int rc = sf_dev_reserve(c, (void**)&c->d_colptr, &c->cap_colptr, cnt.size() * sizeof(int));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_colshots, &c->cap_colshots,
+                                 std::max<size_t>(1, shots_of_col.size()) * sizeof(int));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_orig_map, &c->cap_orig_map, ns * sizeof(int));
+    if (rc) return rc;
+    c->h_colptr.swap(cnt);
+    c->h_colshots.swap(shots_of_col);
+    CK(cudaMemcpyAsync(c->d_colptr, c->h_colptr.data(), c->h_colptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!c->h_colshots.empty())
+        CK(cudaMemcpyAsync(c->d_colshots, c->h_colshots.data(), c->h_colshots.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_orig_map, c->tables_index.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+    return SF_OK;
+}
+
+// Runs the reverse sweeps and the gather for pick gradients already on the
+// device (d_pg, nshots x nrec, caller order); grad is a device pointer.
+int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t st)
+{
+    const int ns = (int)c->hshots.size();
+    const int nstrips = (c->nzz + 31) / 32;
+    const int grid = std::max(1, std::min(ns, c->sms * c->ctas_per_sm));
+    int rc = sf_dev_reserve(c, (void**)&c->d_lam, &c->cap_lam,
+                            (size_t)grid * c->nzz * c->batch_maxcols * sizeof(float));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_hand2, &c->cap_hand2,
+                                 (size_t)grid * nstrips * c->batch_maxcols * 2 * sizeof(float));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_lam_init, &c->cap_lam_init, (size_t)ns * 9 * sizeof(float));
+    if (rc) return rc;
+    rc = prepare_gather(c, st);
+    if (rc) return rc;
+    AdjParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.nzz = c->nzz;
+    p.nxx = c->nxx;
+    p.nb = c->nb;
+    p.dx = c->dx;
+    p.dz = c->dz;
+    p.shots = c->d_shots;
+    p.nshots = ns;
+    p.nstrips = nstrips;
+    p.lam = c->d_lam;
+    p.lam_per_cta = (long long)c->nzz * c->batch_maxcols;
+    p.hand = c->d_hand2;
+    p.hand_per_cta = (long long)nstrips * c->batch_maxcols * 2;
+    p.tcode = c->d_tcode;
+    p.tc1 = c->d_tc1;
+    p.tc2 = c->d_tc2;
+    p.pick_grad = d_pg;
+    p.rx = c->d_rx;
+    p.rz = c->d_rz;
+    p.nrec = c->batch_nrec;
+    p.lam_init = c->d_lam_init;
+    p.counter = c->d_flags + 2;  // flags[2]: adjoint work counter
+    p.err = c->d_flags + 1;
+    CK(cudaMemsetAsync(c->d_flags + 2, 0, sizeof(int), st));
+    k_adjoint<<<grid, c->warps * 32, sf_adj_smem_bytes(c->warps), st>>>(p);
+    CK(cudaGetLastError());
+    GatherParams g;
+    g.nzz = c->nzz;
+    g.nxx = c->nxx;
+    g.nb = c->nb;
+    g.nstrips = nstrips;
+    g.dx = c->dx;
+    g.dz = c->dz;
+    g.shots = c->d_shots;
+    g.shot_of_orig = c->d_orig_map;
+    g.colptr = c->d_colptr;
+    g.colshots = c->d_colshots;
+    g.tcode = c->d_tcode;
+    g.vrec = c->d_tc2;
+    g.lam_init = c->d_lam_init;
+    g.grad = d_grad;
+    const size_t ncell = (size_t)c->nzz * c->nxx;
+    k_gather<<<(unsigned)std::min<size_t>((ncell + 255) / 256, (size_t)c->sms * 16), 256, 0, st>>>(g);
+    CK(cudaGetLastError());
+    c->tape_valid = false;  // the reverse sweeps overwrite the tape's c2 with their terms
+    return SF_OK;
+}
+
+static int grad_target(sf_ctx* c, float* grad, int grad_mem, float** dg)
+{
+    if (grad_mem == SF_MEM_DEVICE) {
+        *dg = grad;
+        return SF_OK;
+    }
+    int rc = sf_dev_reserve(c, (void**)&c->d_gshot, &c->cap_gshot, (size_t)c->nzz * c->nxx * sizeof(float));
+    *dg = c->d_gshot;
+    return rc;
+}
+
+extern "C" int sf_batch_adjoint(sf_ctx* c, const float* pick_grad, int pg_mem, float* grad, int grad_mem,
+                                void* stream)
+{
+    if (!c) return SF_ERR_ARG;
+    if (!c->tape_valid) return sf_fail(c, SF_ERR_STATE, "no taped forward batch to differentiate");
+    if (!grad || (c->batch_nrec > 0 && !pick_grad)) return sf_fail(c, SF_ERR_ARG, "null argument");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t npk = (size_t)c->batch_nshots * c->batch_nrec;
+    const float* d_pg = pick_grad;
+    int rc;
+    if (pg_mem == SF_MEM_HOST) {
+        rc = sf_dev_reserve(c, (void**)&c->d_pg, &c->cap_pg, std::max<size_t>(npk, 1) * sizeof(float));
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(c->d_pg, pick_grad, npk * sizeof(float), cudaMemcpyHostToDevice, st));
+        d_pg = c->d_pg;
+    }
+    float* dg;
+    rc = grad_target(c, grad, grad_mem, &dg);
+    if (rc) return rc;
+    rc = sf_adjoint_device(c, d_pg, dg, st);
+    if (rc) return rc;
+    if (grad_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(grad, dg, (size_t)c->nzz * c->nxx * sizeof(float), cudaMemcpyDeviceToHost, st));
+        return sf_check_flags(c, st);
+    }
+    return SF_OK;
+}
+
+extern "C" int sf_batch_misfit_gradient(sf_ctx* c, const float* t_obs, int obs_mem, double* misfit, float* grad,
+                                        int grad_mem, void* stream)
+{
+    if (!c) return SF_ERR_ARG;
+    if (!c->tape_valid) return sf_fail(c, SF_ERR_STATE, "no taped forward batch to differentiate");
+    if (!t_obs || !grad) return sf_fail(c, SF_ERR_ARG, "null argument");
+    if (!c->batch_picks) return sf_fail(c, SF_ERR_STATE, "the taped batch computed no picks");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t npk = (size_t)c->batch_nshots * c->batch_nrec;
+    int rc = sf_dev_reserve(c, (void**)&c->d_pg, &c->cap_pg, std::max<size_t>(2 * npk, 2) * sizeof(float));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_misfit, &c->cap_misfit, sizeof(double));
+    if (rc) return rc;
+    const float* d_obs = t_obs;
+    if (obs_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(c->d_pg + npk, t_obs, npk * sizeof(float), cudaMemcpyHostToDevice, st));
+        d_obs = c->d_pg + npk;
+    }
+    k_residual<<<1, 1024, 0, st>>>(c->batch_picks, d_obs, npk, c->d_pg, c->d_misfit);
+    CK(cudaGetLastError());
+    float* dg;
+    rc = grad_target(c, grad, grad_mem, &dg);
+    if (rc) return rc;
+    rc = sf_adjoint_device(c, c->d_pg, dg, st);
+    if (rc) return rc;
+    if (misfit) CK(cudaMemcpyAsync(misfit, c->d_misfit, sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (grad_mem == SF_MEM_HOST)
+        CK(cudaMemcpyAsync(grad, dg, (size_t)c->nzz * c->nxx * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (misfit || grad_mem == SF_MEM_HOST) return sf_check_flags(c, st);
+    return SF_OK;
 }

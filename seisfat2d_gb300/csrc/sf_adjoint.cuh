@@ -1,0 +1,366 @@
+// Adjoint-state gradient: reverse sweeps over the forward tape.
+//
+// The forward pass (k_shots<true>) records, for every node of every sweep,
+// which candidate set the node (code bits 0-2), which slowness cell that
+// candidate read (bits 3-4) and two derivative coefficients c1, c2 (see
+// include/seisfat2d.h). The discrete adjoint of one sweep is then the linear
+// recurrence, in pull form, for node n = (i, j) of a sweep with signs (sz, sx):
+//
+//   mu(n)  = ((lam(n) + pv(i+sz, j)) + pe(i, j+sx)) + pev(i+sz, j+sx)
+//   lam(n) <- mu(n) if the node kept its value (code 0), else 0
+//   pv/pe/pev(n) = mu(n) * dT(n)/d{tv, te, tev}   (pushed to the upwind nodes)
+//   v(n)   = mu(n) * c2                           (term of the node's slowness cell)
+//
+// swept in the reverse order. It is the forward's dependency pattern with the
+// march reversed, so the same strip-systolic schedule runs it: lane l owns a
+// row, the lane above supplies pv/pev of the previous step by shfl, the lane's
+// own previous pe is kept in a register. The tape was written in the forward
+// strip's skewed step order, which makes the reverse read of one step 32
+// consecutive entries (lane l of the reverse march is lane 31-l of the
+// forward one).
+#pragma once
+#include "sf_forward.cuh"
+
+namespace sf {
+
+constexpr int kLP = 34;    // lambda slot pitch: 32 rows, then (pv, pev) handoff
+constexpr int kTR = 16;    // tape ring slots (>= kLook + 2)
+constexpr int kTPitch = 72;  // c1[32], c2[32], code bytes (8 words)
+
+struct AdjRing {
+    float L[kRing * kLP];
+    float TP[kTR * kTPitch];
+};
+
+struct AdjStripArgs {
+    float* lam;        // window adjoint field (column stride nzz), in place
+    int nzz, ncols, k;
+    const uint8_t* tcode;  // tape of this (sweep, strip): entries [fstep*32 + flane]
+    const float* tc1;
+    float* tc2;            // overwritten with v = mu * c2
+    AdjRing* ring;
+    CtaShared* sh;
+    int w_in, e_in, w_out, e_out;
+    const float* h_in;     // (pv, pev) pairs of the upwind strip's last row
+    float* h_out;
+    int* err;
+};
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
+{
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// SZ, SX: signs of the forward sweep being reversed.
+template <int SZ, int SX>
+__device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
+{
+    const int lane = threadIdx.x & 31;
+    const int nzz = a.nzz, ncols = a.ncols;
+    const int rb = 32 * a.k;
+    // reverse march: rows along -SZ, columns along -SX
+    const int r = (SZ < 0) ? rb + lane : rb + 31 - lane;
+    const bool vrow = r < nzz;
+    const int tix = r - rb;
+    const int flane = 31 - lane;  // this row's lane in the forward strip
+    float* Lr = a.ring->L;
+    float* TPr = a.ring->TP;
+    float* lamg = a.lam;
+    const bool lt_ok = (rb + lane) < nzz;
+    CtaShared* sh = a.sh;
+    const bool consumer = (lane == 0) && (a.w_in >= 0);
+    const int nsteps = ncols + 31;
+    auto col_of = [&](int m) { return (SX < 0) ? m : ncols - 1 - m; };
+    auto prefetch = [&](int q, int lslot, int tslot) {
+        if (q < ncols) {
+            const int jq = col_of(q);
+            if (lt_ok) cp_async4(&Lr[lslot * kLP + lane], lamg + (size_t)(rb + lane) + (size_t)jq * nzz);
+            if (consumer) {
+                spin_until(&sh->prod[a.w_in], a.e_in + q + 1, sh, a.err);
+                cp_async8(&Lr[lslot * kLP + 32], a.h_in + 2 * (size_t)q);
+            }
+        }
+        if (q < nsteps) {
+            const size_t fs = (size_t)(ncols + 30 - q) * 32;
+            cp_async4(&TPr[tslot * kTPitch + lane], a.tc1 + fs + lane);
+            cp_async4(&TPr[tslot * kTPitch + 32 + lane], a.tc2 + fs + lane);
+            if (lane < 8) cp_async4(&TPr[tslot * kTPitch + 64 + lane], a.tcode + fs + 4 * lane);
+        }
+        cp_commit();
+    };
+
+#pragma unroll 1
+    for (int q = 0; q < kLook; q++) prefetch(q, q, q % kTR);
+
+    int pf_slot = kLook, pf_tslot = kLook % kTR;
+    int m_slot = (kRing - lane) % kRing;
+    int wb_slot = (kRing - 31) % kRing;
+    int t_slot = 0;
+    float my_pv = 0.0f, my_pe = 0.0f, my_pev = 0.0f, pev_hold = 0.0f;
+
+#pragma unroll 1
+    for (int s = 0; s < nsteps; s++) {
+        prefetch(s + kLook, pf_slot, pf_tslot);
+        cp_wait<kLook - 1>();
+        __syncwarp();
+
+        const int m = s - lane;
+        const bool act = vrow && (m >= 0) && (m < ncols);
+        float pv_in = __shfl_up_sync(0xffffffffu, my_pv, 1);
+        float pev_in = __shfl_up_sync(0xffffffffu, my_pev, 1);
+        if (consumer) {
+            pv_in = Lr[m_slot * kLP + 32];
+            pev_in = Lr[m_slot * kLP + 33];
+        }
+        const float lam_in = Lr[m_slot * kLP + tix];
+        const float c1 = TPr[t_slot * kTPitch + flane];
+        const float c2 = TPr[t_slot * kTPitch + 32 + flane];
+        const int code = reinterpret_cast<const uint8_t*>(&TPr[t_slot * kTPitch + 64])[flane];
+
+        float mu = fadd(fadd(fadd(lam_in, pv_in), my_pe), pev_hold);
+        pev_hold = pev_in;
+        float npv = 0.0f, npe = 0.0f, npev = 0.0f;
+        if (act) {
+            const int br = code & 7;
+            float lo = mu, v = 0.0f;
+            if (br != 0) {
+                lo = 0.0f;
+                v = fmul(mu, c2);
+                switch (br) {
+                case 1: npv = mu; break;
+                case 2: npe = mu; break;
+                case 3: npv = fmul(mu, c1); npe = fmul(mu, -c1); npev = mu; break;
+                case 4: npe = fmul(mu, fsub(1.0f, c1)); npev = fmul(mu, c1); break;
+                default: npv = fmul(mu, fsub(1.0f, c1)); npev = fmul(mu, c1); break;
+                }
+            }
+            Lr[m_slot * kLP + tix] = lo;
+            a.tc2[(size_t)(ncols + 30 - s) * 32 + flane] = v;
+            if (lane == 31 && a.w_out >= 0) {
+                reinterpret_cast<float2*>(a.h_out)[m] = make_float2(npv, npev);
+                __threadfence_block();
+                st_volatile(&sh->prod[a.w_out], a.e_out + m + 1);
+            }
+        }
+        my_pv = npv;
+        my_pe = npe;
+        my_pev = npev;
+
+        const int mw = s - 31;
+        if (mw >= 0 && vrow) lamg[(size_t)r + (size_t)col_of(mw) * nzz] = Lr[wb_slot * kLP + tix];
+
+        if (++pf_slot == kRing) pf_slot = 0;
+        if (++pf_tslot == kTR) pf_tslot = 0;
+        if (++m_slot == kRing) m_slot = 0;
+        if (++wb_slot == kRing) wb_slot = 0;
+        if (++t_slot == kTR) t_slot = 0;
+    }
+    cp_wait<0>();
+    __syncwarp();
+}
+
+struct AdjParams {
+    int nzz, nxx, nb;
+    float dx, dz;
+    const ShotDev* shots;   // same table (and order) as the taped forward
+    int nshots;
+    int nstrips;
+    float* lam;             // per-CTA window adjoint, lam + blockIdx.x * lam_per_cta
+    long long lam_per_cta;
+    float* hand;            // per-CTA handoff pairs
+    long long hand_per_cta;
+    uint8_t* tcode;
+    float* tc1;
+    float* tc2;
+    const float* pick_grad; // nshots x nrec, caller order (NaN = no pick)
+    const float* rx;
+    const float* rz;
+    int nrec;
+    float* lam_init;        // nshots x 9, caller order: adjoint of the 3x3 initial values
+    int* counter;
+    int* err;
+};
+
+// Cubic weights of the pick rule (the rule is linear in the 16 nodes):
+// P -> P1 + 0.5 t (P2 - P0 + t (2P0 - 5P1 + 4P2 - P3 + t (3(P1 - P2) + P3 - P0)))
+// (every FP64 operation rounded once, left to right, as written)
+__device__ __forceinline__ void cubic_weights(double t, double w[4])
+{
+    const double t2 = __dmul_rn(t, t), t3 = __dmul_rn(t2, t);
+    w[0] = __dsub_rn(__dadd_rn(__dmul_rn(-0.5, t), t2), __dmul_rn(0.5, t3));
+    w[1] = __dadd_rn(__dsub_rn(1.0, __dmul_rn(2.5, t2)), __dmul_rn(1.5, t3));
+    w[2] = __dsub_rn(__dadd_rn(__dmul_rn(0.5, t), __dmul_rn(2.0, t2)), __dmul_rn(1.5, t3));
+    w[3] = __dadd_rn(__dmul_rn(-0.5, t2), __dmul_rn(0.5, t3));
+}
+
+__global__ void __launch_bounds__(kMaxWarps * 32) k_adjoint(AdjParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
+    AdjRing* rings = reinterpret_cast<AdjRing*>(smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15)));
+    const int tid = threadIdx.x, W = blockDim.x >> 5, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) cs->abort_flag = 0;
+    __syncthreads();
+    float* lam = p.lam + (size_t)blockIdx.x * p.lam_per_cta;
+    float* hb = p.hand + (size_t)blockIdx.x * p.hand_per_cta;
+    const int nzz = p.nzz, nstrips = p.nstrips;
+#pragma unroll 1
+    for (;;) {
+        if (tid == 0) cs->item = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int b = cs->item;
+        __syncthreads();
+        if (b >= p.nshots) break;
+        const ShotDev sh = p.shots[b];
+        const int ncols = sh.ncols;
+        const size_t n = (size_t)nzz * ncols;
+        // seed: adjoint of the final field from the pick gradients
+        for (size_t idx = tid; idx < n; idx += blockDim.x) lam[idx] = 0.0f;
+        __syncthreads();
+        if (warp == 0) {
+            const float* pg = p.pick_grad + (size_t)sh.orig * p.nrec;
+            for (int rr = 0; rr < p.nrec; rr++) {
+                const float g = pg[rr];
+                int i, j;
+                float xd, zd;
+                const bool ok = pick_geom(p.rx[rr], p.rz[rr], p.dx, p.dz, p.nb, nzz, ncols, sh.c0, i, j, xd, zd);
+                if (ok && g == g && lane < 16) {
+                    double wx[4], wz[4];
+                    cubic_weights((double)xd, wx);
+                    cubic_weights((double)zd, wz);
+                    const int aa = lane >> 2, bb = lane & 3;
+                    const float w = __double2float_rn(__dmul_rn(wx[aa], wz[bb]));
+                    float* at = lam + (size_t)(i + bb - 1) + (size_t)(j + aa - 1) * nzz;
+                    *at = fadd(*at, fmul(g, w));
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        // reverse sweeps 3, 2, 1, 0
+#pragma unroll 1
+        for (int sw = 3; sw >= 0; sw--) {
+            if (tid < kMaxWarps) cs->prod[tid] = 0;
+            __syncthreads();
+            const bool fz_pos = !(sw == 1 || sw == 3);  // forward SZ > 0
+            AdjStripArgs a;
+            a.lam = lam;
+            a.nzz = nzz;
+            a.ncols = ncols;
+            a.ring = rings + warp;
+            a.sh = cs;
+            a.err = p.err;
+#pragma unroll 1
+            for (int pidx = warp; pidx < nstrips; pidx += W) {
+                a.k = fz_pos ? nstrips - 1 - pidx : pidx;
+                a.w_in = (pidx > 0) ? warp : -1;
+                a.e_in = chan_entry(pidx, W) * ncols;
+                a.w_out = (pidx < nstrips - 1) ? (pidx + 1) % W : -1;
+                a.e_out = chan_entry(pidx + 1, W) * ncols;
+                a.h_in = hb + 2 * (size_t)pidx * ncols;
+                a.h_out = hb + 2 * (size_t)(pidx + 1) * ncols;
+                const size_t base = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
+                a.tcode = p.tcode + base;
+                a.tc1 = p.tc1 + base;
+                a.tc2 = p.tc2 + base;
+                switch (sw) {
+                case 0: adj_strip<1, 1>(a); break;
+                case 1: adj_strip<-1, 1>(a); break;
+                case 2: adj_strip<1, -1>(a); break;
+                default: adj_strip<-1, -1>(a); break;
+                }
+            }
+            __syncthreads();
+        }
+        if (tid < 9) {
+            const int aa = tid % 3, bb = tid / 3;
+            const int zi = sh.sIdz + aa - 1, xl = sh.sIdx - sh.c0 + bb - 1;
+            p.lam_init[(size_t)sh.orig * 9 + tid] = lam[(size_t)zi + (size_t)xl * nzz];
+        }
+        __syncthreads();
+    }
+}
+
+struct GatherParams {
+    int nzz, nxx, nb, nstrips;
+    float dx, dz;
+    const ShotDev* shots;    // sorted table; shot_of_orig maps caller index -> table row
+    const int* shot_of_orig;
+    const int* colptr;       // CSR over padded columns: caller-order shot indices covering it
+    const int* colshots;
+    const uint8_t* tcode;
+    const float* vrec;       // v terms (tape c2 after the reverse sweeps)
+    const float* lam_init;   // nshots x 9 (caller order)
+    float* grad;             // nzz x nxx
+};
+
+// Tape index of node (i, j) (window coordinates) in forward sweep sw.
+__device__ __forceinline__ size_t tape_index(const ShotDev& sh, int sw, int i, int j, int nstrips, int nzz)
+{
+    const int k = i >> 5;
+    const bool szpos = !(sw == 1 || sw == 3);
+    const bool sxpos = sw < 2;
+    const int flane = szpos ? (i - 32 * k) : (32 * k + 31 - i);
+    const int fm = sxpos ? j : sh.ncols - 1 - j;
+    return tape_strip_base(sh.tape_off, sw, k, nstrips, sh.ncols) + (size_t)(fm + flane) * 32 + flane;
+}
+
+// g(a, b) = sum over shots (caller order, FP64) of the shot's FP32 sum over
+// sweeps 0..3 and corners (dr, dc) = (0,0),(0,1),(1,0),(1,1) of the matching
+// node terms, plus the 3x3 initialisation term lam_init * dist.
+__global__ void k_gather(GatherParams p)
+{
+    const size_t ncell = (size_t)p.nzz * p.nxx;
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncell;
+         cell += (size_t)gridDim.x * blockDim.x) {
+        const int a = (int)(cell % p.nzz), bcol = (int)(cell / p.nzz);
+        double total = 0.0;
+        for (int q = p.colptr[bcol]; q < p.colptr[bcol + 1]; q++) {
+            const int orig = p.colshots[q];
+            const ShotDev sh = p.shots[p.shot_of_orig[orig]];
+            const int b = bcol - sh.c0;
+            float g = 0.0f;
+            for (int sw = 0; sw < 4; sw++)
+                for (int dr = 0; dr < 2; dr++)
+                    for (int dc = 0; dc < 2; dc++) {
+                        const int i = a + 1 - dr, j = b + 1 - dc;
+                        if (i >= p.nzz || j >= sh.ncols) continue;
+                        const size_t t = tape_index(sh, sw, i, j, p.nstrips, p.nzz);
+                        const int cd = p.tcode[t];
+                        if ((cd & 7) && ((cd >> 3) & 1) == dr && ((cd >> 4) & 1) == dc) g = fadd(g, p.vrec[t]);
+                    }
+            const int da = a - sh.sIdz + 1, db = bcol - sh.sIdx + 1;
+            if (da >= 0 && da < 3 && db >= 0 && db < 3) {
+                const double d = src_dist(a, bcol, p.nb, p.dx, p.dz, sh.sx, sh.sz);
+                g = fadd(g, fmul(p.lam_init[(size_t)orig * 9 + da + 3 * db], __double2float_rn(d)));
+            }
+            total += (double)g;
+        }
+        p.grad[cell] = __double2float_rn(total);
+    }
+}
+
+// Residuals r = pick - t_obs (NaN picks or observations contribute nothing)
+// and the misfit 1/2 sum r^2 in FP64 by one CTA in a fixed order.
+__global__ void k_residual(const float* picks, const float* tobs, size_t n, float* res, double* misfit)
+{
+    __shared__ double part[1024];
+    double acc = 0.0;
+    for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const float pk = picks[k], ob = tobs[k];
+        float r = fsub(pk, ob);
+        if (!(r == r)) r = __int_as_float(0x7fc00000);
+        res[k] = r;
+        if (r == r) acc += 0.5 * (double)r * (double)r;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *misfit = part[0];
+}
+
+}  // namespace sf

@@ -39,11 +39,14 @@ struct Rec {
     float c1, c2;
 };
 
-// One node update. s1a/s1b: cells of the vertical upwind edge (row i1,
+// One node update. REF selects the reference build's arithmetic: nvcc
+// contracts four multiply-adds of inner_sweep into FMAs (t1d1, t1d2, the 2D
+// numerator tb*dz2i + ta*dx2i and the discriminant 4 Sref^2 D - K dd^2); with
+// REF false every operation rounds once. s1a/s1b: cells of the vertical upwind edge (row i1,
 // columns max(j-1,1) and j); s2a/s2b: cells of the horizontal edge (rows
 // max(i-1,1) and i, column j1); sref = S[i1][j1]. dr1/dc2 locate i1/j1 in the
 // 2x2 block around the node, dc1a/dr2a locate the clamped first cells.
-template <bool TAPE>
+template <bool TAPE, bool REF>
 __device__ __forceinline__ float node_update(float told, float tv, float te, float tev, float s1a,
                                              float s1b, float s2a, float s2b, float sref,
                                              const Consts& k, int dr1, int dc1a, int dc2, int dr2a,
@@ -51,8 +54,8 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
 {
     float m1 = fminf(s1a, s1b);
     float m2 = fminf(s2a, s2b);
-    float t1d1 = fadd(tv, fmul(k.dz, m1));
-    float t1d2 = fadd(te, fmul(k.dx, m2));
+    float t1d1 = REF ? __fmaf_rn(k.dz, m1, tv) : fadd(tv, fmul(k.dz, m1));
+    float t1d2 = REF ? __fmaf_rn(k.dx, m2, te) : fadd(te, fmul(k.dx, m2));
     float t1D = fminf(t1d1, t1d2);
     float t1 = kBig, t2 = kBig, t3 = kBig;
     float dte = fsub(te, tev);
@@ -64,8 +67,13 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
         float ta = fsub(fadd(tev, te), tv);
         float tb = fadd(fsub(tev, te), tv);
         dd = fsub(ta, tb);
-        rr = fsqrt(fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd)));
-        t1 = fdiv(fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr), k.D);
+        if (REF) {
+            rr = fsqrt(__fmaf_rn(fmul(fmul(4.0f, sref), sref), k.D, -fmul(fmul(k.K, dd), dd)));
+            t1 = fdiv(fadd(__fmaf_rn(tb, k.dz2i, fmul(ta, k.dx2i)), rr), k.D);
+        } else {
+            rr = fsqrt(fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd)));
+            t1 = fdiv(fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr), k.D);
+        }
         br = 3;
     } else if ((dte <= fdiv(fmul(fmul(sref, k.dz), k.dz), k.hyp)) && (dte > 0.0f)) {
         q = fdiv(dte, k.dz);
@@ -117,6 +125,16 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
         }
     }
     return tnew;
+}
+
+// Near-source value of node (zi, xi) in the reference build's FP32
+// arithmetic: S * sqrtf(X*X + Z*Z), X = (xi-nb)*dx - sx (powf(v, 2.0f) = v*v).
+__device__ __forceinline__ float src_value_f32(float s, int zi, int xi, int nb, float dx, float dz,
+                                               float sx, float sz)
+{
+    const float X = fsub(fmul((float)(xi - nb), dx), sx);
+    const float Z = fsub(fmul((float)(zi - nb), dz), sz);
+    return fmul(s, fsqrt(fadd(fmul(X, X), fmul(Z, Z))));
 }
 
 // Near-source value of node (zi, xi) (global padded indices), FP64 then one
@@ -176,15 +194,17 @@ __device__ __forceinline__ float decode_c(uint16_t c, float mn, float mx)
     return fadd(mn, fdiv(fmul(fsub((float)c, 1.0f), fsub(mx, mn)), 65534.0f));
 }
 
-// qP phase slowness of one node (eikonal_ani.cu:59-108). T, S: window
-// pointers at the node; codes already decoded.
+// qP phase slowness of one node (eikonal_ani.cu:59-108); codes already
+// decoded. REF: the reference build's FMAs (|grad T|^2 and the three
+// Christoffel sums).
+template <bool REF>
 __device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, float txm, float s,
                                              float dx, float dz, float c11, float c13, float c15,
                                              float c33, float c35, float c55)
 {
     float dTz = fdiv(fmul(0.5f, fsub(tzp, tzm)), dz);
     float dTx = fdiv(fmul(0.5f, fsub(txp, txm)), dx);
-    float norm = fsqrt(fadd(fmul(dTx, dTx), fmul(dTz, dTz)));
+    float norm = fsqrt(REF ? __fmaf_rn(dTz, dTz, fmul(dTx, dTx)) : fadd(fmul(dTx, dTx), fmul(dTz, dTz)));
     float p0 = fdiv(dTx, norm), p1 = fdiv(dTz, norm);
     float Ro = fmul(fmul(c33, s), s);
     // C[q] / Ro / Ro
@@ -194,12 +214,16 @@ __device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, fl
     float C4 = fdiv(fdiv(c33, Ro), Ro);   // c33
     float C7 = fdiv(fdiv(c35, Ro), Ro);   // c35
     float C8 = fdiv(fdiv(c55, Ro), Ro);   // c55
-    float Gxx = fadd(fadd(fmul(fmul(C0, p0), p0), fmul(fmul(C8, p1), p1)),
-                     fmul(fmul(fmul(2.0f, C6), p0), p1));
-    float Gzz = fadd(fadd(fmul(fmul(C8, p0), p0), fmul(fmul(C4, p1), p1)),
-                     fmul(fmul(fmul(2.0f, C7), p0), p1));
-    float Gxz = fadd(fadd(fmul(fmul(C6, p0), p0), fmul(fmul(C7, p1), p1)),
-                     fmul(fmul(fadd(C3, C8), p0), p1));
+    float Gxx, Gzz, Gxz;
+    if (REF) {
+        Gxx = __fmaf_rn(fmul(fmul(2.0f, C6), p0), p1, __fmaf_rn(fmul(C0, p0), p0, fmul(fmul(C8, p1), p1)));
+        Gzz = __fmaf_rn(fmul(fmul(2.0f, C7), p0), p1, __fmaf_rn(fmul(C8, p0), p0, fmul(fmul(C4, p1), p1)));
+        Gxz = __fmaf_rn(fmul(fadd(C3, C8), p0), p1, __fmaf_rn(fmul(C6, p0), p0, fmul(fmul(C7, p1), p1)));
+    } else {
+        Gxx = fadd(fadd(fmul(fmul(C0, p0), p0), fmul(fmul(C8, p1), p1)), fmul(fmul(fmul(2.0f, C6), p0), p1));
+        Gzz = fadd(fadd(fmul(fmul(C8, p0), p0), fmul(fmul(C4, p1), p1)), fmul(fmul(fmul(2.0f, C7), p0), p1));
+        Gxz = fadd(fadd(fmul(fmul(C6, p0), p0), fmul(fmul(C7, p1), p1)), fmul(fmul(fadd(C3, C8), p0), p1));
+    }
     float coeff1 = fadd(Gxx, Gzz);
     float coeff2 = fsub(Gxx, Gzz);
     float det = fsqrt(fadd(fdiv(fmul(coeff2, coeff2), 4.0f), fmul(Gxz, Gxz)));

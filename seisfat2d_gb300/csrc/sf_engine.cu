@@ -186,6 +186,21 @@ extern "C" int sf_set_launch(sf_ctx* c, int warps, int ctas_per_sm)
     return SF_OK;
 }
 
+extern "C" int sf_set_arithmetic(sf_ctx* c, int mode)
+{
+    if (!c) return SF_ERR_ARG;
+    if (mode != SF_ARITH_REFERENCE && mode != SF_ARITH_IEEE) return sf_fail(c, SF_ERR_ARG, "unknown arithmetic");
+    c->arith = mode;
+    return SF_OK;
+}
+
+extern "C" int sf_get_arithmetic(const sf_ctx* c, int* mode)
+{
+    if (!c || !mode) return SF_ERR_ARG;
+    *mode = c->arith;
+    return SF_OK;
+}
+
 extern "C" int sf_get_launch(const sf_ctx* c, int* warps, int* ctas_per_sm)
 {
     if (!c) return SF_ERR_ARG;
@@ -197,9 +212,11 @@ extern "C" int sf_get_launch(const sf_ctx* c, int* warps, int* ctas_per_sm)
 int sf_fwd_setup(sf_ctx* c)
 {
     size_t mx = sf_fwd_smem_bytes(kMaxWarps);
-    CK(cudaFuncSetAttribute(k_shots<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_shots<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    return SF_OK;
+    CK(cudaFuncSetAttribute(k_shots<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_shots<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_shots<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_shots<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    return sf_adj_setup(c);
 }
 
 // ------------------------------------------------------------------ models
@@ -461,8 +478,14 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     p.picks = d_picks;
     CK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
     const size_t smem = sf_fwd_smem_bytes(c->warps);
-    if (tape) k_shots<true><<<grid, c->warps * 32, smem, st>>>(p);
-    else k_shots<false><<<grid, c->warps * 32, smem, st>>>(p);
+    const dim3 g(grid), b(c->warps * 32);
+    if (c->arith == SF_ARITH_REFERENCE) {
+        if (tape) k_shots<true, true><<<g, b, smem, st>>>(p);
+        else k_shots<false, true><<<g, b, smem, st>>>(p);
+    } else {
+        if (tape) k_shots<true, false><<<g, b, smem, st>>>(p);
+        else k_shots<false, false><<<g, b, smem, st>>>(p);
+    }
     CK(cudaGetLastError());
     c->tables_valid = keep_tables;
     c->tape_valid = tape;

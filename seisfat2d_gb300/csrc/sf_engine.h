@@ -15,6 +15,7 @@ struct sf_ctx {
     int sms = 1;
     int warps = 8;
     int ctas_per_sm = 2;
+    int arith = SF_ARITH_REFERENCE;
     std::string err;
 
     float* d_S = nullptr;       // padded slowness
@@ -54,6 +55,10 @@ struct sf_ctx {
     double* d_misfit = nullptr; size_t cap_misfit = 0;
     int* d_colshots = nullptr; size_t cap_colshots = 0;
     int* d_colptr = nullptr; size_t cap_colptr = 0;
+    int* d_orig_map = nullptr; size_t cap_orig_map = 0;
+    float* d_lam_init = nullptr; size_t cap_lam_init = 0;
+    float* d_hand2 = nullptr; size_t cap_hand2 = 0;
+    std::vector<int> h_colptr, h_colshots;
 };
 
 int sf_fail(sf_ctx* c, int status, const std::string& msg);
@@ -67,3 +72,5 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
 int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int grid,
                     cudaStream_t st);
 void sf_adjoint_release(sf_ctx* c);
+int sf_adj_setup(sf_ctx* c);
+int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t st);

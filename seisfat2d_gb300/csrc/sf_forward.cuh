@@ -49,6 +49,25 @@ struct FwdParams {
     float* picks;         // nshots x nrec, caller order
 };
 
+// 3x3 initial values of one solve into shared memory (modeling.cu:293-306):
+// FP32 as the reference build computes them (REF) or in FP64, rounded once.
+template <bool REF>
+__device__ __forceinline__ void init_block(const FwdParams& p, const ShotDev& sh, const float* Sw,
+                                           float* out)
+{
+    const int tid = threadIdx.x;
+    if (tid < 9) {
+        const int a = tid % 3, bb = tid / 3;
+        const int zi = sh.sIdz + a - 1, xl = sh.sIdx - sh.c0 + bb - 1;
+        const float s = Sw[zi + (size_t)xl * p.nzz];
+        if (REF)
+            out[tid] = src_value_f32(s, zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
+        else
+            out[tid] = __double2float_rn(
+                __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
+    }
+}
+
 __device__ __forceinline__ size_t tape_strip_base(long long tape_off, int sweep, int k, int nstrips,
                                                   int ncols)
 {
@@ -60,7 +79,7 @@ __device__ __forceinline__ size_t tape_strip_base(long long tape_off, int sweep,
 __device__ __forceinline__ int chan_entry(int p, int W) { return p / W - ((p % W == 0) ? 1 : 0); }
 
 // The four sweeps of one solve on the window held by this CTA.
-template <bool TAPE>
+template <bool TAPE, bool REF>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float* Sw, int ldS,
                              float* T, CtaShared* cs, WarpRing* rings)
 {
@@ -109,17 +128,17 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float*
                 a.tc2 = p.tc2 + base;
             }
             switch (sw) {
-            case 0: run_strip<1, 1, true, TAPE>(a); break;
-            case 1: run_strip<-1, 1, false, TAPE>(a); break;
-            case 2: run_strip<1, -1, false, TAPE>(a); break;
-            default: run_strip<-1, -1, false, TAPE>(a); break;
+            case 0: run_strip<1, 1, true, TAPE, REF>(a); break;
+            case 1: run_strip<-1, 1, false, TAPE, REF>(a); break;
+            case 2: run_strip<1, -1, false, TAPE, REF>(a); break;
+            default: run_strip<-1, -1, false, TAPE, REF>(a); break;
             }
         }
         __syncthreads();
     }
 }
 
-template <bool TAPE>
+template <bool TAPE, bool REF>
 __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -140,15 +159,9 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
         float* T = (p.t_per_cta > 0) ? p.Tpool + (size_t)blockIdx.x * p.t_per_cta
                                      : p.Tpool + sh.t_off;
         const float* Sw = p.S + (size_t)sh.c0 * nzz;
-        // time_init (modeling.cu:293-306) in FP64
-        if (tid < 9) {
-            const int a = tid % 3, bb = tid / 3;
-            const int zi = sh.sIdz + a - 1, xi = sh.sIdx + bb - 1;
-            double d = src_dist(zi, xi, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
-            cs->init[tid] = __double2float_rn(__dmul_rn((double)p.S[zi + (size_t)xi * nzz], d));
-        }
+        init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE>(p, sh, Sw, nzz, T, cs, rings);
+        solve_window<TAPE, REF>(p, sh, Sw, nzz, T, cs, rings);
         if (p.ani) {
             // get_quasi_slowness (eikonal_ani.cu:47-111) on the window
             float* Sq = p.Sq + (size_t)blockIdx.x * p.sq_per_cta;
@@ -161,7 +174,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
                 float out = s;
                 if (i >= nb && i < nzz - nb && j >= nb && j < ncols - nb && !(i == sh.sIdz && j == sloc)) {
                     const float* Tc = T + idx;
-                    out = qp_slowness(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz,
+                    out = qp_slowness<REF>(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz,
                                       decode_c(p.cij[0][g], p.mm[0], p.mm[1]),
                                       decode_c(p.cij[1][g], p.mm[2], p.mm[3]),
                                       decode_c(p.cij[2][g], p.mm[4], p.mm[5]),
@@ -172,14 +185,21 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
                 Sq[idx] = out;
             }
             __syncthreads();
-            if (tid < 9) {
-                const int a = tid % 3, bb = tid / 3;
-                const int zi = sh.sIdz + a - 1, xl = sloc + bb - 1;
-                double d = src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
-                cs->init[tid] = __double2float_rn(__dmul_rn((double)Sq[zi + (size_t)xl * nzz], d));
+            {
+                // second time_init reads the qP field (window-local columns)
+                if (tid < 9) {
+                    const int a = tid % 3, bb = tid / 3;
+                    const int zi = sh.sIdz + a - 1, xl = sloc + bb - 1;
+                    const float s = Sq[zi + (size_t)xl * nzz];
+                    if (REF)
+                        cs->init[tid] = src_value_f32(s, zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
+                    else
+                        cs->init[tid] = __double2float_rn(__dmul_rn(
+                            (double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
+                }
             }
             __syncthreads();
-            solve_window<false>(p, sh, Sq, nzz, T, cs, rings);
+            solve_window<false, REF>(p, sh, Sq, nzz, T, cs, rings);
         }
         // receivers (modeling.cu:161-194)
         if (p.nrec > 0 && p.picks) {

@@ -119,7 +119,7 @@ __device__ __forceinline__ bool spin_until(const int* p, int target, CtaShared* 
     return true;
 }
 
-template <int SZ, int SX, bool SW0, bool TAPE>
+template <int SZ, int SX, bool SW0, bool TAPE, bool REF>
 __device__ __forceinline__ void run_strip(const StripArgs& a)
 {
     const int lane = threadIdx.x & 31;
@@ -224,7 +224,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             const float s2b = (SX > 0) ? I_jm : I_j;       // S[i][j1]
             const float sref = (SX > 0) ? Si1_jm : Si1_j;  // S[i1][j1]
             const int dc1a = (j - 1 >= 1) ? 0 : 1;
-            tnew = node_update<TAPE>(told, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc, dr1,
+            tnew = node_update<TAPE, REF>(told, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc, dr1,
                                      dc1a, dc2, dr2a, rec);
         }
         if (act) Tring[m_slot * kTP + tix] = tnew;

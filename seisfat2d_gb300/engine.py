@@ -191,6 +191,16 @@ class Engine:
     def synchronize(self, stream=None):
         self._check(self.L.sf_synchronize(self._ctx, _stream_ptr(stream)), "sf_synchronize")
 
+    def set_arithmetic(self, mode):
+        """'reference' (the reference build's FP32 arithmetic) or 'ieee'."""
+        m = {"reference": _lib.SF_ARITH_REFERENCE, "ieee": _lib.SF_ARITH_IEEE}[mode]
+        self._check(self.L.sf_set_arithmetic(self._ctx, m), "sf_set_arithmetic")
+
+    def get_arithmetic(self):
+        v = C.c_int()
+        self.L.sf_get_arithmetic(self._ctx, C.byref(v))
+        return "reference" if v.value == _lib.SF_ARITH_REFERENCE else "ieee"
+
     def set_launch(self, warps=0, ctas_per_sm=0):
         self._check(self.L.sf_set_launch(self._ctx, int(warps), int(ctas_per_sm)), "sf_set_launch")
 

@@ -33,6 +33,21 @@ CASES = [
     ("iso_300x252_skipped_cells", 300, 252, 10.0, 10.0, 1000.0, 500.0, 0.0, False),
     ("ani_60x30_vti", 60, 30, 10.0, 10.0, 300.0, 0.0, 0.0, True),
     ("ani_45x45_tilt", 45, 45, 10.0, 10.0, 220.0, 100.0, 0.0, True),
+    ("s_iso_96x48_n30", 96, 48, 5.0, 5.0, 237.5, 0.0, 0.30, False),
+    ("s_iso_80x30_dxdz", 80, 30, 7.0, 12.0, 100.0, 0.0, 0.15, False),
+    ("s_ani_60x40_tilt_n", 60, 40, 10.0, 10.0, 290.0, 10.0, 0.10, True),
+]
+
+# rougher inputs that exercise the edge-update branches and the comparisons
+SEARCH_CASES = [
+    ("s_iso_64x40_n10", 64, 40, 10.0, 10.0, 310.0, 5.0, 0.10, False),
+    ("s_iso_40x64_n20", 40, 64, 10.0, 10.0, 190.0, 333.0, 0.20, False),
+    ("s_iso_80x30_dxdz", 80, 30, 7.0, 12.0, 100.0, 0.0, 0.15, False),
+    ("s_iso_50x50_n05", 50, 50, 10.0, 10.0, 0.0, 490.0, 0.05, False),
+    ("s_iso_96x48_n30", 96, 48, 5.0, 5.0, 237.5, 0.0, 0.30, False),
+    ("s_iso_70x35_dxdz2", 70, 35, 12.5, 6.25, 431.0, 87.0, 0.10, False),
+    ("s_ani_60x40_tilt_n", 60, 40, 10.0, 10.0, 290.0, 10.0, 0.10, True),
+    ("s_ani_50x50_tilt_n", 50, 50, 10.0, 10.0, 10.0, 250.0, 0.05, True),
 ]
 
 
@@ -46,7 +61,7 @@ def make_case(name, nx, nz, dx, dz, sx, sz, noise, ani):
         vp = 1.0 / m.astype(np.float64)
         eps = rng.uniform(0.0, 0.25, (nx, nz))
         dl = rng.uniform(-0.05, 0.15, (nx, nz))
-        tilt = 20.0 if "tilt" in name else 0.0
+        tilt = (20.0 if name.startswith("ani") else 35.0) if "tilt" in name else 0.0
         cij = thomsen_stiffness(vp, vp / np.sqrt(3.0), 1000.0, eps, dl, tilt)
         codes, mm = [], []
         for c in cij:
@@ -64,9 +79,10 @@ def make_case(name, nx, nz, dx, dz, sx, sz, noise, ani):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
+    ap.add_argument("--search", action="store_true", help="the rough cases instead")
     a = ap.parse_args()
     os.makedirs(a.out, exist_ok=True)
-    for c in CASES:
+    for c in (SEARCH_CASES if a.search else CASES):
         d = make_case(*c)
         np.savez_compressed(os.path.join(a.out, c[0] + ".npz"), **d)
         print("wrote", c[0])

@@ -12,7 +12,7 @@ def smooth_model(nx, nz, dh, seed=0, vmin=1500.0, vmax=3500.0, noise=0.0):
     cx, cz = rng.uniform(0.3, 0.7) * x[-1], rng.uniform(0.3, 0.7) * z[-1]
     v = v + 300.0 * np.exp(-((x[:, None] - cx) ** 2 + (z[None, :] - cz) ** 2) / (2 * (0.15 * x[-1] + dh) ** 2))
     if noise:
-        v = v * (1.0 + noise * rng.standard_normal(v.shape))
+        v = np.maximum(v * (1.0 + noise * rng.standard_normal(v.shape)), 300.0)
     return (1.0 / v).astype(np.float32)
 
 

@@ -1,0 +1,105 @@
+"""GPU adjoint-state gradient through the C ABI.
+
+The engine's FP32 gradient equals the oracle's FP32 restatement bit for bit
+(same tape, same summation order, shot sums in FP64); it agrees with the
+FP64 adjoint to 1e-3 relative (L2), and the FP64 adjoint with central finite
+differences of the FP64 misfit.
+"""
+import numpy as np
+import pytest
+
+from helpers import smooth_model, surface_receivers
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(nx=70, nz=36, seed=3, noise=0.02, arith="ieee"):
+    from seisfat2d_gb300 import Engine
+    m = smooth_model(nx, nz, 10.0, seed=seed, noise=noise)
+    e = Engine(nx, nz, 10.0, 10.0)
+    e.set_arithmetic(arith)
+    e.set_slowness(m)
+    return e, m
+
+
+@pytest.mark.parametrize("arith", ["ieee", "reference"])
+def test_adjoint_bitexact_vs_oracle(oracle, engine_lib, cuda, arith):
+    e, m = setup(arith=arith)
+    oracle.set_arith(arith)
+    try:
+        S = oracle.expand_boundary(m)
+        rx, rz = surface_receivers(e.nx, 10.0, step=3)
+        rz = rz + 10.0
+        shots = [(120.0, 0.0), (400.0, 30.0, 10, 45), (650.0, 80.0), (333.0, 200.0, 0, 50)]
+        pk = e.batch_forward(shots, rx, rz, keep_tape=True)
+        rng = np.random.default_rng(0)
+        pg = rng.standard_normal(pk.shape).astype(np.float32)
+        pg[np.isnan(pk)] = np.nan
+        g = e.batch_adjoint(pg)
+        go, po = oracle.batch_gradient(S, 10.0, 10.0, shots, rx, rz, pg)
+        assert np.array_equal(pk, po, equal_nan=True)
+        assert np.array_equal(g, go), np.abs(g - go).max()
+        assert np.abs(g).max() > 0
+    finally:
+        oracle.set_arith("ieee")
+
+
+def test_adjoint_fp32_vs_fp64(oracle, engine_lib, cuda):
+    e, m = setup(nx=90, nz=50, seed=8, noise=0.0)
+    S = oracle.expand_boundary(m)
+    rx, rz = surface_receivers(e.nx, 10.0, step=2)
+    shots = [(150.0, 0.0), (600.0, 0.0), (880.0, 0.0)]
+    pk = e.batch_forward(shots, rx, rz, keep_tape=True)
+    pg = np.where(np.isnan(pk), np.nan, np.cos(np.arange(pk.size).reshape(pk.shape) * 0.1)).astype(np.float32)
+    g = e.batch_adjoint(pg).astype(np.float64)
+    g64, _ = oracle.batch_gradient(S, 10.0, 10.0, shots, rx, rz, pg.astype(np.float64), fp64=True)
+    rel = np.linalg.norm(g - g64) / np.linalg.norm(g64)
+    print(f"relative L2 error FP32 adjoint vs FP64 adjoint: {rel:.2e}")
+    assert rel <= 1e-3
+
+
+def test_misfit_gradient_is_adjoint_of_residuals(oracle, engine_lib, cuda):
+    e, m = setup(nx=60, nz=30, seed=4)
+    rx, rz = surface_receivers(e.nx, 10.0, step=2)
+    shots = [(100.0, 0.0), (450.0, 0.0)]
+    pk = e.batch_forward(shots, rx, rz, keep_tape=True)
+    tobs = (pk + 0.01 * np.sin(np.arange(pk.size).reshape(pk.shape))).astype(np.float32)
+    J, g = e.misfit_gradient(tobs)
+    r = (pk - tobs).astype(np.float64)
+    assert abs(J - 0.5 * np.nansum(r * r)) <= 1e-6 * abs(J)
+    e.batch_forward(shots, rx, rz, keep_tape=True)
+    g2 = e.batch_adjoint(np.where(np.isnan(pk), np.nan, pk - tobs).astype(np.float32))
+    assert np.array_equal(g, g2)
+
+
+def test_adjoint_needs_tape_and_consumes_it(engine_lib, cuda):
+    from seisfat2d_gb300._lib import SF_ERR_STATE
+    from seisfat2d_gb300 import EngineError
+    e, m = setup(nx=40, nz=20)
+    rx, rz = surface_receivers(e.nx, 10.0, step=4)
+    pk = e.batch_forward([(100.0, 0.0)], rx, rz)
+    with pytest.raises(EngineError) as ex:
+        e.batch_adjoint(np.zeros_like(pk))
+    assert ex.value.status == SF_ERR_STATE
+    pk = e.batch_forward([(100.0, 0.0)], rx, rz, keep_tape=True)
+    e.batch_adjoint(np.zeros_like(pk))
+    with pytest.raises(EngineError):
+        e.batch_adjoint(np.zeros_like(pk))
+
+
+def test_autograd_wrapper_matches_adjoint(engine_lib, cuda):
+    import torch
+    from seisfat2d_gb300.autograd import EikonalPicks
+    e, m = setup(nx=50, nz=30, seed=9)
+    rx, rz = surface_receivers(e.nx, 10.0, step=3)
+    shots = [(100.0, 0.0), (300.0, 50.0)]
+    S = torch.tensor(e.get_slowness(), device="cuda", requires_grad=True)
+    picks = EikonalPicks.apply(S, e, shots, rx, rz)
+    w = torch.linspace(-1, 1, picks.numel(), device="cuda").reshape(picks.shape)
+    loss = torch.nansum(picks * w)
+    loss.backward()
+    e.set_slowness(S.detach(), padded=True)
+    e.batch_forward(shots, rx, rz, keep_tape=True)
+    pg = torch.where(torch.isnan(picks), torch.nan, w).detach().cpu().numpy()
+    g = e.batch_adjoint(pg)
+    assert np.array_equal(S.grad.cpu().numpy(), g)
