@@ -196,3 +196,23 @@ extern "C" int ref_solve(int nxx, int nzz, int nb, const float* S, float dx, flo
         if (dC[q]) cuMemFree(dC[q]);
     return 0;
 }
+
+// time_set + time_init only (modeling.cu:110-121): the reference's initial
+// field for one source, to pin the near-source arithmetic.
+extern "C" int ref_init(int nxx, int nzz, int nb, const float* S, float dx, float dz, float sx, float sz,
+                        float* T_out)
+{
+    DR(cuCtxSetCurrent(g_ctx));
+    const int matsize = nxx * nzz;
+    CUdeviceptr dT, dS;
+    DR(cuMemAlloc(&dT, sizeof(float) * matsize));
+    DR(cuMemAlloc(&dS, sizeof(float) * matsize));
+    DR(cuMemcpyHtoD(dS, S, sizeof(float) * matsize));
+    int sIdx, sIdz, rc;
+    if ((rc = initialization(dT, dS, matsize, nzz, nb, sx, sz, dx, dz, &sIdx, &sIdz))) return rc;
+    DR(cuCtxSynchronize());
+    DR(cuMemcpyDtoH(T_out, dT, sizeof(float) * matsize));
+    cuMemFree(dT);
+    cuMemFree(dS);
+    return 0;
+}

@@ -50,3 +50,17 @@ def solve(S_padded, dx, dz, sx, sz, ani=None, nb=3, repeats=1):
     if rc != 0:
         raise RuntimeError(f"ref_solve failed ({rc})")
     return T, ms.value
+
+
+def init(S_padded, dx, dz, sx, sz, nb=3):
+    """The reference's time_set + time_init field (no sweeps)."""
+    h = _handle()
+    h.ref_init.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_float, C.c_float,
+                           C.c_float, C.c_void_p]
+    S = np.ascontiguousarray(S_padded, np.float32)
+    T = np.zeros_like(S)
+    rc = h.ref_init(S.shape[0], S.shape[1], nb, C.c_void_p(S.ctypes.data), dx, dz, sx, sz,
+                    C.c_void_p(T.ctypes.data))
+    if rc != 0:
+        raise RuntimeError(f"ref_init failed ({rc})")
+    return T
