@@ -133,6 +133,24 @@ int sf_synchronize(sf_ctx* ctx, void* stream);
 int sf_set_arithmetic(sf_ctx* ctx, int mode);
 int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
 
+/* Per-shot solve that allocates nothing. No counterpart in the reference.
+ * For callers that may not allocate device memory inside a call (hosts that
+ * own all device memory through their own pool and forbid cudaMalloc/cudaFree
+ * in plugin calls, latency-critical loops). Same result as
+ * sf_time_propagation in the default (reference) arithmetic, isotropic.
+ * S: padded slowness on the current device (nzz x nxx, nzz = nz+6, nxx =
+ * nx+6); T: output on the current device (nzz x nxx). Scratch lives in one
+ * static device array of 1 MiB + 256 B that every GPU loading the library
+ * holds until exit: grids with ceil(nzz/32) * nxx > 262144 are rejected with
+ * SF_ERR_RANGE. The first call on a device sets that device up (looks up the
+ * array's device address, sets the kernel's shared-memory limit); make it
+ * before any stream capture. Calls share the array: calls that overlap on the
+ * GPU (other streams, other threads) race and must be serialised by the
+ * caller. Synchronises `stream`; returns SF_ERR_TIMEOUT if an in-kernel wait
+ * gave up. */
+int sf_time_propagation_noalloc(const float* S, int nx, int nz, float dx, float dz, float sx, float sz,
+                                float* T, void* stream);
+
 /* Launch shape: warps per CTA (4..16) and CTAs per SM for batches (1..4);
  * 0 keeps the current value. */
 int sf_set_launch(sf_ctx* ctx, int warps, int ctas_per_sm);

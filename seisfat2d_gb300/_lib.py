@@ -57,6 +57,8 @@ SIGNATURES = {
     "sf_set_arithmetic": (C.c_int, [VP, C.c_int]),
     "sf_get_arithmetic": (C.c_int, [VP, IP]),
     "sf_get_launch": (C.c_int, [VP, IP, IP]),
+    "sf_time_propagation_noalloc": (C.c_int, [VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                              C.c_float, VP, VP]),
 }
 
 _lib = None

@@ -635,3 +635,7 @@ extern "C" int sf_compute_seismogram(sf_ctx* c, const float* T_dev, const float*
     }
     return SF_OK;
 }
+
+// The allocation-free per-shot entry point shares this translation unit's
+// instantiation of k_shots.
+#include "sf_noalloc.cu"

@@ -1,0 +1,125 @@
+// Per-shot solve that allocates nothing (sf_time_propagation_noalloc).
+//
+// For callers that may not allocate device memory during a call: hosts that
+// own all device memory through their own pool and forbid cudaMalloc/cudaFree
+// inside plugin calls (both can synchronise the device and fragment the
+// host's pool), or latency-critical loops that cannot afford an allocation.
+// The caller passes the padded slowness and the output traveltimes; every
+// other buffer the solve needs (the strip-handoff values, the launch's
+// counters and error flag, the shot descriptor) lives in one file-scope
+// static device array of fixed size, which every GPU that loads this library
+// holds until the process exits.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "sf_engine.h"
+
+using namespace sf;
+
+namespace {
+
+// Scratch capacity: strip-handoff values for up to kNoAllocHandoff floats
+// (ceil(nzz/32) strips x nxx columns), i.e. 1 MiB, plus a 256-byte header.
+constexpr size_t kNoAllocHandoff = 262144;
+constexpr size_t kNoAllocHeader = 256;
+
+struct NoAllocHeader {
+    int counter;   // work counter of the launch (must start at 0)
+    int err;       // in-kernel wait timeout flag (must start at 0)
+    int pad[2];
+    ShotDev shot;  // the one shot of the call
+};
+static_assert(sizeof(NoAllocHeader) <= kNoAllocHeader, "header too large");
+
+// Shared by every call on a device; keeps the last call's contents.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHeader + kNoAllocHandoff * sizeof(float)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char* g_scratch_addr[kMaxDevices] = {};  // device address of the array, per device
+
+// Once per device, with that device current: the device address of the
+// scratch array (host code only knows a stand-in for the symbol) and the
+// kernel's shared-memory limit.
+int noalloc_setup(int dev, unsigned char** addr)
+{
+    if (dev < 0 || dev >= kMaxDevices) return SF_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SF_ERR_CUDA;
+        if (cudaFuncSetAttribute(k_shots<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sf_fwd_smem_bytes(kMaxWarps)) != cudaSuccess)
+            return SF_ERR_CUDA;
+        g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    *addr = g_scratch_addr[dev];
+    return SF_OK;
+}
+
+}  // namespace
+
+extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float dx, float dz, float sx, float sz,
+                                           float* T, void* stream)
+{
+    if (!S || !T || nx < 2 || nz < 2 || !(dx > 0.0f) || !(dz > 0.0f)) return SF_ERR_ARG;
+    const int nb = 3, nxx = nx + 2 * nb, nzz = nz + 2 * nb;
+    const size_t nstrips = (size_t)(nzz + 31) / 32;
+    if (nstrips * (size_t)nxx > kNoAllocHandoff) return SF_ERR_RANGE;  // grid beyond the scratch capacity
+    // source node (modeling.cu:112-113)
+    const float fx = (sx + 0.5f * dx) / dx, fz = (sz + 0.5f * dz) / dz;
+    if (!(fx > -1e9f && fx < 1e9f && fz > -1e9f && fz < 1e9f)) return SF_ERR_RANGE;
+    ShotDev sh{};
+    sh.c0 = 0;
+    sh.ncols = nxx;
+    sh.sIdx = (int)fx + nb;
+    sh.sIdz = (int)fz + nb;
+    sh.sx = sx;
+    sh.sz = sz;
+    if (sh.sIdz < 1 || sh.sIdz > nzz - 2 || sh.sIdx < 1 || sh.sIdx > nxx - 2) return SF_ERR_RANGE;
+    sf_skip_cells(nxx, nzz, sh.skip_i, sh.skip_j);
+    sh.orig = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SF_ERR_CUDA;
+    unsigned char* base = nullptr;
+    int rc = noalloc_setup(dev, &base);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    NoAllocHeader hdr{};
+    hdr.shot = sh;  // counter and err start at zero
+    if (cudaMemcpyAsync(base, &hdr, sizeof(hdr), cudaMemcpyHostToDevice, st) != cudaSuccess) return SF_ERR_CUDA;
+    NoAllocHeader* dh = reinterpret_cast<NoAllocHeader*>(base);
+
+    Consts k;
+    k.dx = dx;
+    k.dz = dz;
+    k.dz2i = 1.0f / (dz * dz);
+    k.dx2i = 1.0f / (dx * dx);
+    k.hyp = sqrtf(dx * dx + dz * dz);
+    k.D = k.dz2i + k.dx2i;
+    k.K = k.dz2i * k.dx2i;
+    k.kA = k.dz2i - k.dx2i;
+    k.k2K = 2.0f * k.K;
+    FwdParams p{};
+    p.S = S;
+    p.nzz = nzz;
+    p.nxx = nxx;
+    p.nb = nb;
+    p.kc = k;
+    p.shots = &dh->shot;
+    p.nshots = 1;
+    p.Tpool = T;
+    p.t_per_cta = 0;
+    p.counter = &dh->counter;
+    p.err = &dh->err;
+    p.hand = reinterpret_cast<float*>(base + kNoAllocHeader);
+    p.hand_per_cta = (long long)nstrips * nxx;
+    const int warps = 8;
+    k_shots<false, true><<<1, warps * 32, sf_fwd_smem_bytes(warps), st>>>(p);
+    if (cudaGetLastError() != cudaSuccess) return SF_ERR_CUDA;
+    int err = 0;
+    if (cudaMemcpyAsync(&err, &dh->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return SF_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SF_ERR_CUDA;
+    return err ? SF_ERR_TIMEOUT : SF_OK;
+}
