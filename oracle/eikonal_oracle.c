@@ -140,16 +140,19 @@ void orc_init_block_f64(const float* S, int nzz, float sx, float sz, float dx, f
         }
 }
 
-/* modeling.cu:293-306 in the reference build's FP32 arithmetic
- * (powf(v, 2.0f) taken as v*v). */
+/* modeling.cu:293-306 in the reference build's FP32 arithmetic: nvcc fuses
+ * (xi-nb)*dx - sx into one FMA. The reference squares with CUDA's powf(v,
+ * 2.0f), which this restatement cannot reproduce bit for bit; v*v (correctly
+ * rounded) is used, which differs from CUDA's powf by an ulp for about 3% of
+ * arguments. Exact for sources whose offsets X, Z are exact small values. */
 void orc_init_block_f32(const float* S, int nzz, float sx, float sz, float dx, float dz, int nb,
                            int sIdx, int sIdz, float vals[9])
 {
     for (int b = 0; b < 3; b++)
         for (int a = 0; a < 3; a++) {
             int zi = sIdz + a - 1, xi = sIdx + b - 1;
-            float X = (float)(xi - nb) * dx - sx;
-            float Z = (float)(zi - nb) * dz - sz;
+            float X = fmaf((float)(xi - nb), dx, -sx);
+            float Z = fmaf((float)(zi - nb), dz, -sz);
             vals[a + 3 * b] = S[zi + (size_t)xi * nzz] * sqrtf(X * X + Z * Z);
         }
 }
@@ -241,13 +244,13 @@ static float upd32(float told, float tv, float te, float tev, float s1a, float s
         br = 3;
     } else if ((te - tev <= sref * k->dz * k->dz / k->hyp) && (te - tev > 0.0f)) {
         q = (te - tev) / k->dz;
-        qq = sqrtf(sref * sref - q * q);
-        t2 = te + k->dx * qq;
+        qq = sqrtf(ref ? fmaf(-q, q, sref * sref) : sref * sref - q * q);
+        t2 = ref ? fmaf(k->dx, qq, te) : te + k->dx * qq;
         br = 4;
     } else if ((tv - tev <= sref * k->dx * k->dx / k->hyp) && (tv - tev > 0.0f)) {
         q = (tv - tev) / k->dx;
-        qq = sqrtf(sref * sref - q * q);
-        t3 = tv + k->dz * qq;
+        qq = sqrtf(ref ? fmaf(-q, q, sref * sref) : sref * sref - q * q);
+        t3 = ref ? fmaf(k->dz, qq, tv) : tv + k->dz * qq;
         br = 5;
     }
     float t2D = fminf(t1, fminf(t2, t3));
@@ -744,8 +747,8 @@ int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, i
             for (int a = 0; a < 3; a++) {
                 int zi = sIdz + a - 1, xl = sloc + b - 1;
                 if (g_arith == 1) {
-                    float X = (float)(xl + c0 - nb) * dx - sx;
-                    float Z = (float)(zi - nb) * dz - sz;
+                    float X = fmaf((float)(xl + c0 - nb), dx, -sx);
+                    float Z = fmaf((float)(zi - nb), dz, -sz);
                     init[a + 3 * b] = Sq[zi + (size_t)xl * nzz] * sqrtf(X * X + Z * Z);
                 } else {
                     double ddx = (double)(xl + c0 - nb) * (double)dx - (double)sx;

@@ -138,7 +138,9 @@ void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb,
 /* Arithmetic of the FP32 solvers: 0 = every operation rounded once and the
  * 3x3 initialisation in FP64 (default); 1 = the reference build's arithmetic:
  * FP32 initialisation and fused multiply-adds where nvcc forms them in
- * inner_sweep (t1d1, t1d2, the 2D numerator and discriminant). */
+ * inner_sweep (t1d1, t1d2, the 2D numerator and discriminant, Sref^2 - q^2 and
+ * the two edge updates) and get_quasi_slowness (|grad T|^2, the Christoffel
+ * sums). */
 void orc_set_arith(int mode);
 
 /* Catmull-Rom weights of the pick rule: w[16], node (i-1+b, j-1+a) -> w[a*4+b]

@@ -40,9 +40,10 @@ struct Rec {
 };
 
 // One node update. REF selects the reference build's arithmetic: nvcc
-// contracts four multiply-adds of inner_sweep into FMAs (t1d1, t1d2, the 2D
-// numerator tb*dz2i + ta*dx2i and the discriminant 4 Sref^2 D - K dd^2); with
-// REF false every operation rounds once. s1a/s1b: cells of the vertical upwind edge (row i1,
+// contracts seven multiply-adds of inner_sweep into FMAs (t1d1, t1d2, the 2D
+// numerator tb*dz2i + ta*dx2i, the discriminant 4 Sref^2 D - K dd^2, and in
+// the edge updates Sref^2 - q^2 and te/tv + h*sqrt(..)); with REF false every
+// operation rounds once. s1a/s1b: cells of the vertical upwind edge (row i1,
 // columns max(j-1,1) and j); s2a/s2b: cells of the horizontal edge (rows
 // max(i-1,1) and i, column j1); sref = S[i1][j1]. dr1/dc2 locate i1/j1 in the
 // 2x2 block around the node, dc1a/dr2a locate the clamped first cells.
@@ -77,13 +78,23 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
         br = 3;
     } else if ((dte <= fdiv(fmul(fmul(sref, k.dz), k.dz), k.hyp)) && (dte > 0.0f)) {
         q = fdiv(dte, k.dz);
-        qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
-        t2 = fadd(te, fmul(k.dx, qq));
+        if (REF) {
+            qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
+            t2 = __fmaf_rn(k.dx, qq, te);
+        } else {
+            qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
+            t2 = fadd(te, fmul(k.dx, qq));
+        }
         br = 4;
     } else if ((dtv <= fdiv(fmul(fmul(sref, k.dx), k.dx), k.hyp)) && (dtv > 0.0f)) {
         q = fdiv(dtv, k.dx);
-        qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
-        t3 = fadd(tv, fmul(k.dz, qq));
+        if (REF) {
+            qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
+            t3 = __fmaf_rn(k.dz, qq, tv);
+        } else {
+            qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
+            t3 = fadd(tv, fmul(k.dz, qq));
+        }
         br = 5;
     }
     float t2D = fminf(t1, fminf(t2, t3));
@@ -128,13 +139,14 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
 }
 
 // Near-source value of node (zi, xi) in the reference build's FP32
-// arithmetic: S * sqrtf(X*X + Z*Z), X = (xi-nb)*dx - sx (powf(v, 2.0f) = v*v).
+// arithmetic (time_init, modeling.cu:293-306): X = (xi-nb)*dx - sx fused into
+// one FMA by nvcc, then S * sqrtf(powf(X, 2) + powf(Z, 2)) with CUDA's powf.
 __device__ __forceinline__ float src_value_f32(float s, int zi, int xi, int nb, float dx, float dz,
                                                float sx, float sz)
 {
-    const float X = fsub(fmul((float)(xi - nb), dx), sx);
-    const float Z = fsub(fmul((float)(zi - nb), dz), sz);
-    return fmul(s, fsqrt(fadd(fmul(X, X), fmul(Z, Z))));
+    const float X = __fmaf_rn((float)(xi - nb), dx, -sx);
+    const float Z = __fmaf_rn((float)(zi - nb), dz, -sz);
+    return fmul(s, fsqrt(fadd(powf(X, 2.0f), powf(Z, 2.0f))));
 }
 
 // Near-source value of node (zi, xi) (global padded indices), FP64 then one

@@ -1,8 +1,12 @@
 """GPU parity of the forward solver against the oracle, through the C ABI.
 
 FP32 traveltimes must equal the oracle's FP32 restatement bit for bit (same
-IEEE operations in the same order, every node); picks likewise. The FP64
-oracle bounds the FP32 error at 1e-5 relative.
+IEEE operations in the same order, every node), in both arithmetics; picks
+likewise. Sources sit at integer metres so the near-source offsets are exact
+(the reference arithmetic squares them with CUDA's powf, which the oracle
+cannot restate bit for bit; arbitrary positions are checked against the
+reference's own kernels in test_gpu_reference.py). The FP64 oracle bounds the
+FP32 error at 1e-5 relative.
 """
 import numpy as np
 import pytest
@@ -36,7 +40,7 @@ def test_plain_bitexact_vs_oracle(oracle, engine_lib, cuda, arith, nx, nz):
     S = oracle.expand_boundary(m)
     e = make_engine(nx, nz, dx, dz, m, arith)
     srcs = [(0.0, 0.0), ((nx - 1) * dx, 0.0), (0.0, (nz - 1) * dz), ((nx - 1) * dx, (nz - 1) * dz),
-            (nx * 4.37, nz * 3.11)]
+            (float(round(nx * 4.37)), float(round(nz * 3.11)))]  # integer metres: exact offsets
     for sx, sz in srcs:
         T = e.time_propagation(sx, sz)
         To = oracle.solve_f32(S, dx, dz, sx, sz)
@@ -113,11 +117,11 @@ def test_batched_windows_equal_plain_per_window(oracle, engine_lib, cuda, arith)
     rng = np.random.default_rng(3)
     shots = []
     for k in range(23):
-        sx = float(rng.uniform(0, (nx - 1) * 10.0))
+        sx = float(int(rng.uniform(0, (nx - 1) * 10.0)))
         sidx = int((sx + 5.0) / 10.0) + 3
         c0 = max(0, sidx - int(rng.integers(5, 120)))
         c1 = min(e.nxx, sidx + int(rng.integers(5, 120)))
-        shots.append((sx, float(rng.uniform(0, 200.0)), c0, c1 - c0))
+        shots.append((sx, float(int(rng.uniform(0, 200.0))), c0, c1 - c0))
     shots.append((1500.0, 0.0, 0, 0))  # full width
     rx, rz = surface_receivers(nx, 10.0, step=2)
     pk = e.batch_forward(shots, rx, rz, keep_tables=True)

@@ -1,0 +1,163 @@
+"""The C++ drop-in (Modeling/Eikonal_ISO/Eikonal_ANI/Geometry/admin and
+Tomography_ISO) driven by parameters.txt, end to end on the GPU: the output
+files of modeling.exe, traveltime_tables.exe and inversion.exe."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import smooth_model
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = """#--------------------------------------------------------------
+# Model paramenters
+x_samples = {nx}                       # <int>
+z_samples = {nz}                       # <int>
+
+x_spacing = {dx}                       # [m] <float>
+z_spacing = {dz}                       # [m] <float>
+
+slowness_file = {d}/slowness.bin
+Cijkl_folder = {d}/model_
+SPS = {d}/sps.txt
+RPS = {d}/rps.txt
+modeling_type = {mtype}
+modeling_output_folder = {d}/out_
+batch_shots = {batch}
+quiet = true
+inv_type = 0
+inv_max_it = 3
+smooth_per_iteration = true
+gaussian_filter_stdv = 2.0
+gaussian_filter_samples = 5
+inv_residuo_folder = {d}/
+inv_output_folder = {d}/
+inv_data_folder = {d}/
+inv_data_prefix = obs_shot_
+anisotropy = {aniso}
+mig_tables_folder = {d}/tab_
+"""
+
+
+@pytest.fixture(scope="module")
+def exes(engine_lib):
+    from seisfat2d_gb300.host import build as hb
+    out = hb.build()
+    return {k: os.path.join(out, k) for k in ("modeling.exe", "inversion.exe", "traveltime_tables.exe")}
+
+
+def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False):
+    m.astype(np.float32).tofile(os.path.join(d, "slowness.bin"))
+    with open(os.path.join(d, "sps.txt"), "w") as f:
+        f.write("".join(f"{x},{z}\n" for x, z in shots))
+    with open(os.path.join(d, "rps.txt"), "w") as f:
+        f.write("".join(f"{x},{z}\n" for x, z in recs))
+    p = os.path.join(d, "parameters.txt")
+    with open(p, "w") as f:
+        f.write(PARAMS.format(nx=nx, nz=nz, dx=dx, dz=dz, d=d, mtype=mtype, batch="true" if batch else "false",
+                              aniso="true" if aniso else "false"))
+    return p
+
+
+def run(exe, p):
+    r = subprocess.run([exe, p], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_modeling_exe_matches_oracle(oracle, cuda, exes, tmp_path, batch):
+    nx, nz, dx, dz = 80, 40, 10.0, 10.0
+    m = smooth_model(nx, nz, dx, seed=17, noise=0.02)
+    shots = [(100.0, 0.0), (400.0, 50.0), (700.0, 10.0)]
+    recs = [(float(x), 20.0) for x in range(0, 790, 15)]
+    p = write_case(str(tmp_path), nx, nz, dx, dz, m, shots, recs, batch=batch)
+    run(exes["modeling.exe"], p)
+    oracle.set_arith("reference")
+    try:
+        S = oracle.expand_boundary(m)
+        rx = np.array([r[0] for r in recs], np.float32)
+        rz = np.array([r[1] for r in recs], np.float32)
+        for k, (sx, sz) in enumerate(shots):
+            out = np.fromfile(os.path.join(str(tmp_path), f"out_eikonal_iso_nStations{len(recs)}_shot_{k + 1}.bin"),
+                              np.float32)
+            _, po = oracle.shot(S, dx, dz, sx, sz, rx, rz)
+            assert np.array_equal(out, po, equal_nan=True)
+    finally:
+        oracle.set_arith("ieee")
+
+
+def test_modeling_exe_anisotropic(oracle, cuda, exes, tmp_path):
+    from seisfat2d_gb300.synthetic import thomsen_stiffness
+    nx, nz, dx, dz = 60, 30, 10.0, 10.0
+    rng = np.random.default_rng(3)
+    m = smooth_model(nx, nz, dx, seed=23)
+    vp = 1.0 / m.astype(np.float64)
+    cij = thomsen_stiffness(vp, vp / np.sqrt(3.0), 1000.0, rng.uniform(0, .2, (nx, nz)),
+                            rng.uniform(-.05, .1, (nx, nz)), 10.0)
+    for name, c in zip(["C11", "C13", "C15", "C33", "C35", "C55"], cij):
+        c.astype(np.float32).tofile(os.path.join(str(tmp_path), f"model_{name}.bin"))
+    shots = [(300.0, 0.0)]
+    recs = [(float(x), 0.0) for x in range(0, 590, 10)]
+    p = write_case(str(tmp_path), nx, nz, dx, dz, m, shots, recs, mtype=1)
+    run(exes["modeling.exe"], p)
+    oracle.set_arith("reference")
+    try:
+        codes, mm = [], []
+        for c in cij:
+            cd, mn, mx = oracle.compress(oracle.expand_boundary(c.astype(np.float32)))
+            codes.append(cd)
+            mm += [mn, mx]
+        _, po = oracle.shot(oracle.expand_boundary(m), dx, dz, 300.0, 0.0,
+                            np.array([r[0] for r in recs], np.float32), np.zeros(len(recs), np.float32),
+                            ani=(codes, np.array(mm, np.float32)))
+        out = np.fromfile(os.path.join(str(tmp_path), f"out_eikonal_ani_nStations{len(recs)}_shot_1.bin"), np.float32)
+        assert np.array_equal(out, po, equal_nan=True)
+    finally:
+        oracle.set_arith("ieee")
+
+
+def test_traveltime_tables_exe(oracle, cuda, exes, tmp_path):
+    nx, nz, dx, dz = 50, 25, 10.0, 10.0
+    m = smooth_model(nx, nz, dx, seed=29)
+    shots = [(120.0, 0.0), (300.0, 0.0)]
+    recs = [(40.0, 0.0), (450.0, 100.0)]
+    p = write_case(str(tmp_path), nx, nz, dx, dz, m, shots, recs)
+    run(exes["traveltime_tables.exe"], p)
+    oracle.set_arith("reference")
+    try:
+        S = oracle.expand_boundary(m)
+        for kind, pts in (("src", shots), ("rec", recs)):
+            for k, (x, z) in enumerate(pts):
+                T = np.fromfile(os.path.join(str(tmp_path), f"tab_eikonal_{kind}_{k + 1}.bin"), np.float32)
+                assert np.array_equal(T.reshape(S.shape), oracle.solve_f32(S, dx, dz, x, z))
+    finally:
+        oracle.set_arith("ieee")
+
+
+def test_inversion_exe_reduces_residual(oracle, cuda, exes, tmp_path):
+    from seisfat2d_gb300.synthetic import gaussian_smooth
+    nx, nz, dx, dz = 80, 30, 10.0, 10.0
+    true = smooth_model(nx, nz, dx, seed=31, noise=0.0)
+    start = (1.0 / gaussian_smooth(1.0 / true.astype(np.float64), 6.0)).astype(np.float32)
+    shots = [(float(x), 0.0) for x in range(50, 790, 100)]
+    recs = [(float(x), 0.0) for x in range(0, 790, 20)]
+    d = str(tmp_path)
+    p = write_case(d, nx, nz, dx, dz, start, shots, recs)
+    oracle.set_arith("reference")
+    try:
+        St = oracle.expand_boundary(true)
+        rx = np.array([r[0] for r in recs], np.float32)
+        for k, (sx, sz) in enumerate(shots):
+            _, po = oracle.shot(St, dx, dz, sx, sz, rx, np.zeros(len(recs), np.float32))
+            po.astype(np.float32).tofile(os.path.join(d, f"obs_shot_{k + 1}.bin"))
+    finally:
+        oracle.set_arith("ieee")
+    out = run(exes["inversion.exe"], p)
+    res = np.loadtxt(os.path.join(d, "tomography_iso_convergence_3_iterations.txt"))
+    print("residuo per iteration:", res)
+    assert len(res) == 4 and res[-1] < res[0]
+    vp = np.fromfile(os.path.join(d, f"tomography_iso_final_model_vp_{nz}x{nx}.bin"), np.float32)
+    assert np.isfinite(vp).all() and vp.size == nx * nz
