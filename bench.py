@@ -37,7 +37,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0: engine default)")
-    ap.add_argument("--ctas", type=int, default=0, help="CTAs per SM (0: engine default)")
+    ap.add_argument("--gang", type=int, default=0, help="warps per shot (0: automatic)")
     ap.add_argument("--arith", default="reference", choices=["reference", "ieee"])
     return ap.parse_args()
 
@@ -195,8 +195,8 @@ def run_ours(a):
     nrec = len(w.rx)
     eng = Engine(w.nx, w.nz, w.dx, w.dz, device=local)
     eng.set_arithmetic(a.arith)
-    if a.warps or a.ctas:
-        eng.set_launch(a.warps, a.ctas)
+    if a.warps or a.gang:
+        eng.set_launch(a.warps, a.gang)
     eng.set_slowness(w.slowness)
     tab = eng.shot_table(shots)
     dev = torch.device("cuda", local)
@@ -294,7 +294,7 @@ def run_ours(a):
         "config": {"workload": w.name, "nshots": len(w.shots), "nrec": nrec, "grid": [w.nx, w.nz],
                    "padded": [eng.nxx, eng.nzz], "dh": w.dx, "parallelism": f"shots sharded over {world} GPU(s)",
                    "l2": "flushed between timed steps (512 MB write)",
-                   "launch": {"warps": eng.get_launch()[0], "ctas_per_sm": eng.get_launch()[1]},
+                   "launch": {"warps_per_cta": eng.get_launch()[0], "warps_per_shot": eng.get_launch()[1] or "auto"},
                    "arithmetic": eng.get_arithmetic()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": "sf_set_slowness(host model) + sf_batch_forward(host picks)"},

@@ -140,7 +140,7 @@ int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
  * sf_time_propagation in the default (reference) arithmetic, isotropic.
  * S: padded slowness on the current device (nzz x nxx, nzz = nz+6, nxx =
  * nx+6); T: output on the current device (nzz x nxx). Scratch lives in one
- * static device array of 1 MiB + 256 B that every GPU loading the library
+ * static device array of about 8 MiB that every GPU loading the library
  * holds until exit: grids with ceil(nzz/32) * nxx > 262144 are rejected with
  * SF_ERR_RANGE. The first call on a device sets that device up (looks up the
  * array's device address, sets the kernel's shared-memory limit); make it
@@ -151,10 +151,12 @@ int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
 int sf_time_propagation_noalloc(const float* S, int nx, int nz, float dx, float dz, float sx, float sz,
                                 float* T, void* stream);
 
-/* Launch shape: warps per CTA (4..16) and CTAs per SM for batches (1..4);
- * 0 keeps the current value. */
-int sf_set_launch(sf_ctx* ctx, int warps, int ctas_per_sm);
-int sf_get_launch(const sf_ctx* ctx, int* warps, int* ctas_per_sm);
+/* Launch shape. A shot is solved by a gang of CTAs whose warps each run
+ * every k-th 32-row strip. warps: warps per CTA (1..16; 0 keeps the current
+ * value, default 1); gang_warps: warps per shot (0: chosen per batch so that
+ * all shots of the batch are resident at once when possible). */
+int sf_set_launch(sf_ctx* ctx, int warps, int gang_warps);
+int sf_get_launch(const sf_ctx* ctx, int* warps, int* gang_warps);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,7 @@ using namespace sf;
 void sf_adjoint_release(sf_ctx* c)
 {
     void* bufs[] = {c->d_lam, c->d_vrec, c->d_gshot, c->d_pg, c->d_misfit, c->d_colshots, c->d_colptr,
-                    c->d_lam_init, c->d_hand2, c->d_orig_map};
+                    c->d_lam_init, c->d_hand2, c->d_orig_map, c->d_ctr2};
     for (void* b : bufs)
         if (b) cudaFree(b);
 }
@@ -72,12 +72,16 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
 {
     const int ns = (int)c->hshots.size();
     const int nstrips = (c->nzz + 31) / 32;
-    const int grid = std::max(1, std::min(ns, c->sms * c->ctas_per_sm));
-    int rc = sf_dev_reserve(c, (void**)&c->d_lam, &c->cap_lam,
-                            (size_t)grid * c->nzz * c->batch_maxcols * sizeof(float));
-    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_hand2, &c->cap_hand2,
-                                 (size_t)grid * nstrips * c->batch_maxcols * 2 * sizeof(float));
+    const size_t smem = sf_adj_smem_bytes(c->warps);
+    int G, NG;
+    int rc = sf_gang_shape(c, (const void*)k_adjoint, smem, ns, nstrips, c->gang_warps, &G, &NG);
+    if (rc) return rc;
+    rc = sf_dev_reserve(c, (void**)&c->d_lam, &c->cap_lam, (size_t)NG * c->nzz * c->batch_maxcols * sizeof(float));
+    if (!rc) rc = sf_dev_reserve_zero(c, (void**)&c->d_hand2, &c->cap_hand2,
+                                      (size_t)NG * 4 * nstrips * c->batch_maxcols * 2 * sizeof(unsigned long long));
     if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_lam_init, &c->cap_lam_init, (size_t)ns * 9 * sizeof(float));
+    const size_t nctr = (size_t)NG;
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_ctr2, &c->cap_ctr2, nctr * sizeof(unsigned));
     if (rc) return rc;
     rc = prepare_gather(c, st);
     if (rc) return rc;
@@ -91,10 +95,14 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
     p.shots = c->d_shots;
     p.nshots = ns;
     p.nstrips = nstrips;
+    p.G = G;
+    p.NG = NG;
+    p.maxcols = c->batch_maxcols;
     p.lam = c->d_lam;
-    p.lam_per_cta = (long long)c->nzz * c->batch_maxcols;
+    p.lam_per_gang = (long long)c->nzz * c->batch_maxcols;
     p.hand = c->d_hand2;
-    p.hand_per_cta = (long long)nstrips * c->batch_maxcols * 2;
+    p.bar = c->d_ctr2;
+    p.epoch = sf_next_epoch(c);
     p.tcode = c->d_tcode;
     p.tc1 = c->d_tc1;
     p.tc2 = c->d_tc2;
@@ -103,10 +111,9 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
     p.rz = c->d_rz;
     p.nrec = c->batch_nrec;
     p.lam_init = c->d_lam_init;
-    p.counter = c->d_flags + 2;  // flags[2]: adjoint work counter
     p.err = c->d_flags + 1;
-    CK(cudaMemsetAsync(c->d_flags + 2, 0, sizeof(int), st));
-    k_adjoint<<<grid, c->warps * 32, sf_adj_smem_bytes(c->warps), st>>>(p);
+    CK(cudaMemsetAsync(c->d_ctr2, 0, nctr * sizeof(unsigned), st));
+    k_adjoint<<<NG * G, c->warps * 32, smem, st>>>(p);
     CK(cudaGetLastError());
     GatherParams g;
     g.nzz = c->nzz;

@@ -23,7 +23,7 @@
 
 namespace sf {
 
-constexpr int kLP = 34;    // lambda slot pitch: 32 rows, then (pv, pev) handoff
+constexpr int kLP = 36;    // lambda slot pitch: 32 rows, then the {pv,tag},{pev,tag} handoff pairs
 constexpr int kTR = 16;    // tape ring slots (>= kLook + 2)
 constexpr int kTPitch = 72;  // c1[32], c2[32], code bytes (8 words)
 
@@ -40,17 +40,11 @@ struct AdjStripArgs {
     float* tc2;            // overwritten with v = mu * c2
     AdjRing* ring;
     CtaShared* sh;
-    int w_in, e_in, w_out, e_out;
-    const float* h_in;     // (pv, pev) pairs of the upwind strip's last row
-    float* h_out;
+    const unsigned long long* h_in;  // {pv,tag},{pev,tag} of the upwind strip's row (nullptr: first strip)
+    unsigned long long* h_out;       // pairs this strip feeds to the next one (nullptr: last strip)
+    unsigned tag;
     int* err;
 };
-
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
-{
-    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
 
 // SZ, SX: signs of the forward sweep being reversed.
 template <int SZ, int SX>
@@ -69,17 +63,14 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     float* lamg = a.lam;
     const bool lt_ok = (rb + lane) < nzz;
     CtaShared* sh = a.sh;
-    const bool consumer = (lane == 0) && (a.w_in >= 0);
+    const bool consumer = (lane == 0) && (a.h_in != nullptr);
     const int nsteps = ncols + 31;
     auto col_of = [&](int m) { return (SX < 0) ? m : ncols - 1 - m; };
     auto prefetch = [&](int q, int lslot, int tslot) {
         if (q < ncols) {
             const int jq = col_of(q);
             if (lt_ok) cp_async4(&Lr[lslot * kLP + lane], lamg + (size_t)(rb + lane) + (size_t)jq * nzz);
-            if (consumer) {
-                spin_until(&sh->prod[a.w_in], a.e_in + q + 1, sh, a.err);
-                cp_async8(&Lr[lslot * kLP + 32], a.h_in + 2 * (size_t)q);
-            }
+            if (consumer) cp_async16(&Lr[lslot * kLP + 32], a.h_in + 2 * (size_t)q);
         }
         if (q < nsteps) {
             const size_t fs = (size_t)(ncols + 30 - q) * 32;
@@ -90,6 +81,9 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         cp_commit();
     };
 
+    // let the previous strip get kLook+4 columns ahead before the first prefetches
+    if (consumer) wait_pair(a.h_in + 2 * (size_t)min(kLook + 4, ncols - 1) + 1, a.tag, sh, a.err);
+    __syncwarp();
 #pragma unroll 1
     for (int q = 0; q < kLook; q++) prefetch(q, q, q % kTR);
 
@@ -109,9 +103,21 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         const bool act = vrow && (m >= 0) && (m < ncols);
         float pv_in = __shfl_up_sync(0xffffffffu, my_pv, 1);
         float pev_in = __shfl_up_sync(0xffffffffu, my_pev, 1);
-        if (consumer) {
-            pv_in = Lr[m_slot * kLP + 32];
-            pev_in = Lr[m_slot * kLP + 33];
+        if (lane == 0) {  // upwind row of the strip: the previous strip, or outside the grid
+            pv_in = 0.0f;
+            pev_in = 0.0f;
+            if (consumer && s < ncols) {
+                const unsigned long long* e = reinterpret_cast<const unsigned long long*>(&Lr[m_slot * kLP + 32]);
+                const unsigned long long e0 = e[0], e1 = e[1];
+                if (tag_of(e0) == a.tag && tag_of(e1) == a.tag) {
+                    pv_in = val_of(e0);
+                    pev_in = val_of(e1);
+                } else {
+                    pv_in = wait_pair(a.h_in + 2 * (size_t)s, a.tag, sh, a.err);
+                    pev_in = wait_pair(a.h_in + 2 * (size_t)s + 1, a.tag, sh, a.err);
+                    wait_pair(a.h_in + 2 * (size_t)min(s + kLook + 4, ncols - 1) + 1, a.tag, sh, a.err);
+                }
+            }
         }
         const float lam_in = Lr[m_slot * kLP + tix];
         const float c1 = TPr[t_slot * kTPitch + flane];
@@ -137,10 +143,9 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
             }
             Lr[m_slot * kLP + tix] = lo;
             a.tc2[(size_t)(ncols + 30 - s) * 32 + flane] = v;
-            if (lane == 31 && a.w_out >= 0) {
-                reinterpret_cast<float2*>(a.h_out)[m] = make_float2(npv, npev);
-                __threadfence_block();
-                st_volatile(&sh->prod[a.w_out], a.e_out + m + 1);
+            if (lane == 31 && a.h_out != nullptr) {
+                st_u64(a.h_out + 2 * (size_t)m, pack_tag(npv, a.tag));
+                st_u64(a.h_out + 2 * (size_t)m + 1, pack_tag(npev, a.tag));
             }
         }
         my_pv = npv;
@@ -166,10 +171,12 @@ struct AdjParams {
     const ShotDev* shots;   // same table (and order) as the taped forward
     int nshots;
     int nstrips;
-    float* lam;             // per-CTA window adjoint, lam + blockIdx.x * lam_per_cta
-    long long lam_per_cta;
-    float* hand;            // per-CTA handoff pairs
-    long long hand_per_cta;
+    int G, NG, maxcols;     // gangs as in the forward
+    float* lam;             // per-gang window adjoint, lam + gang * lam_per_gang
+    long long lam_per_gang;
+    unsigned long long* hand;  // per gang [4][nstrips][2 * maxcols] tagged (pv, pev) pairs
+    unsigned* bar;          // per gang barrier counter
+    unsigned epoch;         // launch number (tags)
     uint8_t* tcode;
     float* tc1;
     float* tc2;
@@ -178,7 +185,6 @@ struct AdjParams {
     const float* rz;
     int nrec;
     float* lam_init;        // nshots x 9, caller order: adjoint of the 3x3 initial values
-    int* counter;
     int* err;
 };
 
@@ -199,26 +205,29 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_adjoint(AdjParams p)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
     AdjRing* rings = reinterpret_cast<AdjRing*>(smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15)));
-    const int tid = threadIdx.x, W = blockDim.x >> 5, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const GangPos gp = gang_pos(p.G);
+    const int nzz = p.nzz, nstrips = p.nstrips;
+    float* lam = p.lam + (size_t)gp.gang * p.lam_per_gang;
+    unsigned long long* hb = p.hand + (size_t)gp.gang * 4 * nstrips * 2 * p.maxcols;
+    unsigned* bar = p.bar + gp.gang;
+    unsigned nbar = 0;
     if (tid == 0) cs->abort_flag = 0;
     __syncthreads();
-    float* lam = p.lam + (size_t)blockIdx.x * p.lam_per_cta;
-    float* hb = p.hand + (size_t)blockIdx.x * p.hand_per_cta;
-    const int nzz = p.nzz, nstrips = p.nstrips;
+    int it = 0;
 #pragma unroll 1
-    for (;;) {
-        if (tid == 0) cs->item = atomicAdd(p.counter, 1);
-        __syncthreads();
-        const int b = cs->item;
-        __syncthreads();
-        if (b >= p.nshots) break;
+    for (int b = gp.gang; b < p.nshots; b += p.NG, it++) {
         const ShotDev sh = p.shots[b];
         const int ncols = sh.ncols;
-        const size_t n = (size_t)nzz * ncols;
+        const unsigned tag = (p.epoch << 10) | (unsigned)(it & 1023);
         // seed: adjoint of the final field from the pick gradients
-        for (size_t idx = tid; idx < n; idx += blockDim.x) lam[idx] = 0.0f;
-        __syncthreads();
-        if (warp == 0) {
+        for (int k = gp.slot; k < nstrips; k += gp.slots) {
+            const int i = 32 * k + lane;
+            if (i < nzz)
+                for (int j = 0; j < ncols; j++) lam[(size_t)i + (size_t)j * nzz] = 0.0f;
+        }
+        gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+        if (gp.g == 0 && gp.warp == 0) {
             const float* pg = p.pick_grad + (size_t)sh.orig * p.nrec;
             for (int rr = 0; rr < p.nrec; rr++) {
                 const float g = pg[rr];
@@ -237,33 +246,33 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_adjoint(AdjParams p)
                 __syncwarp();
             }
         }
-        __syncthreads();
-        // reverse sweeps 3, 2, 1, 0
+        gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+        // reverse sweeps 3, 2, 1, 0 (consecutive ones run the rows in opposite
+        // directions: no barrier between them, as in the forward)
+        AdjStripArgs a;
+        a.lam = lam;
+        a.nzz = nzz;
+        a.ncols = ncols;
+        a.ring = rings + gp.warp;
+        a.sh = cs;
+        a.err = p.err;
+        a.tag = tag;
 #pragma unroll 1
         for (int sw = 3; sw >= 0; sw--) {
-            if (tid < kMaxWarps) cs->prod[tid] = 0;
-            __syncthreads();
-            const bool fz_pos = !(sw == 1 || sw == 3);  // forward SZ > 0
-            AdjStripArgs a;
-            a.lam = lam;
-            a.nzz = nzz;
-            a.ncols = ncols;
-            a.ring = rings + warp;
-            a.sh = cs;
-            a.err = p.err;
+            const bool fz_pos = !(sw == 1 || sw == 3);  // forward SZ > 0: reverse march goes up
+            unsigned long long* hs = hb + (size_t)sw * nstrips * 2 * p.maxcols;
+            // strips have a fixed owner (strip k -> slot k mod slots) in every sweep;
+            // processing index pidx runs along the reverse march
+            const int first = fz_pos ? ((nstrips - 1 - gp.slot) % gp.slots + gp.slots) % gp.slots : gp.slot;
 #pragma unroll 1
-            for (int pidx = warp; pidx < nstrips; pidx += W) {
+            for (int pidx = first; pidx < nstrips; pidx += gp.slots) {
                 a.k = fz_pos ? nstrips - 1 - pidx : pidx;
-                a.w_in = (pidx > 0) ? warp : -1;
-                a.e_in = chan_entry(pidx, W) * ncols;
-                a.w_out = (pidx < nstrips - 1) ? (pidx + 1) % W : -1;
-                a.e_out = chan_entry(pidx + 1, W) * ncols;
-                a.h_in = hb + 2 * (size_t)pidx * ncols;
-                a.h_out = hb + 2 * (size_t)(pidx + 1) * ncols;
-                const size_t base = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
-                a.tcode = p.tcode + base;
-                a.tc1 = p.tc1 + base;
-                a.tc2 = p.tc2 + base;
+                a.h_in = (pidx > 0) ? hs + 2 * (size_t)pidx * p.maxcols : nullptr;
+                a.h_out = (pidx < nstrips - 1) ? hs + 2 * (size_t)(pidx + 1) * p.maxcols : nullptr;
+                const size_t tb = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
+                a.tcode = p.tcode + tb;
+                a.tc1 = p.tc1 + tb;
+                a.tc2 = p.tc2 + tb;
                 switch (sw) {
                 case 0: adj_strip<1, 1>(a); break;
                 case 1: adj_strip<-1, 1>(a); break;
@@ -271,14 +280,14 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_adjoint(AdjParams p)
                 default: adj_strip<-1, -1>(a); break;
                 }
             }
-            __syncthreads();
         }
-        if (tid < 9) {
+        gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+        if (gp.g == 0 && tid < 9) {
             const int aa = tid % 3, bb = tid / 3;
             const int zi = sh.sIdz + aa - 1, xl = sh.sIdx - sh.c0 + bb - 1;
             p.lam_init[(size_t)sh.orig * 9 + tid] = lam[(size_t)zi + (size_t)xl * nzz];
         }
-        __syncthreads();
+        gang_barrier(bar, (++nbar) * p.G, cs, p.err);
     }
 }
 

@@ -24,6 +24,11 @@ struct Consts {
     float K;           // dz2i * dx2i
     float kA;          // dz2i - dx2i      (tape coefficient)
     float k2K;         // 2 * (dz2i*dx2i)  (tape coefficient)
+    // correctly rounded reciprocals of the four divisors and, per divisor, whether
+    // Markstein's correction step has been verified to equal IEEE division for
+    // every finite dividend (bit 0 dx, 1 dz, 2 hyp, 3 D)
+    float rdx, rdz, rhyp, rD;
+    int mflags;
 };
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
@@ -31,6 +36,22 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// a / b for one of the context's constant divisors b with reciprocal rb =
+// RN(1/b): Markstein's correction step (P. Markstein, IBM J. Res. Dev. 34,
+// 1990): q = RN(a rb), r = a - b q exactly (one FMA), q' = RN(q + r rb).
+// Every step scales exactly with a by powers of two while all values stay
+// normal, so checking the 2^23 dividends of [1, 2) against IEEE division
+// (done per divisor when a context is created) covers every dividend of
+// magnitude in [2^-100, 2^100]; others, and unverified divisors, divide.
+__device__ __forceinline__ float fdiv_k(float a, float b, float rb, bool verified)
+{
+    const unsigned e = (__float_as_uint(a) >> 23) & 0xffu;
+    if (!verified || e - 27u > 200u) return __fdiv_rn(a, b);
+    const float q = __fmul_rn(a, rb);
+    const float r = __fmaf_rn(-q, b, a);
+    return __fmaf_rn(r, rb, q);
+}
 
 // Tape record of one node (adjoint bookkeeping; see the tape description in
 // include/seisfat2d.h). code bits 0-2 candidate, 3 row code, 4 column code.
@@ -68,34 +89,42 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
         float ta = fsub(fadd(tev, te), tv);
         float tb = fadd(fsub(tev, te), tv);
         dd = fsub(ta, tb);
+        float num;
         if (REF) {
             rr = fsqrt(__fmaf_rn(fmul(fmul(4.0f, sref), sref), k.D, -fmul(fmul(k.K, dd), dd)));
-            t1 = fdiv(fadd(__fmaf_rn(tb, k.dz2i, fmul(ta, k.dx2i)), rr), k.D);
+            num = fadd(__fmaf_rn(tb, k.dz2i, fmul(ta, k.dx2i)), rr);
         } else {
             rr = fsqrt(fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd)));
-            t1 = fdiv(fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr), k.D);
+            num = fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr);
         }
+        t1 = fdiv_k(num, k.D, k.rD, k.mflags & 8);
         br = 3;
-    } else if ((dte <= fdiv(fmul(fmul(sref, k.dz), k.dz), k.hyp)) && (dte > 0.0f)) {
-        q = fdiv(dte, k.dz);
-        if (REF) {
-            qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
-            t2 = __fmaf_rn(k.dx, qq, te);
-        } else {
-            qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
-            t2 = fadd(te, fmul(k.dx, qq));
+    } else {
+        // the two edge candidates of modeling.cu:342-353 share one code path:
+        // t2 (from te, step dz) is tried first, t3 (from tv, step dx) otherwise
+        const bool c2 = (dte <= fdiv_k(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4)) && (dte > 0.0f);
+        bool c3 = false;
+        if (!c2)
+            c3 = (dtv <= fdiv_k(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4)) && (dtv > 0.0f);
+        if (c2 || c3) {
+            const float dn = c2 ? dte : dtv;    // te - tev or tv - tev
+            const float hq = c2 ? k.dz : k.dx;  // step the difference is divided by
+            const float rq = c2 ? k.rdz : k.rdx;
+            const bool vq = c2 ? (k.mflags & 2) : (k.mflags & 1);
+            const float hx = c2 ? k.dx : k.dz;  // step that multiplies the root
+            const float bs = c2 ? te : tv;
+            q = fdiv_k(dn, hq, rq, vq);
+            float t;
+            if (REF) {
+                qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
+                t = __fmaf_rn(hx, qq, bs);
+            } else {
+                qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
+                t = fadd(bs, fmul(hx, qq));
+            }
+            if (c2) { t2 = t; br = 4; }
+            else { t3 = t; br = 5; }
         }
-        br = 4;
-    } else if ((dtv <= fdiv(fmul(fmul(sref, k.dx), k.dx), k.hyp)) && (dtv > 0.0f)) {
-        q = fdiv(dtv, k.dx);
-        if (REF) {
-            qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
-            t3 = __fmaf_rn(k.dz, qq, tv);
-        } else {
-            qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
-            t3 = fadd(tv, fmul(k.dz, qq));
-        }
-        br = 5;
     }
     float t2D = fminf(t1, fminf(t2, t3));
     float cand = fminf(t1D, t2D);

@@ -66,6 +66,20 @@ int sf_dev_reserve(sf_ctx* c, void** p, size_t* cap, size_t bytes)
     return SF_OK;
 }
 
+int sf_dev_reserve_zero(sf_ctx* c, void** p, size_t* cap, size_t bytes)
+{
+    const bool grow = !(bytes <= *cap && *p);
+    int rc = sf_dev_reserve(c, p, cap, bytes);
+    if (rc || !grow) return rc;
+    return sf_cuda_check(c, cudaMemset(*p, 0, *cap), "cudaMemset");
+}
+
+unsigned sf_next_epoch(sf_ctx* c)
+{
+    c->epoch = (c->epoch % ((1u << 22) - 1)) + 1;
+    return c->epoch;
+}
+
 // ------------------------------------------------------------------ kernels
 
 namespace {
@@ -80,6 +94,21 @@ __global__ void k_expand(const float* __restrict__ in, int nx, int nz, int nb, f
         int i = (int)(idx % nzz), j = (int)(idx / nzz);
         int si = min(max(i - nb, 0), nz - 1), sj = min(max(j - nb, 0), nx - 1);
         out[idx] = in[si + (size_t)sj * nz];
+    }
+}
+
+// Checks fdiv_k against __fdiv_rn for b = divs[w] over all dividends of [1, 2)
+// (both signs follow by symmetry); rbs[w] = RN(1/b), bad bit w set on any
+// difference.
+__global__ void k_verify_div(const float* divs, int n, float* rbs, int* bad)
+{
+    const unsigned total = (unsigned)n << 23;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int w = t >> 23;
+        const float b = divs[w], rb = __frcp_rn(b);
+        if ((t & 0x7fffffu) == 0) rbs[w] = rb;
+        const float a = __uint_as_float(0x3f800000u | (t & 0x7fffffu));
+        if (__float_as_uint(fdiv_k(a, b, rb, true)) != __float_as_uint(__fdiv_rn(a, b))) atomicOr(bad, 1 << w);
     }
 }
 
@@ -139,6 +168,7 @@ extern "C" int sf_ctx_create(sf_ctx** out, int nx, int nz, float dx, float dz, i
         st = sf_cuda_check(c, cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
         if (st == SF_OK) c->sms = prop.multiProcessorCount;
     }
+    if (st == SF_OK) st = sf_verify_divisors(c);
     size_t cap = 0;
     if (st == SF_OK) st = sf_dev_reserve(c, (void**)&c->d_S, &cap, sizeof(float) * (size_t)c->nxx * c->nzz);
     cap = 0;
@@ -159,7 +189,7 @@ extern "C" int sf_ctx_destroy(sf_ctx* c)
     cudaSetDevice(c->dev);
     sf_adjoint_release(c);
     void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
-                    c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand};
+                    c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand, c->d_ctr};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete c;
@@ -175,14 +205,13 @@ extern "C" int sf_ctx_dims(const sf_ctx* c, int* nxx, int* nzz, int* nb)
     return SF_OK;
 }
 
-extern "C" int sf_set_launch(sf_ctx* c, int warps, int ctas_per_sm)
+extern "C" int sf_set_launch(sf_ctx* c, int warps, int gang_warps)
 {
     if (!c) return SF_ERR_ARG;
-    if (warps && (warps < 2 || warps > kMaxWarps)) return sf_fail(c, SF_ERR_ARG, "warps must be 2..16");
-    if (ctas_per_sm && (ctas_per_sm < 1 || ctas_per_sm > 4))
-        return sf_fail(c, SF_ERR_ARG, "ctas_per_sm must be 1..4");
+    if (warps < 0 || warps > kMaxWarps) return sf_fail(c, SF_ERR_ARG, "warps per CTA must be 1..16");
+    if (gang_warps < 0 || gang_warps > 1024) return sf_fail(c, SF_ERR_ARG, "gang warps must be 0..1024");
     if (warps) c->warps = warps;
-    if (ctas_per_sm) c->ctas_per_sm = ctas_per_sm;
+    c->gang_warps = gang_warps;
     return SF_OK;
 }
 
@@ -201,11 +230,65 @@ extern "C" int sf_get_arithmetic(const sf_ctx* c, int* mode)
     return SF_OK;
 }
 
-extern "C" int sf_get_launch(const sf_ctx* c, int* warps, int* ctas_per_sm)
+extern "C" int sf_get_launch(const sf_ctx* c, int* warps, int* gang_warps)
 {
     if (!c) return SF_ERR_ARG;
     if (warps) *warps = c->warps;
-    if (ctas_per_sm) *ctas_per_sm = c->ctas_per_sm;
+    if (gang_warps) *gang_warps = c->gang_warps;
+    return SF_OK;
+}
+
+// Warps per shot ("slots"): all strips of a shot on their own warp when the
+// device can hold every shot that way, else the largest divisor of the strip
+// count that keeps all shots resident at once (at least 1).
+int sf_gang_shape(sf_ctx* c, const void* kernel, size_t smem, int nshots, int nstrips, int gang_warps, int* G,
+                  int* NG)
+{
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, c->warps * 32, smem));
+    if (per_sm < 1) return sf_fail(c, SF_ERR_CUDA, "kernel does not fit on an SM");
+    const long long cap_ctas = (long long)per_sm * c->sms;
+    int slots = gang_warps;
+    if (slots <= 0) {
+        const long long cap_warps = cap_ctas * c->warps;
+        slots = 1;
+        for (int d = 1; d <= nstrips; d++)
+            if (nstrips % d == 0 && (long long)d * nshots <= cap_warps) slots = d;
+        if ((long long)nstrips * std::max(1, nshots) <= cap_warps) slots = nstrips;
+    }
+    int g = std::max(1, (slots + c->warps - 1) / c->warps);
+    if (g > cap_ctas) g = (int)cap_ctas;
+    *G = g;
+    *NG = (int)std::max(1LL, std::min<long long>(nshots, cap_ctas / g));
+    return SF_OK;
+}
+
+// Reciprocals of the four constant divisors and whether the fast division
+// equals IEEE division for them (see fdiv_k).
+int sf_verify_divisors(sf_ctx* c)
+{
+    Consts& k = c->kc;
+    float h_div[4] = {k.dx, k.dz, k.hyp, k.D}, h_rb[4] = {0, 0, 0, 0};
+    int h_bad = 0;
+    float* d_div = nullptr;
+    int* d_bad = nullptr;
+    CK(cudaMalloc(&d_div, 8 * sizeof(float) + sizeof(int)));
+    d_bad = reinterpret_cast<int*>(d_div + 8);
+    cudaError_t e = cudaMemcpy(d_div, h_div, sizeof(h_div), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_bad, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        k_verify_div<<<c->sms * 8, 256>>>(d_div, 4, d_div + 4, d_bad);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h_rb, d_div + 4, sizeof(h_rb), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&h_bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_div);
+    CK(e);
+    k.rdx = h_rb[0];
+    k.rdz = h_rb[1];
+    k.rhyp = h_rb[2];
+    k.rD = h_rb[3];
+    k.mflags = (~h_bad) & 0xf;
     return SF_OK;
 }
 
@@ -417,26 +500,40 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
     return SF_OK;
 }
 
-int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape,
-                    int grid, cudaStream_t st)
+int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
+                    cudaStream_t st)
 {
     const int nshots = (int)c->hshots.size();
     const size_t nzz = c->nzz;
-    int rc;
+    const int nstrips = (c->nzz + 31) / 32;
+    const size_t smem = sf_fwd_smem_bytes(c->warps);
+    const bool ref = c->arith == SF_ARITH_REFERENCE;
+    const void* kern = ref ? (tape ? (const void*)k_shots<true, true> : (const void*)k_shots<false, true>)
+                           : (tape ? (const void*)k_shots<true, false> : (const void*)k_shots<false, false>);
+    int G, NG;
+    int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
+    if (rc) return rc;
+    c->last_G = G;
+    c->last_NG = NG;
     rc = sf_dev_reserve(c, (void**)&c->d_shots, &c->cap_shots, nshots * sizeof(ShotDev));
     if (rc) return rc;
     CK(cudaMemcpyAsync(c->d_shots, c->hshots.data(), nshots * sizeof(ShotDev), cudaMemcpyHostToDevice, st));
-    const long long t_per_cta = keep_tables ? 0 : (long long)nzz * c->batch_maxcols;
-    const size_t tfloats = keep_tables ? (size_t)c->batch_T_floats : (size_t)grid * t_per_cta;
+    const long long t_per_gang = keep_tables ? 0 : (long long)nzz * c->batch_maxcols;
+    const size_t tfloats = keep_tables ? (size_t)c->batch_T_floats : (size_t)NG * t_per_gang;
     rc = sf_dev_reserve(c, (void**)&c->d_T, &c->cap_T, tfloats * sizeof(float));
     if (rc) return rc;
     if (ani) {
-        rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)grid * nzz * c->batch_maxcols * sizeof(float));
+        rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)NG * nzz * c->batch_maxcols * sizeof(float));
         if (rc) return rc;
     }
-    const long long hand_per_cta = (long long)((nzz + 31) / 32) * c->batch_maxcols;
-    rc = sf_dev_reserve(c, (void**)&c->d_hand, &c->cap_hand, (size_t)grid * hand_per_cta * sizeof(float));
+    rc = sf_dev_reserve_zero(c, (void**)&c->d_hand, &c->cap_hand,
+                             (size_t)NG * 4 * nstrips * c->batch_maxcols * sizeof(unsigned long long));
     if (rc) return rc;
+    const size_t nctr = (size_t)NG;
+    rc = sf_dev_reserve(c, (void**)&c->d_ctr, &c->cap_ctr, nctr * sizeof(unsigned));
+    if (rc) return rc;
+    if ((long long)(nshots + NG - 1) / NG * (ani ? 2 : 1) > 1023)
+        return sf_fail(c, SF_ERR_ARG, "too many shots per gang for one launch; split the batch");
     if (tape) {
         size_t n = (size_t)c->batch_tape_entries;
         rc = sf_dev_reserve(c, (void**)&c->d_tcode, &c->cap_tcode, n);
@@ -453,19 +550,22 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     p.kc = c->kc;
     p.shots = c->d_shots;
     p.nshots = nshots;
+    p.G = G;
+    p.NG = NG;
+    p.maxcols = c->batch_maxcols;
     p.Tpool = c->d_T;
-    p.t_per_cta = t_per_cta;
-    p.counter = c->d_flags;          // flags[0]: work counter
+    p.t_per_gang = t_per_gang;
     p.err = c->d_flags + 1;          // flags[1]: error flag
     p.hand = c->d_hand;
-    p.hand_per_cta = hand_per_cta;
+    p.bar = c->d_ctr;
+    p.epoch = sf_next_epoch(c);
     p.ani = ani;
     if (ani) {
         const size_t npad = (size_t)c->nxx * c->nzz;
         for (int q = 0; q < 6; q++) p.cij[q] = c->d_cij_all + q * npad;
         std::memcpy(p.mm, c->mm, sizeof(p.mm));
         p.Sq = c->d_Sq;
-        p.sq_per_cta = (long long)nzz * c->batch_maxcols;
+        p.sq_per_gang = (long long)nzz * c->batch_maxcols;
     }
     if (tape) {
         p.tcode = c->d_tcode;
@@ -476,10 +576,9 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     p.rz = c->d_rz;
     p.nrec = nrec;
     p.picks = d_picks;
-    CK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
-    const size_t smem = sf_fwd_smem_bytes(c->warps);
-    const dim3 g(grid), b(c->warps * 32);
-    if (c->arith == SF_ARITH_REFERENCE) {
+    CK(cudaMemsetAsync(c->d_ctr, 0, nctr * sizeof(unsigned), st));
+    const dim3 g(NG * G), b(c->warps * 32);
+    if (ref) {
         if (tape) k_shots<true, true><<<g, b, smem, st>>>(p);
         else k_shots<false, true><<<g, b, smem, st>>>(p);
     } else {
@@ -554,8 +653,7 @@ extern "C" int sf_batch_forward(sf_ctx* c, int ani, const sf_shot* shots, int ns
             dp = c->d_picks;
         }
     }
-    const int grid = std::max(1, std::min(nshots, c->sms * c->ctas_per_sm));
-    rc = sf_launch_shots(c, ani, nrec, dp, tables, tape, grid, st);
+    rc = sf_launch_shots(c, ani, nrec, dp, tables, tape, c->gang_warps, st);
     if (rc) return rc;
     c->batch_nshots = nshots;
     c->batch_picks = dp;
@@ -597,7 +695,7 @@ extern "C" int sf_time_propagation(sf_ctx* c, int ani, float sx, float sz, float
         c->d_T = T;
         c->cap_T = npad * sizeof(float);
     }
-    rc = sf_launch_shots(c, ani, 0, nullptr, true, false, 1, st);
+    rc = sf_launch_shots(c, ani, 0, nullptr, true, false, c->gang_warps, st);
     if (T_mem == SF_MEM_DEVICE) {
         c->d_T = keepT;
         c->cap_T = keepcap;

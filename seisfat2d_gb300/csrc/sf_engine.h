@@ -13,8 +13,8 @@ struct sf_ctx {
     float dx = 0.0f, dz = 0.0f;
     sf::Consts kc{};
     int sms = 1;
-    int warps = 8;
-    int ctas_per_sm = 2;
+    int warps = 1;        // warps per CTA
+    int gang_warps = 0;   // warps solving one shot (0: chosen per batch)
     int arith = SF_ARITH_REFERENCE;
     std::string err;
 
@@ -42,7 +42,10 @@ struct sf_ctx {
     float* d_rz = nullptr; size_t cap_rz = 0;
     float* d_picks = nullptr; size_t cap_picks = 0;
     float* d_Sq = nullptr; size_t cap_Sq = 0;
-    float* d_hand = nullptr; size_t cap_hand = 0;
+    unsigned long long* d_hand = nullptr; size_t cap_hand = 0;
+    unsigned* d_ctr = nullptr; size_t cap_ctr = 0;
+    unsigned epoch = 0;  // launches so far (handoff tags)
+    int last_G = 1, last_NG = 1;
     uint8_t* d_tcode = nullptr; size_t cap_tcode = 0;
     float* d_tc1 = nullptr; size_t cap_tc1 = 0;
     float* d_tc2 = nullptr; size_t cap_tc2 = 0;
@@ -57,20 +60,30 @@ struct sf_ctx {
     int* d_colptr = nullptr; size_t cap_colptr = 0;
     int* d_orig_map = nullptr; size_t cap_orig_map = 0;
     float* d_lam_init = nullptr; size_t cap_lam_init = 0;
-    float* d_hand2 = nullptr; size_t cap_hand2 = 0;
+    unsigned long long* d_hand2 = nullptr; size_t cap_hand2 = 0;
+    unsigned* d_ctr2 = nullptr; size_t cap_ctr2 = 0;
     std::vector<int> h_colptr, h_colshots;
 };
 
 int sf_fail(sf_ctx* c, int status, const std::string& msg);
 int sf_cuda_check(sf_ctx* c, cudaError_t e, const char* what);
 int sf_dev_reserve(sf_ctx* c, void** p, size_t* cap, size_t bytes);
+// Same, zero-filled whenever it (re)allocates.
+int sf_dev_reserve_zero(sf_ctx* c, void** p, size_t* cap, size_t bytes);
+// Next handoff-tag epoch (never 0; wraps within 22 bits).
+unsigned sf_next_epoch(sf_ctx* c);
 int sf_check_flags(sf_ctx* c, cudaStream_t st);
 int sf_fwd_setup(sf_ctx* c);
+int sf_verify_divisors(sf_ctx* c);
 size_t sf_fwd_smem_bytes(int warps);
 void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4]);
 int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape);
-int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int grid,
+int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
                     cudaStream_t st);
+// Gang shape for nshots shots of nstrips strips: CTAs per gang and gangs, so
+// that every gang of the grid is resident at once.
+int sf_gang_shape(sf_ctx* c, const void* kernel, size_t smem, int nshots, int nstrips, int gang_warps, int* G,
+                  int* NG);
 void sf_adjoint_release(sf_ctx* c);
 int sf_adj_setup(sf_ctx* c);
 int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t st);

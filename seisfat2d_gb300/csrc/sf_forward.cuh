@@ -26,18 +26,21 @@ struct FwdParams {
     Consts kc;
     const ShotDev* shots;
     int nshots;
+    int G;                // CTAs per gang (one gang solves one shot at a time)
+    int NG;               // gangs; gang k solves shots k, k+NG, ...
+    int maxcols;          // widest window of the batch
     float* Tpool;
-    long long t_per_cta;  // > 0: each CTA reuses Tpool + blockIdx.x * t_per_cta
-    int* counter;
+    long long t_per_gang; // > 0: each gang reuses Tpool + gang * t_per_gang
     int* err;
-    float* hand;          // strip handoff buffer, hand + blockIdx.x * hand_per_cta
-    long long hand_per_cta;  // >= nstrips * widest window
+    unsigned long long* hand;  // tagged strip handoff pairs: per gang [4 sweeps][nstrips][maxcols]
+    unsigned* bar;        // per gang barrier counter
+    unsigned epoch;       // launch number (tags: epoch << 10 | shot-solve number)
     // anisotropy
     int ani;
     const uint16_t* cij[6];
     float mm[12];
-    float* Sq;            // qP slowness scratch, Sq + blockIdx.x * sq_per_cta
-    long long sq_per_cta;
+    float* Sq;            // qP slowness, Sq + gang * sq_per_gang
+    long long sq_per_gang;
     // tape
     uint8_t* tcode;
     float* tc1;
@@ -74,18 +77,35 @@ __device__ __forceinline__ size_t tape_strip_base(long long tape_off, int sweep,
     return (size_t)tape_off + ((size_t)sweep * nstrips + k) * (size_t)(ncols + 31) * 32;
 }
 
-// Position of strip p (p >= 1) among the strips fed through handoff channel
-// p % W: channel 0 carries W, 2W, ..., channel w > 0 carries w, w+W, ...
-__device__ __forceinline__ int chan_entry(int p, int W) { return p / W - ((p % W == 0) ? 1 : 0); }
+// Where a gang's warps sit: warp w of CTA g of the gang is slot w*G + g.
+// Strip k belongs to slot k mod slots in every sweep, so consecutive strips
+// run on different CTAs and SMs and a warp only rereads rows it wrote.
+struct GangPos {
+    int gang, g, warp, slot, slots;
+};
 
-// The four sweeps of one solve on the window held by this CTA.
-template <bool TAPE, bool REF>
-__device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float* Sw, int ldS,
-                             float* T, CtaShared* cs, WarpRing* rings)
+__device__ __forceinline__ GangPos gang_pos(int G)
 {
-    const int W = blockDim.x >> 5, warp = threadIdx.x >> 5;
+    GangPos q;
+    q.gang = blockIdx.x / G;
+    q.g = blockIdx.x % G;
+    q.warp = threadIdx.x >> 5;
+    q.slots = G * (blockDim.x >> 5);
+    q.slot = q.warp * G + q.g;
+    return q;
+}
+
+// The four sweeps of one solve of the current shot; every warp of the gang
+// runs the strips of its slot. No barrier between sweeps: consecutive sweeps
+// run the rows in opposite directions, a warp rereads only rows it wrote
+// itself, and the handoff chain orders everything else.
+template <bool TAPE, bool REF>
+__device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPos& gp, const float* Sw,
+                             int ldS, float* T, unsigned tag, CtaShared* cs, WarpRing* rings)
+{
     const int nzz = p.nzz, ncols = sh.ncols;
     const int nstrips = (nzz + 31) >> 5;
+    unsigned long long* hb = p.hand + (size_t)gp.gang * 4 * nstrips * p.maxcols;
     StripArgs a;
     a.S = Sw;
     a.ldS = ldS;
@@ -97,30 +117,25 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float*
     a.sIdx = sh.sIdx - sh.c0;
     a.kc = p.kc;
     a.init = cs->init;
-    a.ring = rings + warp;
+    a.ring = rings + gp.warp;
     a.sh = cs;
     a.err = p.err;
     a.tcode = nullptr;
     a.tc1 = nullptr;
     a.tc2 = nullptr;
-    float* hb = p.hand + (size_t)blockIdx.x * p.hand_per_cta;
+    a.tag = tag;
 #pragma unroll 1
     for (int sw = 0; sw < 4; sw++) {
-        if (threadIdx.x < kMaxWarps) cs->prod[threadIdx.x] = 0;
-        __syncthreads();
         const bool szpos = !(sw == 1 || sw == 3);
         a.skip_i = sh.skip_i[sw];
         a.skip_j = sh.skip_j[sw];
+        unsigned long long* hs = hb + (size_t)sw * nstrips * p.maxcols;
+        const int first = szpos ? gp.slot : ((nstrips - 1 - gp.slot) % gp.slots + gp.slots) % gp.slots;
 #pragma unroll 1
-        for (int pidx = warp; pidx < nstrips; pidx += W) {
+        for (int pidx = first; pidx < nstrips; pidx += gp.slots) {
             a.k = szpos ? pidx : nstrips - 1 - pidx;
-            // channel w carries strips p = w, w+W, ... (p >= 1) back to back
-            a.w_in = (pidx > 0) ? warp : -1;
-            a.e_in = chan_entry(pidx, W) * ncols;
-            a.w_out = (pidx < nstrips - 1) ? (pidx + 1) % W : -1;
-            a.e_out = chan_entry(pidx + 1, W) * ncols;
-            a.h_in = hb + (size_t)pidx * ncols;
-            a.h_out = hb + (size_t)(pidx + 1) * ncols;
+            a.h_in = (pidx > 0) ? hs + (size_t)pidx * p.maxcols : nullptr;
+            a.h_out = (pidx < nstrips - 1) ? hs + (size_t)(pidx + 1) * p.maxcols : nullptr;
             if (TAPE) {
                 size_t base = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
                 a.tcode = p.tcode + base;
@@ -134,10 +149,12 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const float*
             default: run_strip<-1, -1, false, TAPE, REF>(a); break;
             }
         }
-        __syncthreads();
     }
 }
 
+// Persistent gangs of G CTAs: gang k solves shots k, k+NG, ... (shots are
+// sorted widest window first). The grid never exceeds what the device can
+// hold at once, so every gang's CTAs are resident together.
 template <bool TAPE, bool REF>
 __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
 {
@@ -145,65 +162,71 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
     WarpRing* rings = reinterpret_cast<WarpRing*>(smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15)));
     const int tid = threadIdx.x;
+    const GangPos gp = gang_pos(p.G);
+    const int nzz = p.nzz;
+    const int nstrips = (nzz + 31) >> 5;
+    unsigned* bar = p.bar + gp.gang;
+    unsigned nbar = 0;
     if (tid == 0) cs->abort_flag = 0;
     __syncthreads();
+    const int nsolves = p.ani ? 2 : 1;
+    int it = 0;
 #pragma unroll 1
-    for (;;) {
-        if (tid == 0) cs->item = atomicAdd(p.counter, 1);
-        __syncthreads();
-        const int b = cs->item;
-        __syncthreads();
-        if (b >= p.nshots) break;
+    for (int b = gp.gang; b < p.nshots; b += p.NG, it++) {
         const ShotDev sh = p.shots[b];
-        const int nzz = p.nzz, ncols = sh.ncols;
-        float* T = (p.t_per_cta > 0) ? p.Tpool + (size_t)blockIdx.x * p.t_per_cta
-                                     : p.Tpool + sh.t_off;
+        const int ncols = sh.ncols;
+        float* T = (p.t_per_gang > 0) ? p.Tpool + (size_t)gp.gang * p.t_per_gang : p.Tpool + sh.t_off;
         const float* Sw = p.S + (size_t)sh.c0 * nzz;
+        const unsigned tag = (p.epoch << 10) | (unsigned)((it * nsolves) & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE, REF>(p, sh, Sw, nzz, T, cs, rings);
+        solve_window<TAPE, REF>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
         if (p.ani) {
-            // get_quasi_slowness (eikonal_ani.cu:47-111) on the window
-            float* Sq = p.Sq + (size_t)blockIdx.x * p.sq_per_cta;
-            const int sloc = sh.sIdx - sh.c0, nb = p.nb;
-            const size_t n = (size_t)nzz * ncols;
-            for (size_t idx = tid; idx < n; idx += blockDim.x) {
-                const int i = (int)(idx % nzz), j = (int)(idx / nzz);
-                const size_t g = (size_t)i + (size_t)(sh.c0 + j) * nzz;
-                float s = p.S[g];
-                float out = s;
-                if (i >= nb && i < nzz - nb && j >= nb && j < ncols - nb && !(i == sh.sIdz && j == sloc)) {
-                    const float* Tc = T + idx;
-                    out = qp_slowness<REF>(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz,
-                                      decode_c(p.cij[0][g], p.mm[0], p.mm[1]),
-                                      decode_c(p.cij[1][g], p.mm[2], p.mm[3]),
-                                      decode_c(p.cij[2][g], p.mm[4], p.mm[5]),
-                                      decode_c(p.cij[3][g], p.mm[6], p.mm[7]),
-                                      decode_c(p.cij[4][g], p.mm[8], p.mm[9]),
-                                      decode_c(p.cij[5][g], p.mm[10], p.mm[11]));
+            // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
+            // warp's strips, once the whole first solve is done
+            gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+            float* Sq = p.Sq + (size_t)gp.gang * p.sq_per_gang;
+            const int sloc = sh.sIdx - sh.c0, nb = p.nb, lane = tid & 31;
+            for (int k = gp.slot; k < nstrips; k += gp.slots) {  // the rows of this warp's strips
+                const int i = 32 * k + lane;
+                if (i >= nzz) continue;
+                for (int j = 0; j < ncols; j++) {
+                    const size_t idx = (size_t)i + (size_t)j * nzz;
+                    const size_t g = (size_t)i + (size_t)(sh.c0 + j) * nzz;
+                    float s = p.S[g];
+                    float out = s;
+                    if (i >= nb && i < nzz - nb && j >= nb && j < ncols - nb && !(i == sh.sIdz && j == sloc)) {
+                        const float* Tc = T + idx;
+                        out = qp_slowness<REF>(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz,
+                                               decode_c(p.cij[0][g], p.mm[0], p.mm[1]),
+                                               decode_c(p.cij[1][g], p.mm[2], p.mm[3]),
+                                               decode_c(p.cij[2][g], p.mm[4], p.mm[5]),
+                                               decode_c(p.cij[3][g], p.mm[6], p.mm[7]),
+                                               decode_c(p.cij[4][g], p.mm[8], p.mm[9]),
+                                               decode_c(p.cij[5][g], p.mm[10], p.mm[11]));
+                    }
+                    Sq[idx] = out;
                 }
-                Sq[idx] = out;
             }
-            __syncthreads();
-            {
+            gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+            if (tid < 9) {
                 // second time_init reads the qP field (window-local columns)
-                if (tid < 9) {
-                    const int a = tid % 3, bb = tid / 3;
-                    const int zi = sh.sIdz + a - 1, xl = sloc + bb - 1;
-                    const float s = Sq[zi + (size_t)xl * nzz];
-                    if (REF)
-                        cs->init[tid] = src_value_f32(s, zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
-                    else
-                        cs->init[tid] = __double2float_rn(__dmul_rn(
-                            (double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
-                }
+                const int a = tid % 3, bb = tid / 3;
+                const int zi = sh.sIdz + a - 1, xl = sloc + bb - 1;
+                const float s = Sq[zi + (size_t)xl * nzz];
+                if (REF)
+                    cs->init[tid] = src_value_f32(s, zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
+                else
+                    cs->init[tid] = __double2float_rn(
+                        __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
             }
             __syncthreads();
-            solve_window<false, REF>(p, sh, Sq, nzz, T, cs, rings);
+            solve_window<false, REF>(p, sh, gp, Sq, nzz, T, tag + 1u, cs, rings);
         }
-        // receivers (modeling.cu:161-194)
+        // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {
-            for (int r = tid; r < p.nrec; r += blockDim.x) {
+            gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+            for (int r = (gp.g * (blockDim.x >> 5) + gp.warp) * 32 + (tid & 31); r < p.nrec; r += gp.slots * 32) {
                 int i, j;
                 float xd, zd;
                 float v = __int_as_float(0x7fc00000);
@@ -212,7 +235,8 @@ __global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
                 p.picks[(size_t)sh.orig * p.nrec + r] = v;
             }
         }
-        __syncthreads();
+        // the gang's buffers are reused by its next shot
+        gang_barrier(bar, (++nbar) * p.G, cs, p.err);
     }
 }
 

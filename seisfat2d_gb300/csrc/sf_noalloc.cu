@@ -19,25 +19,29 @@ using namespace sf;
 
 namespace {
 
-// Scratch capacity: strip-handoff values for up to kNoAllocHandoff floats
-// (ceil(nzz/32) strips x nxx columns), i.e. 1 MiB, plus a 256-byte header.
-constexpr size_t kNoAllocHandoff = 262144;
+// Scratch capacity: the tagged strip-handoff pairs of the four sweeps for
+// grids with ceil(nzz/32) * nxx <= kNoAllocCells (4 x 8 bytes each: 8 MiB),
+// plus a 256-byte header with the launch's error flag, barrier counter,
+// epoch and shot descriptor.
+constexpr size_t kNoAllocCells = 262144;
 constexpr size_t kNoAllocHeader = 256;
 
 struct NoAllocHeader {
-    int counter;   // work counter of the launch (must start at 0)
-    int err;       // in-kernel wait timeout flag (must start at 0)
-    int pad[2];
-    ShotDev shot;  // the one shot of the call
+    int err;           // in-kernel wait timeout flag (must start at 0)
+    unsigned bar;      // gang barrier counter (must start at 0)
+    unsigned epoch;    // handoff tag epoch of the last call (host copy below)
+    int pad;
+    ShotDev shot;      // the one shot of the call
 };
-static_assert(sizeof(NoAllocHeader) <= kNoAllocHeader, "header too large");
+static_assert(sizeof(NoAllocHeader) <= 256, "header too large");
 
 // Shared by every call on a device; keeps the last call's contents.
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHeader + kNoAllocHandoff * sizeof(float)];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHeader + 4 * kNoAllocCells * sizeof(unsigned long long)];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char* g_scratch_addr[kMaxDevices] = {};  // device address of the array, per device
+unsigned g_epoch[kMaxDevices] = {};               // handoff tag epoch per device
 
 // Once per device, with that device current: the device address of the
 // scratch array (host code only knows a stand-in for the symbol) and the
@@ -52,6 +56,9 @@ int noalloc_setup(int dev, unsigned char** addr)
         if (cudaFuncSetAttribute(k_shots<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sf_fwd_smem_bytes(kMaxWarps)) != cudaSuccess)
             return SF_ERR_CUDA;
+        // the tagged pairs must not start with a valid-looking tag
+        if (cudaMemset(p, 0, sizeof(g_noalloc_scratch)) != cudaSuccess) return SF_ERR_CUDA;
+        if (cudaDeviceSynchronize() != cudaSuccess) return SF_ERR_CUDA;
         g_scratch_addr[dev] = static_cast<unsigned char*>(p);
     }
     *addr = g_scratch_addr[dev];
@@ -66,7 +73,7 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     if (!S || !T || nx < 2 || nz < 2 || !(dx > 0.0f) || !(dz > 0.0f)) return SF_ERR_ARG;
     const int nb = 3, nxx = nx + 2 * nb, nzz = nz + 2 * nb;
     const size_t nstrips = (size_t)(nzz + 31) / 32;
-    if (nstrips * (size_t)nxx > kNoAllocHandoff) return SF_ERR_RANGE;  // grid beyond the scratch capacity
+    if (nstrips * (size_t)nxx > kNoAllocCells) return SF_ERR_RANGE;  // grid beyond the scratch capacity
     // source node (modeling.cu:112-113)
     const float fx = (sx + 0.5f * dx) / dx, fz = (sz + 0.5f * dz) / dz;
     if (!(fx > -1e9f && fx < 1e9f && fz > -1e9f && fz < 1e9f)) return SF_ERR_RANGE;
@@ -86,8 +93,15 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     int rc = noalloc_setup(dev, &base);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    unsigned epoch;
+    {
+        std::lock_guard<std::mutex> lock(g_setup_mutex);
+        g_epoch[dev] = (g_epoch[dev] % ((1u << 22) - 1)) + 1;
+        epoch = g_epoch[dev];
+    }
     NoAllocHeader hdr{};
-    hdr.shot = sh;  // counter and err start at zero
+    hdr.shot = sh;  // err and the barrier counter start at zero
+    hdr.epoch = epoch;
     if (cudaMemcpyAsync(base, &hdr, sizeof(hdr), cudaMemcpyHostToDevice, st) != cudaSuccess) return SF_ERR_CUDA;
     NoAllocHeader* dh = reinterpret_cast<NoAllocHeader*>(base);
 
@@ -101,6 +115,8 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     k.K = k.dz2i * k.dx2i;
     k.kA = k.dz2i - k.dx2i;
     k.k2K = 2.0f * k.K;
+    k.rdx = k.rdz = k.rhyp = k.rD = 0.0f;
+    k.mflags = 0;  // plain IEEE division: the fast-division check needs a buffer
     FwdParams p{};
     p.S = S;
     p.nzz = nzz;
@@ -109,12 +125,15 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     p.kc = k;
     p.shots = &dh->shot;
     p.nshots = 1;
+    p.G = 1;  // one CTA of 8 warps solves the shot
+    p.NG = 1;
+    p.maxcols = nxx;
     p.Tpool = T;
-    p.t_per_cta = 0;
-    p.counter = &dh->counter;
+    p.t_per_gang = 0;
     p.err = &dh->err;
-    p.hand = reinterpret_cast<float*>(base + kNoAllocHeader);
-    p.hand_per_cta = (long long)nstrips * nxx;
+    p.hand = reinterpret_cast<unsigned long long*>(base + kNoAllocHeader);
+    p.bar = &dh->bar;
+    p.epoch = epoch;
     const int warps = 8;
     k_shots<false, true><<<1, warps * 32, sf_fwd_smem_bytes(warps), st>>>(p);
     if (cudaGetLastError() != cudaSuccess) return SF_ERR_CUDA;

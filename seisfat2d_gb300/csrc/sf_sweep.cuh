@@ -6,13 +6,16 @@
 // lane l updates node (row(l), column of march index s-l), so the three upwind
 // values of the reference update (modeling.cu:324-326) are: the lane above's
 // result of the previous step (shfl), the lane's own previous result, and the
-// lane's own previous upwind value. Consecutive strips are chained through a
-// per-CTA global buffer: the last lane of strip p writes its row, column by
-// column, and publishes a counter in shared memory; lane 0 of strip p+1
-// prefetches those values through the same cp.async pipeline as its own
-// columns (bounded spin on the counter). Producers never wait on consumers, so
-// every wait points to a lower strip and the schedule cannot deadlock however
-// many strips share a warp.
+// lane's own previous upwind value. Consecutive strips are chained through
+// global memory without fences: the last lane of strip p writes each value of
+// its row together with a tag (launch epoch and shot number) as one 64-bit
+// store; lane 0 of strip p+1 (usually on another SM) prefetches the pair
+// through the same cp.async pipeline as its own columns and checks the tag.
+// A stale pair (the producer has not got there yet) sends lane 0 into a
+// bounded spin on the pair itself, after which it waits kLook+4 columns
+// further ahead so later prefetches find their data. Producers never wait on
+// consumers, so every wait points to a lower strip and the schedule cannot
+// deadlock however strips are spread over warps and CTAs.
 //
 // Column chunks are staged into a per-warp shared-memory ring by cp.async:
 // at step s the warp fetches march column s+LOOK (32 consecutive rows = one
@@ -31,7 +34,7 @@ namespace sf {
 
 constexpr int kRing = 48;   // column slots per warp ring (>= 32 + kLook + 1)
 constexpr int kLook = 12;   // prefetch distance in march columns
-constexpr int kSP = 34;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff at 33
+constexpr int kSP = 36;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff pair at 34..35
 constexpr int kTP = 32;     // T slot pitch
 constexpr int kMaxWarps = 16;
 constexpr long long kSpinLimit = 1ll << 30;          // iterations
@@ -42,10 +45,9 @@ struct WarpRing {
     float T[kRing * kTP];
 };
 
-// Per-CTA shared state (static part), followed by kMaxWarps WarpRing blocks in
-// dynamic shared memory (only the CTA's warps are used).
+// Per-CTA shared state (static part), followed by the CTA's WarpRing blocks in
+// dynamic shared memory.
 struct CtaShared {
-    int prod[kMaxWarps];             // handoff entries published on channel w
     int abort_flag;
     int item;
     float init[9];
@@ -56,12 +58,48 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
     unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
+{
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
 __device__ __forceinline__ void st_volatile(int* p, int v) { *(volatile int*)p = v; }
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_u64(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long pack_tag(float v, unsigned tag)
+{
+    return ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
+}
+__device__ __forceinline__ unsigned tag_of(unsigned long long e) { return (unsigned)(e >> 32); }
+__device__ __forceinline__ float val_of(unsigned long long e) { return __uint_as_float((unsigned)e); }
 
 // Everything one warp needs for one strip of one sweep.
 struct StripArgs {
@@ -77,10 +115,9 @@ struct StripArgs {
     const float* init;  // 9 values in shared memory
     WarpRing* ring;
     CtaShared* sh;
-    int w_in, e_in;     // consumer side: channel and entry base (-1: first strip)
-    int w_out, e_out;   // producer side (-1: last strip)
-    const float* h_in;  // handoff values of this strip's upwind row, by march column
-    float* h_out;       // handoff values this strip feeds to the next one
+    const unsigned long long* h_in;  // {value, tag} of the upwind strip's row by march column (nullptr: first strip)
+    unsigned long long* h_out;       // pairs this strip feeds to the next one (nullptr: last strip)
+    unsigned tag;                    // tag of this shot's pairs
     // tape (TAPE only): base of this sweep/strip, entries [step*32 + lane]
     uint8_t* tcode;
     float* tc1;
@@ -95,28 +132,47 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Bounded wait for *p >= target. On timeout it raises the CTA's abort flag and
-// the launch's error flag, and every later wait returns at once, so the
-// kernel always finishes (its results are then void and the host reports
-// SF_ERR_TIMEOUT).
-__device__ __forceinline__ bool spin_until(const int* p, int target, CtaShared* sh, int* err)
+// Bounded wait until the pair at p carries `tag`; returns its value. On
+// timeout it behaves like wait_counter.
+__device__ __forceinline__ float wait_pair(const unsigned long long* p, unsigned tag, CtaShared* sh, int* err)
 {
-    if (ld_volatile(p) >= target) {
-        __threadfence_block();
-        return true;
-    }
+    unsigned long long e = ld_relaxed_u64(p);
+    if (tag_of(e) == tag) return val_of(e);
     const unsigned long long t0 = global_ns();
     long long n = 0;
-    while (ld_volatile(p) < target) {
-        if (ld_volatile(&sh->abort_flag)) return false;
-        if (++n > kSpinLimit || ((n & 1023) == 0 && global_ns() - t0 > kSpinNs)) {
+    while (tag_of(e = ld_relaxed_u64(p)) != tag) {
+        if (ld_volatile(&sh->abort_flag) || *(volatile int*)err) return 0.0f;
+        __nanosleep(32);
+        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > kSpinNs)) {
             st_volatile(&sh->abort_flag, 1);
             atomicExch(err, 2);
-            return false;
+            return 0.0f;
         }
     }
-    __threadfence_block();
-    return true;
+    return val_of(e);
+}
+
+// Bounded wait until the counter at p reaches `target` (acquire); returns
+// the value seen. On timeout it raises the CTA's abort flag and the launch's
+// error flag and returns `target`, and every later wait of the CTA (or of any
+// CTA once the launch's flag is up) returns at once, so the kernel always
+// finishes (its results are then void and the host reports SF_ERR_TIMEOUT).
+__device__ __forceinline__ unsigned wait_counter(const unsigned* p, unsigned target, CtaShared* sh, int* err)
+{
+    unsigned v = ld_acquire_gpu(p);
+    if (v >= target) return v;
+    const unsigned long long t0 = global_ns();
+    long long n = 0;
+    while ((v = ld_acquire_gpu(p)) < target) {
+        if (ld_volatile(&sh->abort_flag) || *(volatile int*)err) return target;
+        __nanosleep(64);
+        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > kSpinNs)) {
+            st_volatile(&sh->abort_flag, 1);
+            atomicExch(err, 2);
+            return target;
+        }
+    }
+    return v;
 }
 
 template <int SZ, int SX, bool SW0, bool TAPE, bool REF>
@@ -144,26 +200,34 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     const bool lt_ok = (rb + lane) < nzz;
     const float* Sg = a.S;
     float* Tg = a.T;
-    const size_t ldS = (size_t)a.ldS;
+    const int ldS = a.ldS;
 
     CtaShared* sh = a.sh;
-    const bool consumer = (lane == 0) && (a.w_in >= 0);
+    const bool consumer = (lane == 0) && (a.h_in != nullptr);
     auto col_of = [&](int m) { return (SX > 0) ? m : ncols - 1 - m; };
+    // running source addresses of march column q (q advances by one per call)
+    const long long dcol = (SX > 0) ? 1 : -1;
+    const float* pS = Sg + (size_t)ls_row + (long long)col_of(0) * (long long)ldS;
+    const float* pX = Sg + (size_t)(rb + 31) + (long long)col_of(0) * (long long)ldS;
+    const float* pT = Tg + (size_t)(rb + lane) + (long long)col_of(0) * (long long)nzz;
+    const long long dS = dcol * (long long)ldS, dT = dcol * (long long)nzz;
     auto prefetch = [&](int q, int slot) {
         if (q < ncols) {
-            const int jq = col_of(q);
-            if (ls_ok) cp_async4(&Sring[slot * kSP + lane], Sg + (size_t)ls_row + (size_t)jq * ldS);
-            if (lx_ok) cp_async4(&Sring[slot * kSP + 32], Sg + (size_t)(rb + 31) + (size_t)jq * ldS);
-            if (!SW0 && lt_ok)
-                cp_async4(&Tring[slot * kTP + lane], Tg + (size_t)(rb + lane) + (size_t)jq * nzz);
-            if (consumer) {
-                // upwind-row value of march q, once the previous strip has published it
-                spin_until(&sh->prod[a.w_in], a.e_in + q + 1, sh, a.err);
-                cp_async4(&Sring[slot * kSP + 33], a.h_in + q);
-            }
+            if (ls_ok) cp_async4(&Sring[slot * kSP + lane], pS);
+            if (lx_ok) cp_async4(&Sring[slot * kSP + 32], pX);
+            if (!SW0 && lt_ok) cp_async4(&Tring[slot * kTP + lane], pT);
+            if (consumer) cp_async8(&Sring[slot * kSP + 34], a.h_in + q);  // upwind-row pair of march q
         }
         cp_commit();
+        pS += dS;
+        pX += dS;
+        pT += dT;
     };
+
+    // let the previous strip get kLook+4 columns ahead before the first
+    // prefetches of its values
+    if (consumer) wait_pair(a.h_in + min(kLook + 4, ncols - 1), a.tag, sh, a.err);
+    __syncwarp();
 
     // prologue: march columns 0 .. kLook-1
 #pragma unroll 1
@@ -192,7 +256,17 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
         // upwind value from the lane above (or the previous strip)
         float tv = __shfl_up_sync(0xffffffffu, tn, 1);
-        if (consumer) tv = Sring[m_slot * kSP + 33];
+        if (consumer && s < ncols) {
+            const unsigned long long e = *reinterpret_cast<const unsigned long long*>(&Sring[m_slot * kSP + 34]);
+            if (tag_of(e) == a.tag) {
+                tv = val_of(e);
+            } else {
+                // the previous strip had not written this column when it was prefetched:
+                // wait for it, then fall kLook+4 columns behind so later prefetches hit
+                tv = wait_pair(a.h_in + s, a.tag, sh, a.err);
+                wait_pair(a.h_in + min(s + kLook + 4, ncols - 1), a.tag, sh, a.err);
+            }
+        }
         const float te = tn, tev = tvp;
 
         float told;
@@ -236,11 +310,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         }
 
         // feed the next strip: lane 31 just finished march s-31
-        if (lane == 31 && a.w_out >= 0 && act) {
-            a.h_out[m] = tnew;
-            __threadfence_block();
-            st_volatile(&sh->prod[a.w_out], a.e_out + m + 1);
-        }
+        if (lane == 31 && a.h_out != nullptr && act) st_u64(a.h_out + m, pack_tag(tnew, a.tag));
 
         // write back the column every lane has finished
         const int mw = s - 31;
@@ -259,6 +329,20 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     }
     cp_wait<0>();
     __syncwarp();
+}
+
+// Gang-wide barrier: every CTA of the gang arrives once per barrier instance;
+// `target` = (instance + 1) * gang size. Bounded like every wait.
+__device__ __forceinline__ void gang_barrier(unsigned* ctr, unsigned target, CtaShared* sh, int* err)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        wait_counter(ctr, target, sh, err);
+        __threadfence();
+    }
+    __syncthreads();
 }
 
 }  // namespace sf

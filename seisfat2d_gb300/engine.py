@@ -201,8 +201,9 @@ class Engine:
         self.L.sf_get_arithmetic(self._ctx, C.byref(v))
         return "reference" if v.value == _lib.SF_ARITH_REFERENCE else "ieee"
 
-    def set_launch(self, warps=0, ctas_per_sm=0):
-        self._check(self.L.sf_set_launch(self._ctx, int(warps), int(ctas_per_sm)), "sf_set_launch")
+    def set_launch(self, warps=0, gang_warps=0):
+        """warps per CTA (0 keeps it) and warps per shot (0: automatic)."""
+        self._check(self.L.sf_set_launch(self._ctx, int(warps), int(gang_warps)), "sf_set_launch")
 
     def get_launch(self):
         a, b = C.c_int(), C.c_int()

@@ -80,13 +80,13 @@ def test_fp32_within_1e5_of_fp64(oracle, engine_lib, cuda, mode):
     assert rel_err(T[inner], T64[inner]).max() <= 1e-5
 
 
-@pytest.mark.parametrize("warps", [2, 4, 8, 16])
-def test_launch_shapes_same_bits(oracle, engine_lib, cuda, arith, warps):
+@pytest.mark.parametrize("warps,gang", [(1, 0), (1, 1), (1, 2), (2, 0), (4, 3), (8, 0), (16, 16), (3, 5)])
+def test_launch_shapes_same_bits(oracle, engine_lib, cuda, arith, warps, gang):
     nx, nz = 150, 140
     m = smooth_model(nx, nz, 10.0, seed=31, noise=0.02)
     S = oracle.expand_boundary(m)
     e = make_engine(nx, nz, 10.0, 10.0, m, arith)
-    e.set_launch(warps=warps)
+    e.set_launch(warps=warps, gang_warps=gang)
     T = e.time_propagation(700.0, 100.0)
     assert np.array_equal(T, oracle.solve_f32(S, 10.0, 10.0, 700.0, 100.0))
 
@@ -138,7 +138,7 @@ def test_batched_many_shots_grid_smaller_than_batch(oracle, engine_lib, cuda, ar
     m = smooth_model(nx, nz, 10.0, seed=61)
     S = oracle.expand_boundary(m)
     e = make_engine(nx, nz, 10.0, 10.0, m, arith)
-    e.set_launch(warps=4, ctas_per_sm=1)
+    e.set_launch(warps=1, gang_warps=1)  # one warp per shot: every strip in turn
     shots = [(float(5.0 * (k % 398)), 0.0) for k in range(400)]
     rx, rz = surface_receivers(nx, 10.0, step=4)
     pk = e.batch_forward(shots, rx, rz)
