@@ -1,12 +1,17 @@
 """Benchmark of the batched eikonal engine on one GB300 (or N, one process per
 GPU under torchrun, shots sharded across ranks).
 
-Workload: 200 surface shots, each a full 4-sweep isotropic solve on the
-2001 x 501 (2007 x 507 padded) synthetic 6-layer model at 10 m, plus 800
-receiver picks per shot; all shots in one persistent launch. A step is one
-such batch. Prints ONE JSON line (rank 0).
+Default workload (forward + adjoint): 100 surface shots on the 1701 x 351
+(1707 x 357 padded) synthetic faulted layered model at 10 m, 400 receivers.
+A step is one tomography iteration of the batch: the taped forward of every
+shot with its 400 picks in one persistent launch, the pick residuals against
+observed picks and the FP64 misfit, the reverse (adjoint) sweeps of every
+shot in one persistent launch and the deterministic gather of the slowness
+gradient. ``--config 2`` / ``--config 3`` time the forward batch alone (200
+isotropic shots on 2001 x 501; 100 VTI shots on 1601 x 401). Prints ONE JSON
+line (rank 0).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 2|3|4|5]
 """
 import argparse
 import json
@@ -22,23 +27,28 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "eikonal shots/s (batched, FP32, <=1e-5 rel err)"
+METRIC = "eikonal+adjoint shots/s batched vs plain at \u22641e-5 rel err; HBM GB/s"
 UNIT = "shots/s"
-BYTES_PER_CELL_FWD = 48  # 4 sweeps x (S 4 B + T read 4 B + T write 4 B)
+# algorithmic bytes per padded window cell and shot
+BYTES_PER_CELL_FWD = 48       # 4 sweeps x (S 4 B + T read 4 B + T write 4 B)
+BYTES_PER_CELL_FWD_ANI = 120  # 2 x 48 + qP pass (6 x 2 B Cij + T 4 B + S 4 B + S 4 B)
+BYTES_PER_CELL_ADJ = 56       # 4 sweeps x (T 4 B + lam read 4 B + lam write 4 B) + S 4 B + g 4 B
+FA_CONFIGS = (4, 5)
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--config", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0: engine default)")
     ap.add_argument("--gang", type=int, default=0, help="warps per shot (0: automatic)")
     ap.add_argument("--arith", default="reference", choices=["reference", "ieee"])
+    ap.add_argument("--nplain", type=int, default=8, help="shots timed one at a time for the plain solver")
     return ap.parse_args()
 
 
@@ -55,18 +65,6 @@ def load_peaks():
         d = json.load(open(p))
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
-
-
-def load_traffic(name):
-    """DRAM bytes per padded cell per shot of the forward kernel from the
-    committed ncu summary (profiles/), or None."""
-    p = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("dram_bytes_per_cell_shot:"):
-            return float(line.split(":")[1])
-    return None
 
 
 class Clocks:
@@ -131,53 +129,126 @@ def workload(cfg):
     return synthetic.CONFIGS[cfg]()
 
 
-def cpu_baseline(w, seconds, rank):
-    """The oracle's FP32 port of the reference schedule on the host cores
-    (one shot per thread), on a bounded sample of the same shots."""
-    from oracle import oracle as O
-    S = O.expand_boundary(w.slowness)
-    nthreads = os.cpu_count() or 1
-    shots = w.shots
-    # calibrate on one shot, then size the sample to ~`seconds` of work
+def window(s, nxx):
+    c0 = int(s[2]) if len(s) > 2 else 0
+    nc = int(s[3]) if len(s) > 3 and s[3] > 0 else nxx - c0
+    return c0, nc
+
+
+def load_traffic(name):
+    """DRAM bytes per padded window cell and shot of one kernel, from its
+    committed ncu summary under profiles/ (None when absent)."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_cell_shot:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class CpuPort:
+    """The oracle's FP32 restatement of the reference schedule (and, for the
+    forward+adjoint workload, its taped reverse sweeps) on the host cores,
+    one shot per thread."""
+
+    def __init__(self, w, fa):
+        from oracle import oracle as O
+        self.O, self.w, self.fa = O, w, fa
+        self.S = O.expand_boundary(w.slowness)
+        self.nxx = self.S.shape[0]
+        self.ani = None
+        if w.cij is not None:
+            codes, mm = [], []
+            for c in w.cij:
+                cd, mn, mx = O.compress(O.expand_boundary(c))
+                codes.append(cd)
+                mm += [mn, mx]
+            self.ani = (codes, np.array(mm, np.float32))
+        self.nthreads = os.cpu_count() or 1
+
+    def tobs(self, sel):
+        # straight-ray times at 1800 m/s: the reverse sweeps cost the same for any residuals
+        return np.array([np.hypot(self.w.rx - s[0], self.w.rz - s[1]) / 1800.0 for s in sel], np.float32)
+
+    def run(self, sel, nthreads):
+        O, w = self.O, self.w
+        if self.fa:
+            _, _, _, used = O.batch_misfit_gradient(self.S, w.dx, w.dz, sel, w.rx, w.rz, self.tobs(sel),
+                                                    nthreads=nthreads)
+            return used
+        c0 = [window(s, self.nxx)[0] for s in sel]
+        nc = [window(s, self.nxx)[1] for s in sel]
+        _, used = O.batch_picks(self.S, w.dx, w.dz, [s[0] for s in sel], [s[1] for s in sel], c0, nc,
+                                w.rx, w.rz, ani=self.ani, nthreads=nthreads)
+        return used
+
+    def calibrate(self, seconds):
+        """Shots per sample so that one sample takes about `seconds` on all
+        threads (at least one shot per thread, at most the whole batch)."""
+        shots = self.w.shots
+        t0 = time.perf_counter()
+        self.run([shots[len(shots) // 2]], 1)
+        one = time.perf_counter() - t0
+        n = int(seconds * self.nthreads / max(one, 1e-3))
+        n = max(self.nthreads, (n // self.nthreads) * self.nthreads)
+        return min(n, len(shots)), one
+
+    def sample(self, n, k=0):
+        shots = self.w.shots
+        return [shots[(q * len(shots) // n + k) % len(shots)] for q in range(n)]
+
+    def describe(self, n, dt):
+        what = ("taped forward + picks + residuals + reverse sweeps + FP64 gradient sum" if self.fa
+                else "forward + picks")
+        return (f"{n} of the {len(self.w.shots)} shots of {self.w.name} per sample, one shot per thread, "
+                f"{what}, {dt:.1f} s timed; oracle FP32 restatement of the reference schedule "
+                f"(gcc -O2 -fopenmp)")
+
+
+def cpu_baseline(w, seconds, fa):
+    port = CpuPort(w, fa)
+    n, _ = port.calibrate(seconds)
+    sel = port.sample(n)
     t0 = time.perf_counter()
-    O.batch_picks(S, w.dx, w.dz, [shots[0][0]], [shots[0][1]], [0], [S.shape[0]], w.rx, w.rz, nthreads=1)
-    one = time.perf_counter() - t0
-    n = max(nthreads, int(seconds * nthreads / max(one, 1e-3)))
-    n = min(n, len(shots))
-    n = max(nthreads, (n // nthreads) * nthreads) if n >= nthreads else n
-    sel = [shots[k * len(shots) // n] for k in range(n)]
-    sx = [s[0] for s in sel]
-    sz = [s[1] for s in sel]
-    c0 = [s[2] if len(s) > 2 else 0 for s in sel]
-    nc = [s[3] if len(s) > 3 and s[3] > 0 else S.shape[0] - (s[2] if len(s) > 2 else 0) for s in sel]
-    t0 = time.perf_counter()
-    _, used = O.batch_picks(S, w.dx, w.dz, sx, sz, c0, nc, w.rx, w.rz, nthreads=nthreads)
+    used = port.run(sel, port.nthreads)
     dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": UNIT, "cores": used, "kind": "port",
-            "sample": f"{n} of the {len(shots)} shots of {w.name}, one shot per thread, "
-                      f"{dt:.1f} s, oracle FP32 restatement of the reference schedule (-O2)"}
+    return {"value": n / dt, "unit": UNIT, "cores": used, "kind": "port", "sample": port.describe(n, dt)}
 
 
 def run_reference(a):
+    """The reference has no CPU eikonal path and no adjoint; this arm times the
+    oracle's FP32 restatement of its schedule (plus the taped adjoint for the
+    forward+adjoint workload) on all host cores, each step a bounded sample of
+    the same workload."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     w = workload(a.config)
-    samples = []
-    res = None
+    fa = a.config in FA_CONFIGS
+    port = CpuPort(w, fa)
+    n, _ = port.calibrate(a.cpu_seconds / max(1, a.steps))
+    for k in range(a.warmup):
+        port.run(port.sample(n, k), port.nthreads)
+    done, tot, used = 0, 0.0, 1
     for k in range(a.steps):
-        res = cpu_baseline(w, a.cpu_seconds / max(1, a.steps) * 2, rank)
-        samples.append(res["value"])
-    v = statistics.median(samples)
+        sel = port.sample(n, a.warmup + k)
+        t0 = time.perf_counter()
+        used = port.run(sel, port.nthreads)
+        tot += time.perf_counter() - t0
+        done += len(sel)
+    v = done / tot
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": w.name, "nshots": len(w.shots), "nrec": len(w.rx),
-                       "grid": [w.nx, w.nz], "dh": w.dx},
-            "cpu_baseline": dict(res, value=v),
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / max(1, a.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": w.name, "nshots": len(w.shots), "nrec": len(w.rx), "grid": [w.nx, w.nz],
+                       "dh": w.dx, "step": "forward+adjoint" if fa else "forward"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+                             "sample": port.describe(n, tot)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference has no CPU eikonal path; this arm times the oracle's FP32 "
-                    "restatement of its schedule on the host cores"}
+            "note": "the reference has no CPU eikonal path and no adjoint; this arm times the oracle's "
+                    "FP32 restatement of its schedule on the host cores"}
     print(json.dumps(line), flush=True)
 
 
@@ -191,28 +262,50 @@ def run_ours(a):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from seisfat2d_gb300 import Engine
     w = workload(a.config)
+    fa = a.config in FA_CONFIGS
+    ani = w.cij is not None
     shots = w.shots[rank::world]
     nrec = len(w.rx)
     eng = Engine(w.nx, w.nz, w.dx, w.dz, device=local)
     eng.set_arithmetic(a.arith)
     if a.warps or a.gang:
         eng.set_launch(a.warps, a.gang)
-    eng.set_slowness(w.slowness)
-    tab = eng.shot_table(shots)
+    if ani:
+        eng.set_stiffness(w.cij)
     dev = torch.device("cuda", local)
-    picks = torch.empty((len(shots), nrec), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    tab = eng.shot_table(shots)
+    picks = torch.empty((len(shots), nrec), dtype=torch.float32, device=dev)
+    grad = torch.empty((eng.nxx, eng.nzz), dtype=torch.float32, device=dev) if fa else None
+    obs = None
+    if fa:
+        # observed picks: the engine's forward on the true model plus seeded Gaussian noise
+        eng.set_slowness(w.extra["true_slowness"])
+        eng.batch_forward(tab, w.rx, w.rz, out=picks, stream=stream)
+        torch.cuda.synchronize()
+        rng = np.random.default_rng(w.seed * 1000 + rank)
+        noise = rng.normal(0.0, w.extra["noise_sigma"], (len(shots), nrec)).astype(np.float32)
+        obs = picks.clone() + torch.from_numpy(noise).to(dev)
+    eng.set_slowness(w.slowness)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
 
-    def step():
-        eng.batch_forward(tab, w.rx, w.rz, out=picks, stream=stream)
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def step(marks):
+        marks[0].record(stream)
+        eng.batch_forward(tab, w.rx, w.rz, ani=ani, keep_tape=fa, out=picks, stream=stream)
+        marks[1].record(stream)
+        if fa:
+            eng.misfit_gradient(obs, out=grad, stream=stream, want_misfit=False)
+        marks[2].record(stream)
 
     for _ in range(a.warmup):
-        step()
+        step([ev(), ev(), ev()])
     eng.synchronize(stream)
     torch.cuda.synchronize()
     # --- timed: device-resident inputs, L2 flushed between steps
-    times = []
+    times, t_fwd, t_adj = [], [], []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -220,13 +313,12 @@ def run_ours(a):
     with Clocks(local) as clk:
         for _ in range(a.steps):
             flush.zero_()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
+            m = [ev(), ev(), ev()]
+            step(m)
+            m[2].synchronize()
+            times.append(m[0].elapsed_time(m[2]))
+            t_fwd.append(m[0].elapsed_time(m[1]))
+            t_adj.append(m[1].elapsed_time(m[2]))
     eng.synchronize(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -240,8 +332,10 @@ def run_ours(a):
     total_shots = len(w.shots) * a.steps
     value = total_shots / (tot_ms / 1e3)
 
-    # --- end to end through the C ABI with host buffers (model in, picks out)
+    # --- end to end through the C ABI with host buffers: model in, picks (+ misfit, gradient) out
     host_picks = np.zeros((len(shots), nrec), np.float32)
+    host_grad = np.zeros((eng.nxx, eng.nzz), np.float32)
+    host_obs = obs.cpu().numpy() if fa else None
     model = np.ascontiguousarray(w.slowness)
     e2e_times = []
     for k in range(a.warmup + a.steps):
@@ -249,7 +343,9 @@ def run_ours(a):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         eng.set_slowness(model)
-        eng.batch_forward(tab, w.rx, w.rz, out=host_picks, stream=stream)
+        eng.batch_forward(tab, w.rx, w.rz, ani=ani, keep_tape=fa, out=host_picks, stream=stream)
+        if fa:
+            eng.misfit_gradient(host_obs, out=host_grad, stream=stream)
         t1 = time.perf_counter()
         if k >= a.warmup:
             e2e_times.append(t1 - t0)
@@ -259,61 +355,107 @@ def run_ours(a):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_tot = float(t.item())
     e2e_value = total_shots / e2e_tot
-    h2d = model.nbytes + len(shots) * 16 + 2 * w.rx.nbytes
-    d2h = host_picks.nbytes
+    h2d = model.nbytes + len(shots) * 16 + w.rx.nbytes + w.rz.nbytes + (host_obs.nbytes if fa else 0)
+    d2h = host_picks.nbytes + (host_grad.nbytes + 8 if fa else 0)
 
-    # --- plain per-shot drop-in (one shot at a time, one CTA) for batched vs plain
+    # --- plain: one shot at a time, spread over the batch
+    nplain = max(1, min(a.nplain, len(shots)))
+    sel = [shots[q * len(shots) // nplain] for q in range(nplain)]
     Tdev = torch.empty((eng.nxx, eng.nzz), dtype=torch.float32, device=dev)
-    nplain = min(8, len(shots))
-    eng.time_propagation(shots[0][0], shots[0][1], out=Tdev, stream=stream)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
     pk = torch.empty(nrec, dtype=torch.float32, device=dev)
-    for s in shots[:nplain]:
-        eng.time_propagation(s[0], s[1], out=Tdev, stream=stream)
-        eng.compute_seismogram(Tdev, w.rx, w.rz, out=pk, stream=stream)
-    e1.record(stream)
-    e1.synchronize()
-    plain_ms = e0.elapsed_time(e1) / nplain
+
+    def plain_forward():
+        for s in sel:
+            eng.time_propagation(s[0], s[1], ani=ani, out=Tdev, stream=stream)
+            eng.compute_seismogram(Tdev, w.rx, w.rz, out=pk, stream=stream)
+
+    one_tabs = [eng.shot_table([s]) for s in sel]
+    one_obs = [obs[q * len(shots) // nplain:q * len(shots) // nplain + 1].contiguous() for q in range(nplain)] \
+        if fa else None
+    pk1 = torch.empty((1, nrec), dtype=torch.float32, device=dev)
+
+    def plain_fa():
+        for q in range(nplain):
+            eng.batch_forward(one_tabs[q], w.rx, w.rz, keep_tape=True, out=pk1, stream=stream)
+            eng.misfit_gradient(one_obs[q], out=grad, stream=stream, want_misfit=False)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / nplain
+
+    plain_ms = timed(plain_forward)
+    plain_fa_ms = timed(plain_fa) if fa else None
+    eng.synchronize(stream)
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
-    cells = sum((s[3] if len(s) > 3 and s[3] > 0 else eng.nxx) * eng.nzz for s in shots)
-    alg_bytes = BYTES_PER_CELL_FWD * cells
+    cells = sum(window(s, eng.nxx)[1] * eng.nzz for s in shots)
     peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (ms / 1e3) / 1e9
-    tpc = load_traffic("k_shots_cfg2_forward.txt")
+    fwd_bpc = BYTES_PER_CELL_FWD_ANI if ani else BYTES_PER_CELL_FWD
+    kname = "k_shots_tape" if fa else ("k_shots_ani" if ani else "k_shots")
+    stages = {"forward": {"kernel": f"sf::{kname} (one launch)", "ms": statistics.mean(t_fwd),
+                          "algorithmic_bytes": fwd_bpc * cells,
+                          "traffic_file": f"{kname}_cfg{a.config}.txt"}}
+    if fa:
+        stages["adjoint"] = {"kernel": "sf::k_adjoint (+ k_residual, k_gather)", "ms": statistics.mean(t_adj),
+                             "algorithmic_bytes": BYTES_PER_CELL_ADJ * cells,
+                             "traffic_file": f"k_adjoint_cfg{a.config}.txt"}
+    for st in stages.values():
+        st["achieved_gbs"] = st["algorithmic_bytes"] / (st["ms"] / 1e3) / 1e9
+        st["frac"] = st["achieved_gbs"] / peak
+        tpc = load_traffic(st["traffic_file"])
+        st["traffic"] = tpc * cells if tpc else None
+    dom = max(stages.values(), key=lambda st: st["ms"])
+    step_bytes = sum(st["algorithmic_bytes"] for st in stages.values())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded model and geometry)",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded model and geometry" + (
+            "; observed picks = engine forward on the true model + seeded N(0, 2 ms) noise)" if fa else ")"),
         "config": {"workload": w.name, "nshots": len(w.shots), "nrec": nrec, "grid": [w.nx, w.nz],
-                   "padded": [eng.nxx, eng.nzz], "dh": w.dx, "parallelism": f"shots sharded over {world} GPU(s)",
+                   "padded": [eng.nxx, eng.nzz], "dh": w.dx,
+                   "step": ("taped forward + picks, residuals + FP64 misfit, reverse sweeps, gradient gather"
+                            if fa else ("VTI forward (2 solves + qP pass) + picks" if ani else "forward + picks")),
+                   "parallelism": f"shots sharded over {world} GPU(s)",
                    "l2": "flushed between timed steps (512 MB write)",
                    "launch": {"warps_per_cta": eng.get_launch()[0], "warps_per_shot": eng.get_launch()[1] or "auto"},
                    "arithmetic": eng.get_arithmetic()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "path": "sf_set_slowness(host model) + sf_batch_forward(host picks)"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": (tpc * cells) if tpc else None,
-                     "algorithmic_bytes": alg_bytes, "kernel": "sf::k_shots<false>"},
-        "plain": {"ms_per_shot": plain_ms, "shots_per_s": 1e3 / plain_ms,
-                  "batched_vs_plain": value / world / (1e3 / plain_ms)},
-        "gpu_launches": a.steps,
+                "path": "sf_set_slowness(host model) + sf_batch_forward(host picks)" +
+                        (" + sf_batch_misfit_gradient(host picks in, host misfit and gradient out)" if fa else "")},
+        "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": dom["frac"], "peak_source": peak_kind, "traffic": dom["traffic"],
+                     "kernel": dom["kernel"], "algorithmic_bytes": dom["algorithmic_bytes"],
+                     "stages": stages,
+                     "step": {"algorithmic_bytes": step_bytes,
+                              "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
+                              "frac": step_bytes / (ms / 1e3) / 1e9 / peak}},
+        "plain": {"forward_ms_per_shot": plain_ms, "forward_shots_per_s": 1e3 / plain_ms,
+                  "path": "sf_time_propagation + sf_compute_seismogram, one shot per call",
+                  "batched_vs_plain_forward": value / world / (1e3 / plain_ms)},
+        "gpu_launches": a.steps * (4 if fa else 1),
         "clocks": clk.summary(),
         "wall_s_timed": wall,
     }
+    if fa:
+        line["plain"].update({
+            "forward_adjoint_ms_per_shot": plain_fa_ms, "forward_adjoint_shots_per_s": 1e3 / plain_fa_ms,
+            "forward_adjoint_path": "sf_batch_forward + sf_batch_misfit_gradient on a one-shot batch, per shot",
+            "batched_vs_plain_forward_adjoint": value / world / (1e3 / plain_fa_ms)})
     if not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, a.cpu_seconds, rank)
+        line["cpu_baseline"] = cpu_baseline(w, a.cpu_seconds, fa)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
-
 
 def main():
     a = parse()

@@ -932,3 +932,78 @@ void orc_adjoint_f64(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* 
 {
     ADJ_BODY(double)
 }
+
+/* ------------------------------------------------- batch misfit gradient */
+
+int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots,
+                           const float* sx, const float* sz, const int* c0, const int* ncols,
+                           const float* rx, const float* rz, int nrec, const float* tobs,
+                           float* picks, double* misfit, float* grad, int nthreads)
+{
+    int used = 1;
+    size_t* off = (size_t*)malloc(sizeof(size_t) * ((size_t)nshots + 1));
+    off[0] = 0;
+    for (int b = 0; b < nshots; b++) off[b + 1] = off[b] + (size_t)nzz * ncols[b];
+    float* gw = (float*)calloc(off[nshots] ? off[nshots] : 1, sizeof(float));
+    int bad = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(| : bad)
+#endif
+    for (int b = 0; b < nshots; b++) {
+        const int nc = ncols[b];
+        int sIdx, sIdz;
+        orc_source_index(sx[b], sz[b], dx, dz, nb, &sIdx, &sIdz);
+        const int sloc = sIdx - c0[b];
+        if (sIdz < 1 || sIdz > nzz - 2 || sloc < 1 || sloc > nc - 2 || c0[b] < 0 || c0[b] + nc > nxx) {
+            bad |= 1;
+            continue;
+        }
+        const size_t n = (size_t)nzz * nc;
+        const float* Sw = S + (size_t)c0[b] * nzz;
+        float init[9];
+        double iv[9], dist[9];
+        if (g_arith == 1) {
+            orc_init_block_f32(S, nzz, sx[b], sz[b], dx, dz, nb, sIdx, sIdz, init);
+        } else {
+            orc_init_block_f64(S, nzz, sx[b], sz[b], dx, dz, nb, sIdx, sIdz, iv);
+            for (int q = 0; q < 9; q++) init[q] = (float)iv[q];
+        }
+        init_dist_f64(nb, sx[b], sz[b], dx, dz, sIdx, sIdz, dist);
+        float df[9];
+        for (int q = 0; q < 9; q++) df[q] = (float)dist[q];
+        float* T = (float*)malloc(n * sizeof(float));
+        uint8_t* code = (uint8_t*)malloc(4 * n);
+        float* c1 = (float*)malloc(4 * n * sizeof(float));
+        float* c2 = (float*)malloc(4 * n * sizeof(float));
+        float* lam = (float*)malloc(n * sizeof(float));
+        float* pg = (float*)malloc(sizeof(float) * (nrec > 0 ? nrec : 1));
+        orc_solve_tape_f32(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, code, c1, c2);
+        float* pk = picks + (size_t)b * nrec;
+        orc_picks_f32(T, nzz, nc, c0[b], dx, dz, nb, rx, rz, nrec, pk);
+        for (int r = 0; r < nrec; r++) pg[r] = pk[r] - tobs[(size_t)b * nrec + r]; /* NaN: no pick */
+        orc_seed_lambda_f32(nzz, nc, c0[b], dx, dz, nb, rx, rz, nrec, pg, lam);
+        orc_adjoint_f32(nzz, nc, sIdz, sloc, code, c1, c2, df, lam, gw + off[b]);
+        free(T); free(code); free(c1); free(c2); free(lam); free(pg);
+    }
+#ifdef _OPENMP
+    used = nthreads;
+#endif
+    /* shot gradients summed in FP64 in caller order; misfit over (shot, receiver) */
+    double* acc = (double*)calloc((size_t)nzz * nxx, sizeof(double));
+    double J = 0.0;
+    for (int b = 0; b < nshots; b++) {
+        const size_t base = (size_t)c0[b] * nzz;
+        for (size_t q = 0; q < off[b + 1] - off[b]; q++) acc[base + q] += (double)gw[off[b] + q];
+        for (int r = 0; r < nrec; r++) {
+            double d = (double)picks[(size_t)b * nrec + r] - (double)tobs[(size_t)b * nrec + r];
+            if (d == d) J += 0.5 * d * d;
+        }
+    }
+    for (size_t q = 0; q < (size_t)nzz * nxx; q++) grad[q] = (float)acc[q];
+    if (misfit) *misfit = J;
+    free(acc);
+    free(gw);
+    free(off);
+    return bad ? -1 : used;
+}

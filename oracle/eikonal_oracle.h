@@ -135,6 +135,18 @@ void orc_seed_lambda_f32(int nzz, int ncols, int c0, float dx, float dz, int nb,
 void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
                          const float* rz, int nrec, const double* pg, double* lam);
 
+/* FP32 oracle of sf_batch_misfit_gradient for a batch of shot windows, one
+ * shot per thread: taped solve, picks, pick residual r = pick - tobs (NaN:
+ * no pick), seed, reverse sweeps into the shot's window gradient (FP32); the
+ * window gradients are then summed onto grad (nxx x nzz) in FP64 in caller
+ * order and rounded once. misfit = sum 0.5 r^2 in FP64 over (shot, receiver)
+ * in order. Returns the number of threads used, or -1 if a source lies
+ * outside its window. */
+int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots,
+                           const float* sx, const float* sz, const int* c0, const int* ncols,
+                           const float* rx, const float* rz, int nrec, const float* tobs,
+                           float* picks, double* misfit, float* grad, int nthreads);
+
 /* Arithmetic of the FP32 solvers: 0 = every operation rounded once and the
  * 3x3 initialisation in FP64 (default); 1 = the reference build's arithmetic:
  * FP32 initialisation and fused multiply-adds where nvcc forms them in

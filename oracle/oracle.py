@@ -71,6 +71,10 @@ def lib():
                                           f32p, f32p, C.c_int, f32p, f32p]
         L.orc_seed_lambda_f64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
                                           f32p, f32p, C.c_int, f64p, f64p]
+        L.orc_batch_gradient_f32.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float,
+                                             C.c_int, f32p, f32p, i32p, i32p, f32p, f32p, C.c_int,
+                                             f32p, f32p, C.POINTER(C.c_double), f32p, C.c_int]
+        L.orc_batch_gradient_f32.restype = C.c_int
         _lib = L
     return _lib
 
@@ -247,6 +251,29 @@ def batch_picks(S, dx, dz, sx, sz, c0, ncols, rx, rz, nb=3, ani=None, nthreads=0
                                np.ascontiguousarray(ncols, np.int32), 1 if ani is not None else 0,
                                arr, mm, _f32(rx), _f32(rz), len(rx), out, nthreads)
     return out, used
+
+
+def batch_misfit_gradient(S, dx, dz, shots, rx, rz, t_obs, nb=3, nthreads=0):
+    """FP32 oracle of sf_batch_misfit_gradient, one shot per thread.
+    shots: (sx, sz) or (sx, sz, c0, ncols). Returns (misfit, grad (nxx, nzz),
+    picks (nshots, nrec), threads_used)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ns = len(shots)
+    sx = _f32([s[0] for s in shots])
+    sz = _f32([s[1] for s in shots])
+    c0 = np.array([int(s[2]) if len(s) > 2 else 0 for s in shots], np.int32)
+    nc = np.array([int(s[3]) if len(s) > 3 and s[3] > 0 else nxx - int(c0[k]) for k, s in enumerate(shots)],
+                  np.int32)
+    picks = np.zeros((ns, len(rx)), np.float32)
+    grad = np.zeros((nxx, nzz), np.float32)
+    mis = C.c_double()
+    used = lib().orc_batch_gradient_f32(nzz, nxx, nb, S, dx, dz, ns, sx, sz, c0, nc, _f32(rx), _f32(rz),
+                                        len(rx), _f32(np.asarray(t_obs).reshape(ns, len(rx))), picks,
+                                        C.byref(mis), grad, nthreads)
+    if used < 0:
+        raise ValueError("a source lies outside its window")
+    return mis.value, grad, picks, used
 
 
 def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):

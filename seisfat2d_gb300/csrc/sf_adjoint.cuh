@@ -66,19 +66,31 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     const bool consumer = (lane == 0) && (a.h_in != nullptr);
     const int nsteps = ncols + 31;
     auto col_of = [&](int m) { return (SX < 0) ? m : ncols - 1 - m; };
+    // running source addresses of march q (q advances by one per call): the
+    // lambda column, the handoff pairs, and forward tape step ncols+30-q
+    const long long dL = (SX < 0) ? (long long)nzz : -(long long)nzz;
+    const float* pL = lamg + (size_t)(rb + lane) + (long long)col_of(0) * (long long)nzz;
+    const unsigned long long* pH = a.h_in;
+    const size_t fs0 = (size_t)(ncols + 30) * 32;
+    const float* pT1 = a.tc1 + fs0 + lane;
+    const float* pT2 = a.tc2 + fs0 + lane;
+    const uint8_t* pTc = a.tcode + fs0 + 4 * lane;
     auto prefetch = [&](int q, int lslot, int tslot) {
         if (q < ncols) {
-            const int jq = col_of(q);
-            if (lt_ok) cp_async4(&Lr[lslot * kLP + lane], lamg + (size_t)(rb + lane) + (size_t)jq * nzz);
-            if (consumer) cp_async16(&Lr[lslot * kLP + 32], a.h_in + 2 * (size_t)q);
+            if (lt_ok) cp_async4(&Lr[lslot * kLP + lane], pL);
+            if (consumer) cp_async16(&Lr[lslot * kLP + 32], pH);
         }
         if (q < nsteps) {
-            const size_t fs = (size_t)(ncols + 30 - q) * 32;
-            cp_async4(&TPr[tslot * kTPitch + lane], a.tc1 + fs + lane);
-            cp_async4(&TPr[tslot * kTPitch + 32 + lane], a.tc2 + fs + lane);
-            if (lane < 8) cp_async4(&TPr[tslot * kTPitch + 64 + lane], a.tcode + fs + 4 * lane);
+            cp_async4(&TPr[tslot * kTPitch + lane], pT1);
+            cp_async4(&TPr[tslot * kTPitch + 32 + lane], pT2);
+            if (lane < 8) cp_async4(&TPr[tslot * kTPitch + 64 + lane], pTc);
         }
         cp_commit();
+        pL += dL;
+        pH += 2;
+        pT1 -= 32;
+        pT2 -= 32;
+        pTc -= 32;
     };
 
     // let the previous strip get kLook+4 columns ahead before the first prefetches
@@ -86,6 +98,11 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     __syncwarp();
 #pragma unroll 1
     for (int q = 0; q < kLook; q++) prefetch(q, q, q % kTR);
+
+    // running destinations: the term v of forward tape step ncols+30-s, and
+    // the write-back of march column s-31 (row r)
+    float* pV = a.tc2 + fs0 + flane;
+    float* pW = lamg + (size_t)r + (long long)col_of(0) * (long long)nzz;
 
     int pf_slot = kLook, pf_tslot = kLook % kTR;
     int m_slot = (kRing - lane) % kRing;
@@ -142,7 +159,7 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
                 }
             }
             Lr[m_slot * kLP + tix] = lo;
-            a.tc2[(size_t)(ncols + 30 - s) * 32 + flane] = v;
+            *pV = v;
             if (lane == 31 && a.h_out != nullptr) {
                 st_u64(a.h_out + 2 * (size_t)m, pack_tag(npv, a.tag));
                 st_u64(a.h_out + 2 * (size_t)m + 1, pack_tag(npev, a.tag));
@@ -152,8 +169,11 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         my_pe = npe;
         my_pev = npev;
 
-        const int mw = s - 31;
-        if (mw >= 0 && vrow) lamg[(size_t)r + (size_t)col_of(mw) * nzz] = Lr[wb_slot * kLP + tix];
+        pV -= 32;
+        if (s >= 31) {
+            if (vrow) *pW = Lr[wb_slot * kLP + tix];
+            pW += dL;
+        }
 
         if (++pf_slot == kRing) pf_slot = 0;
         if (++pf_tslot == kTR) pf_tslot = 0;
@@ -200,7 +220,9 @@ __device__ __forceinline__ void cubic_weights(double t, double w[4])
     w[3] = __dadd_rn(__dmul_rn(-0.5, t2), __dmul_rn(0.5, t3));
 }
 
-__global__ void __launch_bounds__(kMaxWarps * 32) k_adjoint(AdjParams p)
+// (kMaxWarps * 32, 1): the block size alone as the bound caps the kernel at
+// 64 registers and spills the strip loop's state.
+__global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);

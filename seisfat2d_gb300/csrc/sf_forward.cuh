@@ -156,7 +156,9 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
 // sorted widest window first). The grid never exceeds what the device can
 // hold at once, so every gang's CTAs are resident together.
 template <bool TAPE, bool REF>
-__global__ void __launch_bounds__(kMaxWarps * 32) k_shots(FwdParams p)
+// (kMaxWarps * 32, 1): with the block size alone as the bound ptxas caps the
+// kernel at 64 registers and spills the strip loop's state to local memory.
+__global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);

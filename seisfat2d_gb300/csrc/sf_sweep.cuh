@@ -233,6 +233,12 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 #pragma unroll 1
     for (int q = 0; q < kLook; q++) prefetch(q, q);
 
+    // running destinations: write-back of march column s-31 (row r), tape entry s*32+lane
+    float* pW = Tg + (size_t)r + (long long)col_of(0) * (long long)nzz;
+    uint8_t* pcode = TAPE ? a.tcode + lane : nullptr;
+    float* pc1 = TAPE ? a.tc1 + lane : nullptr;
+    float* pc2 = TAPE ? a.tc2 + lane : nullptr;
+
     int pf_slot = kLook;                                  // slot of march s+kLook
     int m_slot = (kRing - lane) % kRing;                  // slot of march s-lane
     int wb_slot = (kRing - 31) % kRing;                   // slot of march s-31
@@ -303,19 +309,21 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         }
         if (act) Tring[m_slot * kTP + tix] = tnew;
         if (TAPE) {
-            const size_t t = (size_t)s * 32 + lane;
-            a.tcode[t] = act ? rec.code : (uint8_t)0;
-            a.tc1[t] = rec.c1;
-            a.tc2[t] = rec.c2;
+            *pcode = act ? rec.code : (uint8_t)0;
+            *pc1 = rec.c1;
+            *pc2 = rec.c2;
+            pcode += 32;
+            pc1 += 32;
+            pc2 += 32;
         }
 
         // feed the next strip: lane 31 just finished march s-31
         if (lane == 31 && a.h_out != nullptr && act) st_u64(a.h_out + m, pack_tag(tnew, a.tag));
 
         // write back the column every lane has finished
-        const int mw = s - 31;
-        if (mw >= 0 && vrow) {
-            Tg[(size_t)r + (size_t)col_of(mw) * nzz] = Tring[wb_slot * kTP + tix];
+        if (s >= 31) {
+            if (vrow) *pW = Tring[wb_slot * kTP + tix];
+            pW += dT;
         }
 
         // carry state

@@ -178,15 +178,18 @@ class Engine:
                     "sf_batch_adjoint")
         return out
 
-    def misfit_gradient(self, t_obs, out=None, stream=None):
+    def misfit_gradient(self, t_obs, out=None, stream=None, want_misfit=True):
+        """Misfit 1/2 sum (pick - t_obs)^2 of the taped batch and its slowness
+        gradient (padded (nxx, nzz)). With want_misfit False and a device
+        ``out`` the call only enqueues work on ``stream`` (misfit is None)."""
         if out is None:
             out = np.zeros((self.nxx, self.nzz), np.float32)
         po, omem, k1 = _ptr(t_obs)
         p, mem, k2 = _ptr(out)
         mis = C.c_double()
-        self._check(self.L.sf_batch_misfit_gradient(self._ctx, po, omem, C.byref(mis), p, mem,
-                                                    _stream_ptr(stream)), "sf_batch_misfit_gradient")
-        return mis.value, out
+        self._check(self.L.sf_batch_misfit_gradient(self._ctx, po, omem, C.byref(mis) if want_misfit else None,
+                                                    p, mem, _stream_ptr(stream)), "sf_batch_misfit_gradient")
+        return (mis.value if want_misfit else None), out
 
     def synchronize(self, stream=None):
         self._check(self.L.sf_synchronize(self._ctx, _stream_ptr(stream)), "sf_synchronize")
