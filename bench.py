@@ -192,16 +192,19 @@ class CpuPort:
         one = time.perf_counter() - t0
         n = int(seconds * self.nthreads / max(one, 1e-3))
         n = max(self.nthreads, (n // self.nthreads) * self.nthreads)
-        return min(n, len(shots)), one
+        return min(n, 50 * len(shots)), one
 
     def sample(self, n, k=0):
+        """n shots spread over the batch (the batch repeated when n exceeds it)."""
         shots = self.w.shots
-        return [shots[(q * len(shots) // n + k) % len(shots)] for q in range(n)]
+        if n <= len(shots):
+            return [shots[(q * len(shots) // n + k) % len(shots)] for q in range(n)]
+        return [shots[(q + k) % len(shots)] for q in range(n)]
 
     def describe(self, n, dt):
         what = ("taped forward + picks + residuals + reverse sweeps + FP64 gradient sum" if self.fa
                 else "forward + picks")
-        return (f"{n} of the {len(self.w.shots)} shots of {self.w.name} per sample, one shot per thread, "
+        return (f"{n} shots of {self.w.name} ({len(self.w.shots)} in the batch) per sample, one shot per thread, "
                 f"{what}, {dt:.1f} s timed; oracle FP32 restatement of the reference schedule "
                 f"(gcc -O2 -fopenmp)")
 
@@ -292,20 +295,27 @@ def run_ours(a):
     def ev():
         return torch.cuda.Event(enable_timing=True)
 
-    def step(marks):
-        marks[0].record(stream)
-        eng.batch_forward(tab, w.rx, w.rz, ani=ani, keep_tape=fa, out=picks, stream=stream)
-        marks[1].record(stream)
+    misfit = torch.empty(1, dtype=torch.float64, device=dev)
+    tuned = None
+    if fa:
+        # planned batch: shots and receivers stay on the device, the iteration
+        # replays from the engine's CUDA graph; the autotuner picks the launch shape
+        eng.plan_batch(tab, w.rx, w.rz, stream=stream)
+        if not (a.warps or a.gang):
+            tuned = eng.plan_autotune(picks, t_obs=obs, grad=grad, misfit=misfit, reps=2, stream=stream)
+
+    def step():
         if fa:
-            eng.misfit_gradient(obs, out=grad, stream=stream, want_misfit=False)
-        marks[2].record(stream)
+            eng.plan_graph_launch(picks, t_obs=obs, grad=grad, misfit=misfit, stream=stream)
+        else:
+            eng.batch_forward(tab, w.rx, w.rz, ani=ani, out=picks, stream=stream)
 
     for _ in range(a.warmup):
-        step([ev(), ev(), ev()])
+        step()
     eng.synchronize(stream)
     torch.cuda.synchronize()
     # --- timed: device-resident inputs, L2 flushed between steps
-    times, t_fwd, t_adj = [], [], []
+    times = []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -313,12 +323,12 @@ def run_ours(a):
     with Clocks(local) as clk:
         for _ in range(a.steps):
             flush.zero_()
-            m = [ev(), ev(), ev()]
-            step(m)
-            m[2].synchronize()
-            times.append(m[0].elapsed_time(m[2]))
-            t_fwd.append(m[0].elapsed_time(m[1]))
-            t_adj.append(m[1].elapsed_time(m[2]))
+            m = [ev(), ev()]
+            m[0].record(stream)
+            step()
+            m[1].record(stream)
+            m[1].synchronize()
+            times.append(m[0].elapsed_time(m[1]))
     eng.synchronize(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
@@ -331,6 +341,28 @@ def run_ours(a):
         dist.barrier()
     total_shots = len(w.shots) * a.steps
     value = total_shots / (tot_ms / 1e3)
+
+    # --- per-kernel device times (CUDA events the engine records around each
+    # launch on this stream), the same steps run eagerly, L2 flushed between steps
+    eng.set_kernel_timing(True)
+    kt = {}
+    eager_ms = []
+    for _ in range(a.steps):
+        flush.zero_()
+        m = [ev(), ev()]
+        m[0].record(stream)
+        if fa:
+            eng.plan_iteration(picks, t_obs=obs, grad=grad, misfit=misfit, stream=stream)
+        else:
+            step()
+        m[1].record(stream)
+        for k, v in eng.kernel_times().items():
+            kt.setdefault(k, []).append(v)
+        m[1].synchronize()
+        eager_ms.append(m[0].elapsed_time(m[1]))
+    eng.set_kernel_timing(False)
+    eng.synchronize(stream)
+    kt = {k: statistics.mean(v) for k, v in kt.items()}
 
     # --- end to end through the C ABI with host buffers: model in, picks (+ misfit, gradient) out
     host_picks = np.zeros((len(shots), nrec), np.float32)
@@ -401,17 +433,20 @@ def run_ours(a):
     peak, peak_kind = load_peaks()
     fwd_bpc = BYTES_PER_CELL_FWD_ANI if ani else BYTES_PER_CELL_FWD
     kname = "k_shots_tape" if fa else ("k_shots_ani" if ani else "k_shots")
-    stages = {"forward": {"kernel": f"sf::{kname} (one launch)", "ms": statistics.mean(t_fwd),
-                          "algorithmic_bytes": fwd_bpc * cells,
-                          "traffic_file": f"{kname}_cfg{a.config}.txt"}}
+    stages = {"forward": {"kernel": "sf::k_shots<tape>" if fa else "sf::k_shots", "ms": kt["forward"],
+                          "algorithmic_bytes": fwd_bpc * cells, "traffic_file": f"{kname}_cfg{a.config}.txt"}}
     if fa:
-        stages["adjoint"] = {"kernel": "sf::k_adjoint (+ k_residual, k_gather)", "ms": statistics.mean(t_adj),
-                             "algorithmic_bytes": BYTES_PER_CELL_ADJ * cells,
+        stages["adjoint"] = {"kernel": "sf::k_adjoint", "ms": kt["adjoint"],
+                             "algorithmic_bytes": (BYTES_PER_CELL_ADJ - 8) * cells,
                              "traffic_file": f"k_adjoint_cfg{a.config}.txt"}
+        stages["gather"] = {"kernel": "sf::k_gather", "ms": kt["gather"], "algorithmic_bytes": 8 * cells,
+                            "traffic_file": f"k_gather_cfg{a.config}.txt"}
+        stages["residual"] = {"kernel": "sf::k_residual", "ms": kt["residual"],
+                              "algorithmic_bytes": 3 * 4 * len(shots) * nrec, "traffic_file": None}
     for st in stages.values():
         st["achieved_gbs"] = st["algorithmic_bytes"] / (st["ms"] / 1e3) / 1e9
         st["frac"] = st["achieved_gbs"] / peak
-        tpc = load_traffic(st["traffic_file"])
+        tpc = load_traffic(st["traffic_file"]) if st["traffic_file"] else None
         st["traffic"] = tpc * cells if tpc else None
     dom = max(stages.values(), key=lambda st: st["ms"])
     step_bytes = sum(st["algorithmic_bytes"] for st in stages.values())
@@ -427,7 +462,12 @@ def run_ours(a):
                             if fa else ("VTI forward (2 solves + qP pass) + picks" if ani else "forward + picks")),
                    "parallelism": f"shots sharded over {world} GPU(s)",
                    "l2": "flushed between timed steps (512 MB write)",
-                   "launch": {"warps_per_cta": eng.get_launch()[0], "warps_per_shot": eng.get_launch()[1] or "auto"},
+                   "launch": {"warps_per_cta": eng.get_launch()[0], "warps_per_shot": eng.get_launch()[1] or "auto",
+                              "chosen_by": "sf_plan_autotune" if tuned else ("flags" if (a.warps or a.gang) else
+                                                                             "default")},
+                   "timed_path": ("sf_plan_graph_launch (CUDA graph of the planned iteration)" if fa
+                                  else "sf_batch_forward"),
+                   "eager_ms_per_step": statistics.mean(eager_ms),
                    "arithmetic": eng.get_arithmetic()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": "sf_set_slowness(host model) + sf_batch_forward(host picks)" +
@@ -435,7 +475,8 @@ def run_ours(a):
         "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": dom["frac"], "peak_source": peak_kind, "traffic": dom["traffic"],
                      "kernel": dom["kernel"], "algorithmic_bytes": dom["algorithmic_bytes"],
-                     "stages": stages,
+                     "stages": stages, "timing": "CUDA events recorded by the engine around each launch "
+                                                 "(sf_set_kernel_timing), mean over the eager steps",
                      "step": {"algorithmic_bytes": step_bytes,
                               "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
                               "frac": step_bytes / (ms / 1e3) / 1e9 / peak}},

@@ -158,6 +158,52 @@ int sf_time_propagation_noalloc(const float* S, int nx, int nz, float dx, float 
 int sf_set_launch(sf_ctx* ctx, int warps, int gang_warps);
 int sf_get_launch(const sf_ctx* ctx, int* warps, int* gang_warps);
 
+/* ---- planned batches, CUDA graphs, autotuner (no counterpart in the
+ * reference, which solves one shot per call: inversion.cpp:52-67 and
+ * migration.cu:116-171 loop over time_propagation) ----
+ *
+ * sf_plan_batch fixes a batch on the context: isotropic shots (windows as in
+ * sf_batch_forward) and receivers are uploaded once and every buffer a
+ * forward + adjoint iteration needs is reserved, so that sf_plan_iteration
+ * only enqueues device work on `stream` (no allocation, no host copy, no
+ * synchronisation); it zeroes the handoff buffers of its two persistent
+ * kernels first, so it may be captured into a CUDA graph by the caller and
+ * replayed any number of times.
+ * Synchronises `stream` once. Any other batch call on the context (or
+ * sf_time_propagation) ends the plan; sf_set_launch / sf_set_arithmetic make
+ * the next iteration reconfigure it (outside a capture).
+ *
+ * One iteration, device pointers only: the taped forward of every shot with
+ * its picks (picks, nshots x nrec, caller order); then, when t_obs is not
+ * null, the residuals picks - t_obs (NaN = no pick), the misfit
+ * 1/2 sum r^2 in FP64 (misfit: one device double, may be null), the reverse
+ * sweeps and the deterministic gather of dJ/dS into grad (padded nxx x nzz,
+ * overwritten). Errors of in-kernel waits surface at sf_synchronize. */
+int sf_plan_batch(sf_ctx* ctx, const sf_shot* shots, int nshots, const float* rx, const float* rz,
+                  int nrec, void* stream);
+int sf_plan_iteration(sf_ctx* ctx, const float* t_obs, float* picks, double* misfit, float* grad,
+                      void* stream);
+/* The same iteration from a CUDA graph the context owns: captured on first use
+ * (and again when the pointers or the plan's launch shape change), then
+ * replayed with cudaGraphLaunch on `stream`. */
+int sf_plan_graph_launch(sf_ctx* ctx, const float* t_obs, float* picks, double* misfit, float* grad,
+                         void* stream);
+/* Autotuner: times `reps` iterations of the plan for each candidate launch
+ * shape (1, 2, 4 warps per CTA x automatic, all, 1/2, 1/3, 1/4 of the strips
+ * per gang), keeps the fastest (as sf_set_launch would) and reports it.
+ * Every shape computes the same bits. Synchronises `stream`. */
+int sf_plan_autotune(sf_ctx* ctx, const float* t_obs, float* picks, double* misfit, float* grad, int reps,
+                     void* stream, int* best_warps, int* best_gang_warps, float* best_ms);
+
+/* Per-kernel device times: with timing on, CUDA events are recorded around
+ * each launch of the batched kernels on the call's stream (not inside graph
+ * captures). sf_kernel_times writes, for the latest launch of each kernel
+ * since the previous query, its time in ms (-1: not launched), waiting for
+ * it: ms[0] forward (k_shots), ms[1] pick residuals, ms[2] reverse sweeps
+ * (k_adjoint), ms[3] gradient gather. */
+int sf_set_kernel_timing(sf_ctx* ctx, int enable);
+int sf_kernel_times(sf_ctx* ctx, float* ms, int n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -996,7 +996,8 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
         const size_t base = (size_t)c0[b] * nzz;
         for (size_t q = 0; q < off[b + 1] - off[b]; q++) acc[base + q] += (double)gw[off[b] + q];
         for (int r = 0; r < nrec; r++) {
-            double d = (double)picks[(size_t)b * nrec + r] - (double)tobs[(size_t)b * nrec + r];
+            /* the residual is the FP32 pick gradient; its square is summed in FP64 */
+            double d = (double)(picks[(size_t)b * nrec + r] - tobs[(size_t)b * nrec + r]);
             if (d == d) J += 0.5 * d * d;
         }
     }

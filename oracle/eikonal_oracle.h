@@ -140,7 +140,7 @@ void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb,
  * no pick), seed, reverse sweeps into the shot's window gradient (FP32); the
  * window gradients are then summed onto grad (nxx x nzz) in FP64 in caller
  * order and rounded once. misfit = sum 0.5 r^2 in FP64 over (shot, receiver)
- * in order. Returns the number of threads used, or -1 if a source lies
+ * in order, r the FP32 residual. Returns the number of threads used, or -1 if a source lies
  * outside its window. */
 int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots,
                            const float* sx, const float* sz, const int* c0, const int* ncols,

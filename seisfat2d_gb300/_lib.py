@@ -59,6 +59,12 @@ SIGNATURES = {
     "sf_get_launch": (C.c_int, [VP, IP, IP]),
     "sf_time_propagation_noalloc": (C.c_int, [VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                                               C.c_float, VP, VP]),
+    "sf_plan_batch": (C.c_int, [VP, C.POINTER(sf_shot), C.c_int, VP, VP, C.c_int, VP]),
+    "sf_plan_iteration": (C.c_int, [VP, VP, VP, VP, VP, VP]),
+    "sf_plan_graph_launch": (C.c_int, [VP, VP, VP, VP, VP, VP]),
+    "sf_plan_autotune": (C.c_int, [VP, VP, VP, VP, VP, C.c_int, VP, IP, IP, FP]),
+    "sf_set_kernel_timing": (C.c_int, [VP, C.c_int]),
+    "sf_kernel_times": (C.c_int, [VP, FP, C.c_int]),
 }
 
 _lib = None

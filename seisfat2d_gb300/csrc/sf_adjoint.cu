@@ -66,9 +66,7 @@ static int prepare_gather(sf_ctx* c, cudaStream_t st)
     return SF_OK;
 }
 
-// Runs the reverse sweeps and the gather for pick gradients already on the
-// device (d_pg, nshots x nrec, caller order); grad is a device pointer.
-int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t st)
+int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
 {
     const int ns = (int)c->hshots.size();
     const int nstrips = (c->nzz + 31) / 32;
@@ -85,7 +83,7 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
     if (rc) return rc;
     rc = prepare_gather(c, st);
     if (rc) return rc;
-    AdjParams p;
+    AdjParams& p = A->p;
     std::memset(&p, 0, sizeof(p));
     p.nzz = c->nzz;
     p.nxx = c->nxx;
@@ -102,20 +100,16 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
     p.lam_per_gang = (long long)c->nzz * c->batch_maxcols;
     p.hand = c->d_hand2;
     p.bar = c->d_ctr2;
-    p.epoch = sf_next_epoch(c);
     p.tcode = c->d_tcode;
     p.tc1 = c->d_tc1;
     p.tc2 = c->d_tc2;
-    p.pick_grad = d_pg;
     p.rx = c->d_rx;
     p.rz = c->d_rz;
     p.nrec = c->batch_nrec;
     p.lam_init = c->d_lam_init;
     p.err = c->d_flags + 1;
-    CK(cudaMemsetAsync(c->d_ctr2, 0, nctr * sizeof(unsigned), st));
-    k_adjoint<<<NG * G, c->warps * 32, smem, st>>>(p);
-    CK(cudaGetLastError());
-    GatherParams g;
+    GatherParams& g = A->g;
+    std::memset(&g, 0, sizeof(g));
     g.nzz = c->nzz;
     g.nxx = c->nxx;
     g.nb = c->nb;
@@ -129,10 +123,56 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
     g.tcode = c->d_tcode;
     g.vrec = c->d_tc2;
     g.lam_init = c->d_lam_init;
-    g.grad = d_grad;
     const size_t ncell = (size_t)c->nzz * c->nxx;
-    k_gather<<<(unsigned)std::min<size_t>((ncell + 255) / 256, (size_t)c->sms * 16), 256, 0, st>>>(g);
+    A->kern = (const void*)k_adjoint;
+    A->gkern = (const void*)k_gather;
+    A->grid = dim3(NG * G);
+    A->block = dim3(c->warps * 32);
+    A->smem = smem;
+    A->nctr = nctr;
+    A->hand_bytes = (size_t)NG * 4 * nstrips * c->batch_maxcols * 2 * sizeof(unsigned long long);
+    A->ggrid = dim3((unsigned)std::min<size_t>((ncell + 255) / 256, (size_t)c->sms * 16));
+    A->gblock = dim3(256);
+    return SF_OK;
+}
+
+int sf_adj_enqueue(sf_ctx* c, AdjLaunch& A, const float* d_pg, float* d_grad, unsigned epoch, cudaStream_t st)
+{
+    A.p.pick_grad = d_pg;
+    A.p.epoch = epoch;
+    A.g.grad = d_grad;
+    CK(cudaMemsetAsync(A.p.bar, 0, A.nctr * sizeof(unsigned), st));
+    int rc = sf_kt_begin(c, SF_KT_ADJOINT, st);
+    if (rc) return rc;
+    void* args[] = {&A.p};
+    CK(cudaLaunchKernel(A.kern, A.grid, A.block, args, A.smem, st));
+    rc = sf_kt_end(c, SF_KT_ADJOINT, st);
+    if (!rc) rc = sf_kt_begin(c, SF_KT_GATHER, st);
+    if (rc) return rc;
+    void* gargs[] = {&A.g};
+    CK(cudaLaunchKernel(A.gkern, A.ggrid, A.gblock, gargs, 0, st));
+    return sf_kt_end(c, SF_KT_GATHER, st);
+}
+
+int sf_residual_enqueue(sf_ctx* c, const float* d_picks, const float* d_obs, float* d_pg, double* d_misfit,
+                        cudaStream_t st)
+{
+    const size_t npk = (size_t)c->batch_nshots * c->batch_nrec;
+    int rc = sf_kt_begin(c, SF_KT_RESIDUAL, st);
+    if (rc) return rc;
+    k_residual<<<1, 1024, 0, st>>>(d_picks, d_obs, npk, d_pg, d_misfit);
     CK(cudaGetLastError());
+    return sf_kt_end(c, SF_KT_RESIDUAL, st);
+}
+
+// Runs the reverse sweeps and the gather for pick gradients already on the
+// device (d_pg, nshots x nrec, caller order); grad is a device pointer.
+int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t st)
+{
+    AdjLaunch A;
+    int rc = sf_adj_configure(c, st, &A);
+    if (!rc) rc = sf_adj_enqueue(c, A, d_pg, d_grad, sf_next_epoch(c), st);
+    if (rc) return rc;
     c->tape_valid = false;  // the reverse sweeps overwrite the tape's c2 with their terms
     return SF_OK;
 }
@@ -195,8 +235,8 @@ extern "C" int sf_batch_misfit_gradient(sf_ctx* c, const float* t_obs, int obs_m
         CK(cudaMemcpyAsync(c->d_pg + npk, t_obs, npk * sizeof(float), cudaMemcpyHostToDevice, st));
         d_obs = c->d_pg + npk;
     }
-    k_residual<<<1, 1024, 0, st>>>(c->batch_picks, d_obs, npk, c->d_pg, c->d_misfit);
-    CK(cudaGetLastError());
+    rc = sf_residual_enqueue(c, c->batch_picks, d_obs, c->d_pg, c->d_misfit, st);
+    if (rc) return rc;
     float* dg;
     rc = grad_target(c, grad, grad_mem, &dg);
     if (rc) return rc;

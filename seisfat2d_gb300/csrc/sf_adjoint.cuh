@@ -19,6 +19,7 @@
 // consecutive entries (lane l of the reverse march is lane 31-l of the
 // forward one).
 #pragma once
+#include "sf_adjoint_params.cuh"
 #include "sf_forward.cuh"
 
 namespace sf {
@@ -185,29 +186,6 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     __syncwarp();
 }
 
-struct AdjParams {
-    int nzz, nxx, nb;
-    float dx, dz;
-    const ShotDev* shots;   // same table (and order) as the taped forward
-    int nshots;
-    int nstrips;
-    int G, NG, maxcols;     // gangs as in the forward
-    float* lam;             // per-gang window adjoint, lam + gang * lam_per_gang
-    long long lam_per_gang;
-    unsigned long long* hand;  // per gang [4][nstrips][2 * maxcols] tagged (pv, pev) pairs
-    unsigned* bar;          // per gang barrier counter
-    unsigned epoch;         // launch number (tags)
-    uint8_t* tcode;
-    float* tc1;
-    float* tc2;
-    const float* pick_grad; // nshots x nrec, caller order (NaN = no pick)
-    const float* rx;
-    const float* rz;
-    int nrec;
-    float* lam_init;        // nshots x 9, caller order: adjoint of the 3x3 initial values
-    int* err;
-};
-
 // Cubic weights of the pick rule (the rule is linear in the 16 nodes):
 // P -> P1 + 0.5 t (P2 - P0 + t (2P0 - 5P1 + 4P2 - P3 + t (3(P1 - P2) + P3 - P0)))
 // (every FP64 operation rounded once, left to right, as written)
@@ -312,19 +290,6 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
         gang_barrier(bar, (++nbar) * p.G, cs, p.err);
     }
 }
-
-struct GatherParams {
-    int nzz, nxx, nb, nstrips;
-    float dx, dz;
-    const ShotDev* shots;    // sorted table; shot_of_orig maps caller index -> table row
-    const int* shot_of_orig;
-    const int* colptr;       // CSR over padded columns: caller-order shot indices covering it
-    const int* colshots;
-    const uint8_t* tcode;
-    const float* vrec;       // v terms (tape c2 after the reverse sweeps)
-    const float* lam_init;   // nshots x 9 (caller order)
-    float* grad;             // nzz x nxx
-};
 
 // Tape index of node (i, j) (window coordinates) in forward sweep sw.
 __device__ __forceinline__ size_t tape_index(const ShotDev& sh, int sw, int i, int j, int nstrips, int nzz)

@@ -1,0 +1,43 @@
+// Launch parameters of the adjoint kernels (plain structs, no device code).
+#pragma once
+#include "sf_forward.cuh"
+
+namespace sf {
+
+struct AdjParams {
+    int nzz, nxx, nb;
+    float dx, dz;
+    const ShotDev* shots;   // same table (and order) as the taped forward
+    int nshots;
+    int nstrips;
+    int G, NG, maxcols;     // gangs as in the forward
+    float* lam;             // per-gang window adjoint, lam + gang * lam_per_gang
+    long long lam_per_gang;
+    unsigned long long* hand;  // per gang [4][nstrips][2 * maxcols] tagged (pv, pev) pairs
+    unsigned* bar;          // per gang barrier counter
+    unsigned epoch;         // launch number (tags)
+    uint8_t* tcode;
+    float* tc1;
+    float* tc2;
+    const float* pick_grad; // nshots x nrec, caller order (NaN = no pick)
+    const float* rx;
+    const float* rz;
+    int nrec;
+    float* lam_init;        // nshots x 9, caller order: adjoint of the 3x3 initial values
+    int* err;
+};
+
+struct GatherParams {
+    int nzz, nxx, nb, nstrips;
+    float dx, dz;
+    const ShotDev* shots;    // sorted table; shot_of_orig maps caller index -> table row
+    const int* shot_of_orig;
+    const int* colptr;       // CSR over padded columns: caller-order shot indices covering it
+    const int* colshots;
+    const uint8_t* tcode;
+    const float* vrec;       // v terms (tape c2 after the reverse sweeps)
+    const float* lam_init;   // nshots x 9 (caller order)
+    float* grad;             // nzz x nxx
+};
+
+}  // namespace sf

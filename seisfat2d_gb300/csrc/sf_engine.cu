@@ -187,6 +187,7 @@ extern "C" int sf_ctx_destroy(sf_ctx* c)
 {
     if (!c) return SF_OK;
     cudaSetDevice(c->dev);
+    sf_plan_release(c);
     sf_adjoint_release(c);
     void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
                     c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand, c->d_ctr};
@@ -212,6 +213,7 @@ extern "C" int sf_set_launch(sf_ctx* c, int warps, int gang_warps)
     if (gang_warps < 0 || gang_warps > 1024) return sf_fail(c, SF_ERR_ARG, "gang warps must be 0..1024");
     if (warps) c->warps = warps;
     c->gang_warps = gang_warps;
+    c->plan_dirty = true;  // a planned batch is reconfigured before its next iteration
     return SF_OK;
 }
 
@@ -220,6 +222,7 @@ extern "C" int sf_set_arithmetic(sf_ctx* c, int mode)
     if (!c) return SF_ERR_ARG;
     if (mode != SF_ARITH_REFERENCE && mode != SF_ARITH_IEEE) return sf_fail(c, SF_ERR_ARG, "unknown arithmetic");
     c->arith = mode;
+    c->plan_dirty = true;
     return SF_OK;
 }
 
@@ -443,6 +446,7 @@ void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4])
 // queue). Returns SF_ERR_RANGE for a source outside its window.
 int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape)
 {
+    c->plan_valid = false;  // the planned batch's tables are replaced
     c->hshots.resize(nshots);
     std::vector<int> order(nshots);
     std::vector<std::pair<int, std::array<int, 8>>> skip_cache;
@@ -500,8 +504,8 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
     return SF_OK;
 }
 
-int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
-                    cudaStream_t st)
+int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, int gang_warps, cudaStream_t st,
+                     FwdLaunch* L)
 {
     const int nshots = (int)c->hshots.size();
     const size_t nzz = c->nzz;
@@ -513,6 +517,8 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
     if (rc) return rc;
+    if ((long long)(nshots + NG - 1) / NG * (ani ? 2 : 1) > 1023)
+        return sf_fail(c, SF_ERR_ARG, "too many shots per gang for one launch; split the batch");
     c->last_G = G;
     c->last_NG = NG;
     rc = sf_dev_reserve(c, (void**)&c->d_shots, &c->cap_shots, nshots * sizeof(ShotDev));
@@ -532,8 +538,6 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     const size_t nctr = (size_t)NG;
     rc = sf_dev_reserve(c, (void**)&c->d_ctr, &c->cap_ctr, nctr * sizeof(unsigned));
     if (rc) return rc;
-    if ((long long)(nshots + NG - 1) / NG * (ani ? 2 : 1) > 1023)
-        return sf_fail(c, SF_ERR_ARG, "too many shots per gang for one launch; split the batch");
     if (tape) {
         size_t n = (size_t)c->batch_tape_entries;
         rc = sf_dev_reserve(c, (void**)&c->d_tcode, &c->cap_tcode, n);
@@ -541,7 +545,7 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
         if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc2, &c->cap_tc2, n * sizeof(float));
         if (rc) return rc;
     }
-    FwdParams p;
+    FwdParams& p = L->p;
     std::memset(&p, 0, sizeof(p));
     p.S = c->d_S;
     p.nzz = c->nzz;
@@ -558,7 +562,6 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     p.err = c->d_flags + 1;          // flags[1]: error flag
     p.hand = c->d_hand;
     p.bar = c->d_ctr;
-    p.epoch = sf_next_epoch(c);
     p.ani = ani;
     if (ani) {
         const size_t npad = (size_t)c->nxx * c->nzz;
@@ -575,24 +578,56 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     p.rx = c->d_rx;
     p.rz = c->d_rz;
     p.nrec = nrec;
-    p.picks = d_picks;
-    CK(cudaMemsetAsync(c->d_ctr, 0, nctr * sizeof(unsigned), st));
-    const dim3 g(NG * G), b(c->warps * 32);
-    if (ref) {
-        if (tape) k_shots<true, true><<<g, b, smem, st>>>(p);
-        else k_shots<false, true><<<g, b, smem, st>>>(p);
-    } else {
-        if (tape) k_shots<true, false><<<g, b, smem, st>>>(p);
-        else k_shots<false, false><<<g, b, smem, st>>>(p);
-    }
-    CK(cudaGetLastError());
+    L->kern = kern;
+    L->grid = dim3(NG * G);
+    L->block = dim3(c->warps * 32);
+    L->smem = smem;
+    L->nctr = nctr;
+    L->hand_bytes = (size_t)NG * 4 * nstrips * c->batch_maxcols * sizeof(unsigned long long);
+    return SF_OK;
+}
+
+int sf_kt_begin(sf_ctx* c, int k, cudaStream_t st)
+{
+    if (!c->timing) return SF_OK;
+    c->kt_rec[k] = true;
+    CK(cudaEventRecord(c->kt_ev[k][0], st));
+    return SF_OK;
+}
+
+int sf_kt_end(sf_ctx* c, int k, cudaStream_t st)
+{
+    if (!c->timing) return SF_OK;
+    CK(cudaEventRecord(c->kt_ev[k][1], st));
+    return SF_OK;
+}
+
+int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st)
+{
+    L.p.picks = d_picks;
+    L.p.epoch = epoch;
+    CK(cudaMemsetAsync(L.p.bar, 0, L.nctr * sizeof(unsigned), st));
+    int rc = sf_kt_begin(c, SF_KT_FORWARD, st);
+    if (rc) return rc;
+    void* args[] = {&L.p};
+    CK(cudaLaunchKernel(L.kern, L.grid, L.block, args, L.smem, st));
+    return sf_kt_end(c, SF_KT_FORWARD, st);
+}
+
+int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
+                    cudaStream_t st)
+{
+    FwdLaunch L;
+    int rc = sf_fwd_configure(c, ani, nrec, keep_tables, tape, gang_warps, st, &L);
+    if (!rc) rc = sf_fwd_enqueue(c, L, d_picks, sf_next_epoch(c), st);
+    if (rc) return rc;
     c->tables_valid = keep_tables;
     c->tape_valid = tape;
     c->batch_nrec = nrec;
     return SF_OK;
 }
 
-static int upload_receivers(sf_ctx* c, const float* rx, const float* rz, int nrec, cudaStream_t st)
+int sf_upload_receivers(sf_ctx* c, const float* rx, const float* rz, int nrec, cudaStream_t st)
 {
     if (nrec <= 0) return SF_OK;
     int rc = sf_dev_reserve(c, (void**)&c->d_rx, &c->cap_rx, nrec * sizeof(float));
@@ -642,7 +677,7 @@ extern "C" int sf_batch_forward(sf_ctx* c, int ani, const sf_shot* shots, int ns
     c->tables_valid = false;
     int rc = sf_prepare_shots(c, shots, nshots, tables, tape);
     if (rc) return rc;
-    rc = upload_receivers(c, rx, rz, nrec, st);
+    rc = sf_upload_receivers(c, rx, rz, nrec, st);
     if (rc) return rc;
     float* dp = nullptr;
     if (nrec > 0) {
@@ -716,7 +751,7 @@ extern "C" int sf_compute_seismogram(sf_ctx* c, const float* T_dev, const float*
     if (nrec == 0) return SF_OK;
     CK(cudaSetDevice(c->dev));
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = upload_receivers(c, rx, rz, nrec, st);
+    int rc = sf_upload_receivers(c, rx, rz, nrec, st);
     if (rc) return rc;
     float* dp = picks;
     if (picks_mem == SF_MEM_HOST) {

@@ -5,7 +5,35 @@
 #include <vector>
 
 #include "../../include/seisfat2d.h"
+#include "sf_adjoint_params.cuh"
 #include "sf_forward.cuh"
+
+// One configured launch of the batched forward: parameters fixed except the
+// handoff-tag epoch and the picks pointer, which every enqueue sets.
+struct FwdLaunch {
+    sf::FwdParams p{};
+    const void* kern = nullptr;  // the k_shots instantiation
+    dim3 grid, block;
+    size_t smem = 0;
+    size_t nctr = 0;             // gang barrier counters zeroed before the launch
+    size_t hand_bytes = 0;       // handoff pairs of the launch's gangs
+};
+
+// One configured adjoint (reverse sweeps + gather); the pick gradients, the
+// gradient target and the epoch are set by every enqueue.
+struct AdjLaunch {
+    sf::AdjParams p{};
+    sf::GatherParams g{};
+    const void* kern = nullptr;   // k_adjoint
+    const void* gkern = nullptr;  // k_gather
+    dim3 grid, block, ggrid, gblock;
+    size_t smem = 0;
+    size_t nctr = 0;
+    size_t hand_bytes = 0;
+};
+
+// Kernels timed by sf_kernel_times (events around each launch when enabled).
+enum { SF_KT_FORWARD = 0, SF_KT_RESIDUAL = 1, SF_KT_ADJOINT = 2, SF_KT_GATHER = 3, SF_KT_N = 4 };
 
 struct sf_ctx {
     int dev = 0;
@@ -63,6 +91,24 @@ struct sf_ctx {
     unsigned long long* d_hand2 = nullptr; size_t cap_hand2 = 0;
     unsigned* d_ctr2 = nullptr; size_t cap_ctr2 = 0;
     std::vector<int> h_colptr, h_colshots;
+
+    // per-kernel timing (sf_set_kernel_timing)
+    bool timing = false;
+    cudaEvent_t kt_ev[SF_KT_N][2] = {};
+    bool kt_rec[SF_KT_N] = {};
+
+    // planned batch (sf_plan_batch) and its CUDA graph
+    bool plan_valid = false;
+    bool plan_dirty = false;     // launch shape or arithmetic changed since configuring
+    unsigned plan_gen = 0;        // bumped whenever the plan's launches change
+    FwdLaunch plan_f;
+    AdjLaunch plan_a;
+    int plan_nrec = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    unsigned graph_gen = 0;
+    const void* graph_ptrs[4] = {};   // t_obs, picks, misfit, grad of the capture
 };
 
 int sf_fail(sf_ctx* c, int status, const std::string& msg);
@@ -80,6 +126,21 @@ void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4]);
 int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape);
 int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
                     cudaStream_t st);
+// The two halves of sf_launch_shots: configure (gang shape, buffers, shot
+// table upload; host work and allocation) and enqueue (counter reset and the
+// launch; stream work only, capturable).
+int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, int gang_warps, cudaStream_t st,
+                     FwdLaunch* L);
+int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st);
+int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A);
+int sf_adj_enqueue(sf_ctx* c, AdjLaunch& A, const float* d_pg, float* d_grad, unsigned epoch, cudaStream_t st);
+int sf_residual_enqueue(sf_ctx* c, const float* d_picks, const float* d_obs, float* d_pg, double* d_misfit,
+                        cudaStream_t st);
+int sf_upload_receivers(sf_ctx* c, const float* rx, const float* rz, int nrec, cudaStream_t st);
+// Event pair around one launch when kernel timing is on.
+int sf_kt_begin(sf_ctx* c, int k, cudaStream_t st);
+int sf_kt_end(sf_ctx* c, int k, cudaStream_t st);
+void sf_plan_release(sf_ctx* c);
 // Gang shape for nshots shots of nstrips strips: CTAs per gang and gangs, so
 // that every gang of the grid is resident at once.
 int sf_gang_shape(sf_ctx* c, const void* kernel, size_t smem, int nshots, int nstrips, int gang_warps, int* G,

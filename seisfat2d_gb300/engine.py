@@ -191,6 +191,64 @@ class Engine:
                                                     p, mem, _stream_ptr(stream)), "sf_batch_misfit_gradient")
         return (mis.value if want_misfit else None), out
 
+    # -------------------------------------------------------- planned batches
+    def plan_batch(self, shots, rx, rz, stream=None):
+        """Fix an isotropic batch (shots as for batch_forward) for
+        plan_iteration / plan_graph_launch / plan_autotune."""
+        tab = shots if isinstance(shots, C.Array) else self.shot_table(shots)
+        rx = np.ascontiguousarray(rx, np.float32)
+        rz = np.ascontiguousarray(rz, np.float32)
+        self._check(self.L.sf_plan_batch(self._ctx, tab, len(tab), C.c_void_p(rx.ctypes.data),
+                                         C.c_void_p(rz.ctypes.data), len(rx), _stream_ptr(stream)),
+                    "sf_plan_batch")
+        self._plan = (len(tab), len(rx))
+
+    @staticmethod
+    def _dev_ptr(t, what):
+        if t is None:
+            return None
+        if not _is_dev(t) or not t.is_contiguous():
+            raise ValueError(f"{what} must be a contiguous CUDA tensor")
+        return C.c_void_p(t.data_ptr())
+
+    def _plan_args(self, t_obs, picks, misfit, grad):
+        return (self._dev_ptr(t_obs, "t_obs"), self._dev_ptr(picks, "picks"), self._dev_ptr(misfit, "misfit"),
+                self._dev_ptr(grad, "grad"))
+
+    def plan_iteration(self, picks, t_obs=None, grad=None, misfit=None, stream=None):
+        """Enqueue one iteration of the planned batch (device tensors only):
+        picks (nshots, nrec) f32; with t_obs, grad (nxx, nzz) f32 and
+        optionally misfit (1,) f64."""
+        a = self._plan_args(t_obs, picks, misfit, grad)
+        self._check(self.L.sf_plan_iteration(self._ctx, *a, _stream_ptr(stream)), "sf_plan_iteration")
+
+    def plan_graph_launch(self, picks, t_obs=None, grad=None, misfit=None, stream=None):
+        """The same iteration replayed from the context's CUDA graph."""
+        a = self._plan_args(t_obs, picks, misfit, grad)
+        self._check(self.L.sf_plan_graph_launch(self._ctx, *a, _stream_ptr(stream)), "sf_plan_graph_launch")
+
+    def plan_autotune(self, picks, t_obs=None, grad=None, misfit=None, reps=3, stream=None):
+        """Pick the fastest launch shape for the planned batch; returns
+        (warps_per_cta, gang_warps, ms_per_iteration)."""
+        a = self._plan_args(t_obs, picks, misfit, grad)
+        w, g, ms = C.c_int(), C.c_int(), C.c_float()
+        self._check(self.L.sf_plan_autotune(self._ctx, *a, int(reps), _stream_ptr(stream), C.byref(w), C.byref(g),
+                                            C.byref(ms)), "sf_plan_autotune")
+        return w.value, g.value, ms.value
+
+    # ------------------------------------------------------------ timing
+    KERNELS = ("forward", "residual", "adjoint", "gather")
+
+    def set_kernel_timing(self, enable=True):
+        self._check(self.L.sf_set_kernel_timing(self._ctx, 1 if enable else 0), "sf_set_kernel_timing")
+
+    def kernel_times(self):
+        """{kernel: ms} of the latest launch of each batched kernel since the
+        previous query (kernels not launched are left out)."""
+        ms = (C.c_float * 4)()
+        self._check(self.L.sf_kernel_times(self._ctx, ms, 4), "sf_kernel_times")
+        return {k: float(v) for k, v in zip(self.KERNELS, ms) if v >= 0.0}
+
     def synchronize(self, stream=None):
         self._check(self.L.sf_synchronize(self._ctx, _stream_ptr(stream)), "sf_synchronize")
 

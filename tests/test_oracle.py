@@ -242,3 +242,25 @@ def test_fp64_adjoint_matches_finite_differences(oracle):
         if abs(vals[0] - vals[1]) <= 1e-3 * scale and abs(fd - g[j, i]) <= 1e-3 * scale:
             ok += 1
     assert ok >= 28, ok
+
+
+def test_threaded_batch_gradient_matches_per_shot_path(oracle):
+    """orc_batch_gradient_f32 (one shot per thread, FP64 ordered sum) equals
+    the per-shot tape/seed/adjoint path and its misfit the FP64 sum of the
+    FP32 residuals."""
+    rng = np.random.default_rng(0)
+    S = oracle.expand_boundary((1.0 / rng.uniform(1500, 3000, (60, 40))).astype(np.float32))
+    shots = [(100.0, 0.0), (300.0, 50.0, 10, 40), (500.0, 20.0), (250.0, 0.0, 0, 35)]
+    rx = np.linspace(0, 590, 25).astype(np.float32)
+    rz = np.full(25, 5.0, np.float32)
+    tobs = rng.normal(0.2, 0.02, (len(shots), 25)).astype(np.float32)
+    tobs[1, 3] = np.nan
+    J, g, pk, used = oracle.batch_misfit_gradient(S, 10.0, 10.0, shots, rx, rz, tobs)
+    _, pk2 = oracle.batch_gradient(S, 10.0, 10.0, shots, rx, rz, np.zeros_like(tobs))
+    pg = (pk2 - tobs).astype(np.float32)
+    g2, _ = oracle.batch_gradient(S, 10.0, 10.0, shots, rx, rz, pg)
+    assert used >= 1
+    assert np.array_equal(pk, pk2, equal_nan=True)
+    assert np.array_equal(g, g2)
+    r = pg.astype(np.float64)
+    assert J == pytest.approx(0.5 * np.nansum(r * r), rel=1e-13)
