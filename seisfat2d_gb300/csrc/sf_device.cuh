@@ -43,11 +43,16 @@ __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 // Every step scales exactly with a by powers of two while all values stay
 // normal, so checking the 2^23 dividends of [1, 2) against IEEE division
 // (done per divisor when a context is created) covers every dividend of
-// magnitude in [2^-100, 2^100]; others, and unverified divisors, divide.
-__device__ __forceinline__ float fdiv_k(float a, float b, float rb, bool verified)
+// magnitude in [2^-100, 2^100]. EXACT (or an unverified divisor) divides.
+// Otherwise a dividend outside that range (or NaN) sets `bad`, and the
+// caller recomputes the node with EXACT: the check stays a compare, and the
+// rare exact path is one warp-uniform branch per step instead of a branch
+// per division.
+template <bool EXACT>
+__device__ __forceinline__ float fdiv_k(float a, float b, float rb, bool verified, bool& bad)
 {
-    const unsigned e = (__float_as_uint(a) >> 23) & 0xffu;
-    if (!verified || e - 27u > 200u) return __fdiv_rn(a, b);
+    if (EXACT) return __fdiv_rn(a, b);
+    bad |= !verified || (__float_as_uint(a) & 0x7f800000u) - 0x0d800000u > 0x64000000u;  // exponent not in [27, 227]
     const float q = __fmul_rn(a, rb);
     const float r = __fmaf_rn(-q, b, a);
     return __fmaf_rn(r, rb, q);
@@ -68,11 +73,11 @@ struct Rec {
 // columns max(j-1,1) and j); s2a/s2b: cells of the horizontal edge (rows
 // max(i-1,1) and i, column j1); sref = S[i1][j1]. dr1/dc2 locate i1/j1 in the
 // 2x2 block around the node, dc1a/dr2a locate the clamped first cells.
-template <bool TAPE, bool REF>
+template <bool TAPE, bool REF, bool EXACT = false>
 __device__ __forceinline__ float node_update(float told, float tv, float te, float tev, float s1a,
                                              float s1b, float s2a, float s2b, float sref,
                                              const Consts& k, int dr1, int dc1a, int dc2, int dr2a,
-                                             Rec& rec)
+                                             Rec& rec, bool& bad)
 {
     float m1 = fminf(s1a, s1b);
     float m2 = fminf(s2a, s2b);
@@ -97,15 +102,17 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
             rr = fsqrt(fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd)));
             num = fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr);
         }
-        t1 = fdiv_k(num, k.D, k.rD, k.mflags & 8);
+        t1 = fdiv_k<EXACT>(num, k.D, k.rD, k.mflags & 8, bad);
         br = 3;
     } else {
         // the two edge candidates of modeling.cu:342-353 share one code path:
         // t2 (from te, step dz) is tried first, t3 (from tv, step dx) otherwise
-        const bool c2 = (dte <= fdiv_k(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4)) && (dte > 0.0f);
+        const bool c2 = (dte <= fdiv_k<EXACT>(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4, bad)) &&
+                         (dte > 0.0f);
         bool c3 = false;
         if (!c2)
-            c3 = (dtv <= fdiv_k(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4)) && (dtv > 0.0f);
+            c3 = (dtv <= fdiv_k<EXACT>(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4, bad)) &&
+                     (dtv > 0.0f);
         if (c2 || c3) {
             const float dn = c2 ? dte : dtv;    // te - tev or tv - tev
             const float hq = c2 ? k.dz : k.dx;  // step the difference is divided by
@@ -113,7 +120,7 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
             const bool vq = c2 ? (k.mflags & 2) : (k.mflags & 1);
             const float hx = c2 ? k.dx : k.dz;  // step that multiplies the root
             const float bs = c2 ? te : tv;
-            q = fdiv_k(dn, hq, rq, vq);
+            q = fdiv_k<EXACT>(dn, hq, rq, vq, bad);
             float t;
             if (REF) {
                 qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
@@ -148,10 +155,10 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
                 rec.code = (uint8_t)(br | (dr1 << 3) | (dc2 << 4));
                 if (br == 3) {
                     if (rr > 0.0f) {
-                        rec.c1 = fdiv(fadd(k.kA, fdiv(fmul(k.k2K, dd), rr)), k.D);
+                        rec.c1 = fdiv_k<EXACT>(fadd(k.kA, fdiv(fmul(k.k2K, dd), rr)), k.D, k.rD, k.mflags & 8, bad);
                         rec.c2 = fdiv(fmul(4.0f, sref), rr);
                     } else {
-                        rec.c1 = fdiv(k.kA, k.D);
+                        rec.c1 = fdiv_k<EXACT>(k.kA, k.D, k.rD, k.mflags & 8, bad);
                     }
                 } else {
                     float hx = (br == 4) ? k.dx : k.dz;

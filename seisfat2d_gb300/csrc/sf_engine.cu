@@ -108,7 +108,9 @@ __global__ void k_verify_div(const float* divs, int n, float* rbs, int* bad)
         const float b = divs[w], rb = __frcp_rn(b);
         if ((t & 0x7fffffu) == 0) rbs[w] = rb;
         const float a = __uint_as_float(0x3f800000u | (t & 0x7fffffu));
-        if (__float_as_uint(fdiv_k(a, b, rb, true)) != __float_as_uint(__fdiv_rn(a, b))) atomicOr(bad, 1 << w);
+        bool out_of_range = false;
+        if (__float_as_uint(fdiv_k<false>(a, b, rb, true, out_of_range)) != __float_as_uint(__fdiv_rn(a, b)))
+            atomicOr(bad, 1 << w);
     }
 }
 

@@ -28,12 +28,16 @@
 // same bits as the reference's anti-diagonal launches, so this schedule is a
 // bit-exact replacement of eikonal_solver (modeling.cu:123-159).
 #pragma once
+#include <type_traits>
+
 #include "sf_device.cuh"
 
 namespace sf {
 
-constexpr int kRing = 48;   // column slots per warp ring (>= 32 + kLook + 1)
-constexpr int kLook = 12;   // prefetch distance in march columns
+constexpr int kU = 4;       // march steps per block of the strip loop
+constexpr int kLook = 8;    // prefetch distance in march columns (a multiple of kU)
+constexpr int kRing = 48;   // column slots per warp ring (a multiple of kU, >= 32 + kLook + kU)
+constexpr int kAhead = kLook + 2 * kU;  // columns a consumer lets its producer get ahead after a stall
 constexpr int kSP = 36;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff pair at 34..35
 constexpr int kTP = 32;     // T slot pitch
 constexpr int kMaxWarps = 16;
@@ -224,9 +228,9 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         pT += dT;
     };
 
-    // let the previous strip get kLook+4 columns ahead before the first
+    // let the previous strip get kAhead columns ahead before the first
     // prefetches of its values
-    if (consumer) wait_pair(a.h_in + min(kLook + 4, ncols - 1), a.tag, sh, a.err);
+    if (consumer) wait_pair(a.h_in + min(kAhead, ncols - 1), a.tag, sh, a.err);
     __syncwarp();
 
     // prologue: march columns 0 .. kLook-1
@@ -239,61 +243,88 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     float* pc1 = TAPE ? a.tc1 + lane : nullptr;
     float* pc2 = TAPE ? a.tc2 + lane : nullptr;
 
-    int pf_slot = kLook;                                  // slot of march s+kLook
-    int m_slot = (kRing - lane) % kRing;                  // slot of march s-lane
-    int wb_slot = (kRing - 31) % kRing;                   // slot of march s-31
     float tn = 0.0f, tvp = 0.0f;                          // own last result, last upwind value
     float cU = 0.0f, cI = 0.0f;                           // carried S of rows r-1, r
     const int nsteps = ncols + 31;
+    int b0 = 0;                                           // ring slot of march s0
 
+    // Blocks of kU steps: one wait for the staged columns per block, then the
+    // block's ring reads, its kU node updates, and its stores. Within a block
+    // the node updates are the only serial chain; the loads before and the
+    // stores after it are independent of it.
 #pragma unroll 1
-    for (int s = 0; s < nsteps; s++) {
-        prefetch(s + kLook, pf_slot);
+    for (int s0 = 0; s0 < nsteps; s0 += kU) {
+        {
+            int pf0 = b0 + kLook;
+            if (pf0 >= kRing) pf0 -= kRing;
+#pragma unroll
+            for (int u = 0; u < kU; u++) prefetch(s0 + kLook + u, pf0 + u);
+        }
+        // march columns <= s0+kU are staged (SX < 0 reads one column ahead)
         cp_wait<kLook - 1>();
         __syncwarp();
 
-        const int m = s - lane;
-        const bool act = vrow && (m >= 0) && (m < ncols);
-        const int j = col_of(m);
-        // S of the new column: march m (SX>0) or m+1 (SX<0)
-        int n_slot = (SX > 0) ? m_slot : (m_slot + 1 == kRing ? 0 : m_slot + 1);
-        float nU = Sring[n_slot * kSP + tix];
-        float nI = Sring[n_slot * kSP + six];
-
-        // upwind value from the lane above (or the previous strip)
-        float tv = __shfl_up_sync(0xffffffffu, tn, 1);
-        if (consumer && s < ncols) {
-            const unsigned long long e = *reinterpret_cast<const unsigned long long*>(&Sring[m_slot * kSP + 34]);
-            if (tag_of(e) == a.tag) {
-                tv = val_of(e);
-            } else {
-                // the previous strip had not written this column when it was prefetched:
-                // wait for it, then fall kLook+4 columns behind so later prefetches hit
-                tv = wait_pair(a.h_in + s, a.tag, sh, a.err);
-                wait_pair(a.h_in + min(s + kLook + 4, ncols - 1), a.tag, sh, a.err);
+        int ml = b0 - lane;                               // slot of march s0 - lane
+        if (ml < 0) ml += kRing;
+        int msl[kU];
+        float nU[kU], nI[kU], told[kU];
+        unsigned long long pr[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            int ms = ml + u;
+            if (ms >= kRing) ms -= kRing;
+            msl[u] = ms;
+            // S of the new column: march m (SX>0) or m+1 (SX<0)
+            const int ns = (SX > 0) ? ms : (ms + 1 == kRing ? 0 : ms + 1);
+            nU[u] = Sring[ns * kSP + tix];
+            nI[u] = Sring[ns * kSP + six];
+            told[u] = SW0 ? kBig : Tring[ms * kTP + tix];
+            pr[u] = consumer ? *reinterpret_cast<const unsigned long long*>(&Sring[ms * kSP + 34]) : 0ull;
+        }
+        if (consumer) {
+            // a pair the previous strip had not written when it was prefetched:
+            // wait for it, then fall kAhead columns behind so later prefetches hit
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const int s = s0 + u;
+                if (s < ncols && tag_of(pr[u]) != a.tag) {
+                    pr[u] = pack_tag(wait_pair(a.h_in + s, a.tag, sh, a.err), a.tag);
+                    wait_pair(a.h_in + min(s + kAhead, ncols - 1), a.tag, sh, a.err);
+                }
             }
         }
-        const float te = tn, tev = tvp;
 
-        float told;
-        if (SW0) {
-            told = kBig;
-            const int da = r - a.sIdz + 1, db = j - a.sIdx + 1;
-            if (da >= 0 && da < 3 && db >= 0 && db < 3) told = a.init[da + 3 * db];
-        } else {
-            told = Tring[m_slot * kTP + tix];
-        }
+        float tnw[kU];
+        bool actv[kU];
+        Rec rec[kU];
+        // the block's kU node updates; EXACT divides with IEEE division
+        auto updates = [&](auto exact_tag) -> bool {
+        constexpr bool EXACT = decltype(exact_tag)::value;
+        bool bad = false;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int s = s0 + u;
+            const int m = s - lane;
+            const bool act = vrow && (m >= 0) && (m < ncols);
+            const int j = col_of(m);
+            // upwind value from the lane above (or the previous strip)
+            float tv = __shfl_up_sync(0xffffffffu, tn, 1);
+            if (consumer && s < ncols) tv = val_of(pr[u]);
+            const float te = tn, tev = tvp;
 
-        float U_j, I_j, U_jm, I_jm;
-        if (SX > 0) { U_j = nU; I_j = nI; U_jm = cU; I_jm = cI; }
-        else        { U_j = cU; I_j = cI; U_jm = nU; I_jm = nI; }
+            float to = told[u];
+            if (SW0) {
+                const int da = r - a.sIdz + 1, db = j - a.sIdx + 1;
+                if (da >= 0 && da < 3 && db >= 0 && db < 3) to = a.init[da + 3 * db];
+            }
+            float U_j, I_j, U_jm, I_jm;
+            if (SX > 0) { U_j = nU[u]; I_j = nI[u]; U_jm = cU; I_jm = cI; }
+            else        { U_j = cU; I_j = cI; U_jm = nU[u]; I_jm = nI[u]; }
 
-        float tnew = told;
-        Rec rec;
-        rec.code = 0; rec.c1 = 0.0f; rec.c2 = 0.0f;
-        const bool inner = act && irow && (j >= 1) && (j <= ncols - 2) &&
-                           !(r == a.skip_i && j == a.skip_j);
-        if (inner) {
+            float tnew = to;
+            rec[u].code = 0; rec[u].c1 = 0.0f; rec[u].c2 = 0.0f;
+            const bool inner = act && irow && (j >= 1) && (j <= ncols - 2) &&
+                               !(r == a.skip_i && j == a.skip_j);
             // rows: i1 (SZ>0: r-1, else r); columns: j-1 (clamped to 1), j
             const float Si1_j = (SZ > 0) ? U_j : I_j;
             const float Si1_jm = (SZ > 0) ? U_jm : I_jm;
@@ -304,36 +335,66 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             const float s2b = (SX > 0) ? I_jm : I_j;       // S[i][j1]
             const float sref = (SX > 0) ? Si1_jm : Si1_j;  // S[i1][j1]
             const int dc1a = (j - 1 >= 1) ? 0 : 1;
-            tnew = node_update<TAPE, REF>(told, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc, dr1,
-                                     dc1a, dc2, dr2a, rec);
+            bool bad_u = false;
+            if (inner)
+                tnew = node_update<TAPE, REF, EXACT>(to, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc, dr1,
+                                                     dc1a, dc2, dr2a, rec[u], bad_u);
+            bad |= bad_u;
+            tnw[u] = tnew;
+            actv[u] = act;
+            // carry state
+            if (act) tn = tnew;
+            tvp = tv;
+            cU = nU[u];
+            cI = nI[u];
         }
-        if (act) Tring[m_slot * kTP + tix] = tnew;
-        if (TAPE) {
-            *pcode = act ? rec.code : (uint8_t)0;
-            *pc1 = rec.c1;
-            *pc2 = rec.c2;
-            pcode += 32;
-            pc1 += 32;
-            pc2 += 32;
+        return bad;
+        };
+        {
+            const float tn0 = tn, tvp0 = tvp, cU0 = cU, cI0 = cI;
+            // a quotient outside the range the fast division was verified on
+            // (one vote per block): the block again with IEEE division
+            if (__any_sync(0xffffffffu, updates(std::false_type{}))) {
+                tn = tn0;
+                tvp = tvp0;
+                cU = cU0;
+                cI = cI0;
+                updates(std::true_type{});
+            }
         }
 
-        // feed the next strip: lane 31 just finished march s-31
-        if (lane == 31 && a.h_out != nullptr && act) st_u64(a.h_out + m, pack_tag(tnew, a.tag));
-
-        // write back the column every lane has finished
-        if (s >= 31) {
-            if (vrow) *pW = Tring[wb_slot * kTP + tix];
-            pW += dT;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int s = s0 + u;
+            if (actv[u]) Tring[msl[u] * kTP + tix] = tnw[u];
+            if (TAPE) {
+                if (s < nsteps) {
+                    *pcode = actv[u] ? rec[u].code : (uint8_t)0;
+                    *pc1 = rec[u].c1;
+                    *pc2 = rec[u].c2;
+                }
+                pcode += 32;
+                pc1 += 32;
+                pc2 += 32;
+            }
+            // feed the next strip: lane 31 just finished march s-31
+            if (lane == 31 && a.h_out != nullptr && actv[u]) st_u64(a.h_out + (s - 31), pack_tag(tnw[u], a.tag));
         }
-
-        // carry state
-        if (act) tn = tnew;
-        tvp = tv;
-        cU = nU;
-        cI = nI;
-        if (++pf_slot == kRing) pf_slot = 0;
-        if (++m_slot == kRing) m_slot = 0;
-        if (++wb_slot == kRing) wb_slot = 0;
+        // write back the columns every lane has finished (march s-31)
+        int wb = b0 + (kRing - 31);
+        if (wb >= kRing) wb -= kRing;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int s = s0 + u;
+            if (s >= 31 && s < nsteps) {
+                int ws = wb + u;
+                if (ws >= kRing) ws -= kRing;
+                if (vrow) *pW = Tring[ws * kTP + tix];
+                pW += dT;
+            }
+        }
+        b0 += kU;
+        if (b0 >= kRing) b0 -= kRing;
     }
     cp_wait<0>();
     __syncwarp();
