@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -19,7 +20,7 @@ using namespace sf;
 void sf_adjoint_release(sf_ctx* c)
 {
     void* bufs[] = {c->d_lam, c->d_vrec, c->d_gshot, c->d_pg, c->d_misfit, c->d_colshots, c->d_colptr,
-                    c->d_lam_init, c->d_hand2, c->d_orig_map, c->d_ctr2};
+                    c->d_lam_init, c->d_hand2, c->d_orig_map, c->d_ctr2, c->d_seed_i, c->d_seed_w};
     for (void* b : bufs)
         if (b) cudaFree(b);
 }
@@ -33,6 +34,88 @@ int sf_adj_setup(sf_ctx* c)
 {
     CK(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sf_adj_smem_bytes(kMaxWarps)));
+    return SF_OK;
+}
+
+// Catmull-Rom weights of the pick rule for offset t (the rule is linear in
+// its 16 nodes): P -> P1 + 0.5 t (P2 - P0 + t (2P0 - 5P1 + 4P2 - P3 + t (3(P1 -
+// P2) + P3 - P0))), every FP64 operation rounded once, left to right.
+static void cubic_weights(double t, double w[4])
+{
+    const double t2 = t * t, t3 = t2 * t;
+    w[0] = ((-0.5 * t) + t2) - (0.5 * t3);
+    w[1] = (1.0 - (2.5 * t2)) + (1.5 * t3);
+    w[2] = ((0.5 * t) + (2.0 * t2)) - (1.5 * t3);
+    w[3] = (-0.5 * t2) + (0.5 * t3);
+}
+
+// Seed table of the batch's receivers for the adjoint (host, once per batch):
+// the receiver's node and offsets as the pick rule computes them in FP32
+// (modeling.cu:161-194: the same operations as pick_geom on the device), its
+// 16 weights in FP64 rounded once to FP32, and per padded node the list of
+// (receiver, weight) in receiver order. Whether a receiver's stencil lies in
+// a shot's window is decided per shot from its padded column.
+static int prepare_seed(sf_ctx* c, cudaStream_t st)
+{
+    const int nrec = c->batch_nrec, nzz = c->nzz, nb = c->nb;
+    const float dx = c->dx, dz = c->dz;
+    std::vector<int> rec_jg(std::max(nrec, 1), -1000000);
+    std::vector<std::pair<long long, std::pair<int, float>>> ent;  // (node key, (receiver, weight))
+    for (int r = 0; r < nrec; r++) {
+        const float x = c->h_rx[r], z = c->h_rz[r];
+        const float ax = (x + 0.5f * dx) / dx, az = (z + 0.5f * dz) / dz;
+        const float x0 = std::floor(ax) * dx, z0 = std::floor(az) * dz;
+        const float x1 = std::floor(ax) * dx + dx, z1 = std::floor(az) * dz + dz;
+        const float xd = (x - x0) / (x1 - x0), zd = (z - z0) / (z1 - z0);
+        if (!(ax > -1e9f && ax < 1e9f && az > -1e9f && az < 1e9f)) continue;
+        const int i = (int)az + nb, jg = (int)ax + nb;
+        if (i - 1 < 1 || i + 2 > nzz - 2) continue;  // rows outside the grid: never picked
+        if (jg - 1 < 1 || jg + 2 > c->nxx - 2) continue;  // no window can hold the stencil
+        rec_jg[r] = jg;
+        double wx[4], wz[4];
+        cubic_weights((double)xd, wx);
+        cubic_weights((double)zd, wz);
+        for (int aa = 0; aa < 4; aa++)
+            for (int bb = 0; bb < 4; bb++) {
+                const long long key = (long long)(jg + aa - 1) * nzz + (i + bb - 1);
+                ent.push_back({key, {r, (float)(wx[aa] * wz[bb])}});
+            }
+    }
+    std::stable_sort(ent.begin(), ent.end(),
+                     [](const auto& a, const auto& b) { return a.first < b.first; });  // receiver order kept
+    std::vector<int> ptr(1, 0), row, col, rec;
+    std::vector<float> w;
+    for (size_t e = 0; e < ent.size(); e++) {
+        if (e == 0 || ent[e].first != ent[e - 1].first) {
+            if (e) ptr.push_back((int)e);
+            row.push_back((int)(ent[e].first % nzz));
+            col.push_back((int)(ent[e].first / nzz));
+        }
+        rec.push_back(ent[e].second.first);
+        w.push_back(ent[e].second.second);
+    }
+    ptr.push_back((int)ent.size());
+    if (ent.empty()) ptr.assign(1, 0);
+    const int nn = (int)row.size(), ne = (int)rec.size();
+    std::vector<int> pack;
+    pack.reserve(ptr.size() + 2 * nn + ne + rec_jg.size());
+    pack.insert(pack.end(), ptr.begin(), ptr.end());
+    pack.insert(pack.end(), row.begin(), row.end());
+    pack.insert(pack.end(), col.begin(), col.end());
+    pack.insert(pack.end(), rec.begin(), rec.end());
+    pack.insert(pack.end(), rec_jg.begin(), rec_jg.end());
+    int rc = sf_dev_reserve(c, (void**)&c->d_seed_i, &c->cap_seed_i, pack.size() * sizeof(int));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_seed_w, &c->cap_seed_w, std::max<size_t>(w.size(), 1) * sizeof(float));
+    if (rc) return rc;
+    c->h_seed_pack.swap(pack);
+    c->h_seed_w.swap(w);
+    CK(cudaMemcpyAsync(c->d_seed_i, c->h_seed_pack.data(), c->h_seed_pack.size() * sizeof(int),
+                       cudaMemcpyHostToDevice, st));
+    if (!c->h_seed_w.empty())
+        CK(cudaMemcpyAsync(c->d_seed_w, c->h_seed_w.data(), c->h_seed_w.size() * sizeof(float),
+                           cudaMemcpyHostToDevice, st));
+    c->seed_nodes = nn;
+    c->seed_entries = ne;
     return SF_OK;
 }
 
@@ -82,6 +165,7 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_ctr2, &c->cap_ctr2, nctr * sizeof(unsigned));
     if (rc) return rc;
     rc = prepare_gather(c, st);
+    if (!rc) rc = prepare_seed(c, st);
     if (rc) return rc;
     AdjParams& p = A->p;
     std::memset(&p, 0, sizeof(p));
@@ -108,6 +192,16 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     p.nrec = c->batch_nrec;
     p.lam_init = c->d_lam_init;
     p.err = c->d_flags + 1;
+    {
+        const int nn = c->seed_nodes, ne = c->seed_entries;
+        p.nseed = nn;
+        p.seed_ptr = c->d_seed_i;
+        p.seed_row = c->d_seed_i + nn + 1;
+        p.seed_col = c->d_seed_i + 2 * nn + 1;
+        p.seed_rec = c->d_seed_i + 3 * nn + 1;
+        p.rec_jg = c->d_seed_i + 3 * nn + 1 + ne;
+        p.seed_w = c->d_seed_w;
+    }
     GatherParams& g = A->g;
     std::memset(&g, 0, sizeof(g));
     g.nzz = c->nzz;

@@ -25,7 +25,7 @@
 namespace sf {
 
 constexpr int kLP = 36;    // lambda slot pitch: 32 rows, then the {pv,tag},{pev,tag} handoff pairs
-constexpr int kTR = 16;    // tape ring slots (>= kLook + 2)
+constexpr int kTR = 16;    // tape ring slots (a multiple of kU, > kLook + kU)
 constexpr int kTPitch = 72;  // c1[32], c2[32], code bytes (8 words)
 
 struct AdjRing {
@@ -94,8 +94,8 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         pTc -= 32;
     };
 
-    // let the previous strip get kLook+4 columns ahead before the first prefetches
-    if (consumer) wait_pair(a.h_in + 2 * (size_t)min(kLook + 4, ncols - 1) + 1, a.tag, sh, a.err);
+    // let the previous strip get kAhead columns ahead before the first prefetches
+    if (consumer) wait_pair(a.h_in + 2 * (size_t)min(kAhead, ncols - 1) + 1, a.tag, sh, a.err);
     __syncwarp();
 #pragma unroll 1
     for (int q = 0; q < kLook; q++) prefetch(q, q, q % kTR);
@@ -105,97 +105,134 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     float* pV = a.tc2 + fs0 + flane;
     float* pW = lamg + (size_t)r + (long long)col_of(0) * (long long)nzz;
 
-    int pf_slot = kLook, pf_tslot = kLook % kTR;
-    int m_slot = (kRing - lane) % kRing;
-    int wb_slot = (kRing - 31) % kRing;
-    int t_slot = 0;
     float my_pv = 0.0f, my_pe = 0.0f, my_pev = 0.0f, pev_hold = 0.0f;
+    int b0 = 0, tb0 = 0;  // ring slots of march s0 (lambda, tape)
 
+    // Blocks of kU steps, as in the forward: one wait per block, the block's
+    // ring reads, its kU linear updates (the only serial chain), its stores.
 #pragma unroll 1
-    for (int s = 0; s < nsteps; s++) {
-        prefetch(s + kLook, pf_slot, pf_tslot);
-        cp_wait<kLook - 1>();
+    for (int s0 = 0; s0 < nsteps; s0 += kU) {
+        {
+            int pf0 = b0 + kLook;
+            if (pf0 >= kRing) pf0 -= kRing;
+            int tf0 = tb0 + kLook;
+            if (tf0 >= kTR) tf0 -= kTR;
+#pragma unroll
+            for (int u = 0; u < kU; u++) prefetch(s0 + kLook + u, pf0 + u, tf0 + u);
+        }
+        cp_wait<kLook>();
         __syncwarp();
 
-        const int m = s - lane;
-        const bool act = vrow && (m >= 0) && (m < ncols);
-        float pv_in = __shfl_up_sync(0xffffffffu, my_pv, 1);
-        float pev_in = __shfl_up_sync(0xffffffffu, my_pev, 1);
-        if (lane == 0) {  // upwind row of the strip: the previous strip, or outside the grid
-            pv_in = 0.0f;
-            pev_in = 0.0f;
-            if (consumer && s < ncols) {
-                const unsigned long long* e = reinterpret_cast<const unsigned long long*>(&Lr[m_slot * kLP + 32]);
-                const unsigned long long e0 = e[0], e1 = e[1];
-                if (tag_of(e0) == a.tag && tag_of(e1) == a.tag) {
-                    pv_in = val_of(e0);
-                    pev_in = val_of(e1);
-                } else {
-                    pv_in = wait_pair(a.h_in + 2 * (size_t)s, a.tag, sh, a.err);
-                    pev_in = wait_pair(a.h_in + 2 * (size_t)s + 1, a.tag, sh, a.err);
-                    wait_pair(a.h_in + 2 * (size_t)min(s + kLook + 4, ncols - 1) + 1, a.tag, sh, a.err);
+        int ml = b0 - lane;  // slot of march s0 - lane
+        if (ml < 0) ml += kRing;
+        int msl[kU], code[kU];
+        float lam_in[kU], c1[kU], c2[kU];
+        unsigned long long e0[kU], e1[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            int ms = ml + u;
+            if (ms >= kRing) ms -= kRing;
+            msl[u] = ms;
+            lam_in[u] = Lr[ms * kLP + tix];
+            const int ts = tb0 + u;
+            c1[u] = TPr[ts * kTPitch + flane];
+            c2[u] = TPr[ts * kTPitch + 32 + flane];
+            code[u] = reinterpret_cast<const uint8_t*>(&TPr[ts * kTPitch + 64])[flane];
+            if (consumer) {
+                const unsigned long long* e = reinterpret_cast<const unsigned long long*>(&Lr[ms * kLP + 32]);
+                e0[u] = e[0];
+                e1[u] = e[1];
+            } else {
+                e0[u] = e1[u] = 0ull;
+            }
+        }
+        if (consumer) {
+            // pairs the previous strip had not written when they were prefetched:
+            // wait for them, then fall kAhead columns behind so later prefetches hit
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const int s = s0 + u;
+                if (s < ncols && (tag_of(e0[u]) != a.tag || tag_of(e1[u]) != a.tag)) {
+                    e0[u] = pack_tag(wait_pair(a.h_in + 2 * (size_t)s, a.tag, sh, a.err), a.tag);
+                    e1[u] = pack_tag(wait_pair(a.h_in + 2 * (size_t)s + 1, a.tag, sh, a.err), a.tag);
+                    wait_pair(a.h_in + 2 * (size_t)min(s + kAhead, ncols - 1) + 1, a.tag, sh, a.err);
                 }
             }
         }
-        const float lam_in = Lr[m_slot * kLP + tix];
-        const float c1 = TPr[t_slot * kTPitch + flane];
-        const float c2 = TPr[t_slot * kTPitch + 32 + flane];
-        const int code = reinterpret_cast<const uint8_t*>(&TPr[t_slot * kTPitch + 64])[flane];
 
-        float mu = fadd(fadd(fadd(lam_in, pv_in), my_pe), pev_hold);
-        pev_hold = pev_in;
-        float npv = 0.0f, npe = 0.0f, npev = 0.0f;
-        if (act) {
-            const int br = code & 7;
-            float lo = mu, v = 0.0f;
-            if (br != 0) {
-                lo = 0.0f;
-                v = fmul(mu, c2);
+        float lo[kU], vv[kU], opv[kU], opev[kU];
+        bool actv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int s = s0 + u;
+            const int m = s - lane;
+            const bool act = vrow && (m >= 0) && (m < ncols);
+            float pv_in = __shfl_up_sync(0xffffffffu, my_pv, 1);
+            float pev_in = __shfl_up_sync(0xffffffffu, my_pev, 1);
+            if (lane == 0) {  // upwind row of the strip: the previous strip, or outside the grid
+                const bool have = consumer && s < ncols;
+                pv_in = have ? val_of(e0[u]) : 0.0f;
+                pev_in = have ? val_of(e1[u]) : 0.0f;
+            }
+            const float mu = fadd(fadd(fadd(lam_in[u], pv_in), my_pe), pev_hold);
+            pev_hold = pev_in;
+            float npv = 0.0f, npe = 0.0f, npev = 0.0f, l = mu, v = 0.0f;
+            const int br = code[u] & 7;
+            if (act && br != 0) {
+                l = 0.0f;
+                v = fmul(mu, c2[u]);
+                const float cc = c1[u];
                 switch (br) {
                 case 1: npv = mu; break;
                 case 2: npe = mu; break;
-                case 3: npv = fmul(mu, c1); npe = fmul(mu, -c1); npev = mu; break;
-                case 4: npe = fmul(mu, fsub(1.0f, c1)); npev = fmul(mu, c1); break;
-                default: npv = fmul(mu, fsub(1.0f, c1)); npev = fmul(mu, c1); break;
+                case 3: npv = fmul(mu, cc); npe = fmul(mu, -cc); npev = mu; break;
+                case 4: npe = fmul(mu, fsub(1.0f, cc)); npev = fmul(mu, cc); break;
+                default: npv = fmul(mu, fsub(1.0f, cc)); npev = fmul(mu, cc); break;
                 }
             }
-            Lr[m_slot * kLP + tix] = lo;
-            *pV = v;
-            if (lane == 31 && a.h_out != nullptr) {
-                st_u64(a.h_out + 2 * (size_t)m, pack_tag(npv, a.tag));
-                st_u64(a.h_out + 2 * (size_t)m + 1, pack_tag(npev, a.tag));
+            lo[u] = l;
+            vv[u] = v;
+            opv[u] = npv;
+            opev[u] = npev;
+            actv[u] = act;
+            my_pv = npv;
+            my_pe = npe;
+            my_pev = npev;
+        }
+
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int s = s0 + u;
+            if (actv[u]) {
+                Lr[msl[u] * kLP + tix] = lo[u];
+                *pV = vv[u];
+                if (lane == 31 && a.h_out != nullptr) {
+                    const int m = s - 31;
+                    st_u64(a.h_out + 2 * (size_t)m, pack_tag(opv[u], a.tag));
+                    st_u64(a.h_out + 2 * (size_t)m + 1, pack_tag(opev[u], a.tag));
+                }
+            }
+            pV -= 32;
+        }
+        int wb = b0 + (kRing - 31);  // slot of march s0 - 31
+        if (wb >= kRing) wb -= kRing;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int s = s0 + u;
+            if (s >= 31 && s < nsteps) {
+                int ws = wb + u;
+                if (ws >= kRing) ws -= kRing;
+                if (vrow) *pW = Lr[ws * kLP + tix];
+                pW += dL;
             }
         }
-        my_pv = npv;
-        my_pe = npe;
-        my_pev = npev;
-
-        pV -= 32;
-        if (s >= 31) {
-            if (vrow) *pW = Lr[wb_slot * kLP + tix];
-            pW += dL;
-        }
-
-        if (++pf_slot == kRing) pf_slot = 0;
-        if (++pf_tslot == kTR) pf_tslot = 0;
-        if (++m_slot == kRing) m_slot = 0;
-        if (++wb_slot == kRing) wb_slot = 0;
-        if (++t_slot == kTR) t_slot = 0;
+        b0 += kU;
+        if (b0 >= kRing) b0 -= kRing;
+        tb0 += kU;
+        if (tb0 >= kTR) tb0 -= kTR;
     }
     cp_wait<0>();
     __syncwarp();
-}
-
-// Cubic weights of the pick rule (the rule is linear in the 16 nodes):
-// P -> P1 + 0.5 t (P2 - P0 + t (2P0 - 5P1 + 4P2 - P3 + t (3(P1 - P2) + P3 - P0)))
-// (every FP64 operation rounded once, left to right, as written)
-__device__ __forceinline__ void cubic_weights(double t, double w[4])
-{
-    const double t2 = __dmul_rn(t, t), t3 = __dmul_rn(t2, t);
-    w[0] = __dsub_rn(__dadd_rn(__dmul_rn(-0.5, t), t2), __dmul_rn(0.5, t3));
-    w[1] = __dadd_rn(__dsub_rn(1.0, __dmul_rn(2.5, t2)), __dmul_rn(1.5, t3));
-    w[2] = __dsub_rn(__dadd_rn(__dmul_rn(0.5, t), __dmul_rn(2.0, t2)), __dmul_rn(1.5, t3));
-    w[3] = __dadd_rn(__dmul_rn(-0.5, t2), __dmul_rn(0.5, t3));
 }
 
 // (kMaxWarps * 32, 1): the block size alone as the bound caps the kernel at
@@ -220,30 +257,31 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
         const ShotDev sh = p.shots[b];
         const int ncols = sh.ncols;
         const unsigned tag = (p.epoch << 10) | (unsigned)(it & 1023);
-        // seed: adjoint of the final field from the pick gradients
-        for (int k = gp.slot; k < nstrips; k += gp.slots) {
-            const int i = 32 * k + lane;
-            if (i < nzz)
-                for (int j = 0; j < ncols; j++) lam[(size_t)i + (size_t)j * nzz] = 0.0f;
-        }
-        gang_barrier(bar, (++nbar) * p.G, cs, p.err);
-        if (gp.g == 0 && gp.warp == 0) {
+        // seed: adjoint of the final field from the pick gradients. The window
+        // is zeroed by the whole gang, then each seeded node sums its
+        // receivers' terms in receiver order (the order of a receiver-by-
+        // receiver accumulation, hence the same bits).
+        {
+            const int gt = gp.g * blockDim.x + tid, gn = p.G * blockDim.x;
+            const size_t nw = (size_t)nzz * ncols;
+#pragma unroll 4
+            for (size_t q = gt; q < nw; q += gn) lam[q] = 0.0f;
+            gang_barrier(bar, (++nbar) * p.G, cs, p.err);
             const float* pg = p.pick_grad + (size_t)sh.orig * p.nrec;
-            for (int rr = 0; rr < p.nrec; rr++) {
-                const float g = pg[rr];
-                int i, j;
-                float xd, zd;
-                const bool ok = pick_geom(p.rx[rr], p.rz[rr], p.dx, p.dz, p.nb, nzz, ncols, sh.c0, i, j, xd, zd);
-                if (ok && g == g && lane < 16) {
-                    double wx[4], wz[4];
-                    cubic_weights((double)xd, wx);
-                    cubic_weights((double)zd, wz);
-                    const int aa = lane >> 2, bb = lane & 3;
-                    const float w = __double2float_rn(__dmul_rn(wx[aa], wz[bb]));
-                    float* at = lam + (size_t)(i + bb - 1) + (size_t)(j + aa - 1) * nzz;
-                    *at = fadd(*at, fmul(g, w));
+            for (int n = gt; n < p.nseed; n += gn) {
+                const int col = p.seed_col[n] - sh.c0;
+                if (col < 0 || col >= ncols) continue;
+                float acc = 0.0f;
+                bool any = false;
+                for (int e = p.seed_ptr[n]; e < p.seed_ptr[n + 1]; e++) {
+                    const int rr = p.seed_rec[e];
+                    const int jl = p.rec_jg[rr] - sh.c0;
+                    const float g = pg[rr];
+                    if (jl - 1 < 1 || jl + 2 > ncols - 2 || !(g == g)) continue;
+                    acc = fadd(acc, fmul(g, p.seed_w[e]));
+                    any = true;
                 }
-                __syncwarp();
+                if (any) lam[(size_t)p.seed_row[n] + (size_t)col * nzz] = acc;
             }
         }
         gang_barrier(bar, (++nbar) * p.G, cs, p.err);

@@ -25,6 +25,17 @@ struct AdjParams {
     int nrec;
     float* lam_init;        // nshots x 9, caller order: adjoint of the 3x3 initial values
     int* err;
+    // seed table: node n (row seed_row[n], padded column seed_col[n]) gets, in
+    // receiver order, pick_grad[r] * seed_w[e] for entries e of
+    // [seed_ptr[n], seed_ptr[n+1]) whose receiver r = seed_rec[e] has its
+    // stencil inside the shot's window (column rec_jg[r] - c0)
+    int nseed;
+    const int* seed_ptr;
+    const int* seed_row;
+    const int* seed_col;
+    const int* seed_rec;
+    const int* rec_jg;
+    const float* seed_w;
 };
 
 struct GatherParams {

@@ -91,6 +91,13 @@ struct sf_ctx {
     unsigned long long* d_hand2 = nullptr; size_t cap_hand2 = 0;
     unsigned* d_ctr2 = nullptr; size_t cap_ctr2 = 0;
     std::vector<int> h_colptr, h_colshots;
+    // adjoint seed table (receivers of the batch): seeded nodes, CSR of
+    // their (receiver, weight) entries in receiver order
+    int* d_seed_i = nullptr; size_t cap_seed_i = 0;    // [ptr nn+1][row nn][gcol nn][rec ne][rec_jg nrec]
+    float* d_seed_w = nullptr; size_t cap_seed_w = 0;
+    int seed_nodes = 0, seed_entries = 0;
+    std::vector<int> h_seed_pack;
+    std::vector<float> h_seed_w;
 
     // per-kernel timing (sf_set_kernel_timing)
     bool timing = false;
