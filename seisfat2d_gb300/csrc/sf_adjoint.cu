@@ -19,8 +19,8 @@ using namespace sf;
 
 void sf_adjoint_release(sf_ctx* c)
 {
-    void* bufs[] = {c->d_lam, c->d_vrec, c->d_gshot, c->d_pg, c->d_misfit, c->d_colshots, c->d_colptr,
-                    c->d_lam_init, c->d_hand2, c->d_orig_map, c->d_ctr2, c->d_seed_i, c->d_seed_w};
+    void* bufs[] = {c->d_lam, c->d_vrec, c->d_gshot, c->d_pg, c->d_misfit, c->d_colptr,
+                    c->d_lam_init, c->d_hand2, c->d_ctr2, c->d_seed_i, c->d_seed_w, c->d_gshots};
     for (void* b : bufs)
         if (b) cudaFree(b);
 }
@@ -119,33 +119,44 @@ static int prepare_seed(sf_ctx* c, cudaStream_t st)
     return SF_OK;
 }
 
-// Device buffers of the gather (shots per column, caller order) for the last
-// taped batch; rebuilt when the batch changes.
+// The gather's shot lists (host, once per batch): for each block of kGT
+// padded columns, the shots whose window covers any of its columns, in caller
+// order, with what the gather needs of each.
 static int prepare_gather(sf_ctx* c, cudaStream_t st)
 {
     const int ns = (int)c->hshots.size();
-    std::vector<int> cnt(c->nxx + 1, 0);
-    std::vector<const ShotDev*> by_orig(ns);
-    for (const ShotDev& d : c->hshots) by_orig[d.orig] = &d;
-    for (int o = 0; o < ns; o++)
-        for (int j = by_orig[o]->c0; j < by_orig[o]->c0 + by_orig[o]->ncols; j++) cnt[j + 1]++;
-    for (int j = 0; j < c->nxx; j++) cnt[j + 1] += cnt[j];
-    std::vector<int> shots_of_col(cnt[c->nxx]);
-    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-    for (int o = 0; o < ns; o++)
-        for (int j = by_orig[o]->c0; j < by_orig[o]->c0 + by_orig[o]->ncols; j++) shots_of_col[fill[j]++] = o;
-    int rc = sf_dev_reserve(c, (void**)&c->d_colptr, &c->cap_colptr, cnt.size() * sizeof(int));
-    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_colshots, &c->cap_colshots,
-                                 std::max<size_t>(1, shots_of_col.size()) * sizeof(int));
-    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_orig_map, &c->cap_orig_map, ns * sizeof(int));
+    const int nblk = (c->nxx + kGT - 1) / kGT;
+    std::vector<int> ptr(nblk + 1, 0);
+    std::vector<GatherShot> ent;
+    for (int cb = 0; cb < nblk; cb++) {
+        const int col = cb * kGT;
+        for (int o = 0; o < ns; o++) {
+            const ShotDev& d = c->hshots[c->tables_index[o]];
+            if (d.c0 < col + kGT && d.c0 + d.ncols > col) {
+                GatherShot g;
+                std::memset(&g, 0, sizeof(g));
+                g.tape_off = d.tape_off;
+                g.c0 = d.c0;
+                g.ncols = d.ncols;
+                g.sIdx = d.sIdx;
+                g.sIdz = d.sIdz;
+                g.sx = d.sx;
+                g.sz = d.sz;
+                g.orig = o;
+                ent.push_back(g);
+            }
+        }
+        ptr[cb + 1] = (int)ent.size();
+    }
+    int rc = sf_dev_reserve(c, (void**)&c->d_colptr, &c->cap_colptr, ptr.size() * sizeof(int));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_gshots, &c->cap_gshots, std::max<size_t>(ent.size(), 1) * sizeof(GatherShot));
     if (rc) return rc;
-    c->h_colptr.swap(cnt);
-    c->h_colshots.swap(shots_of_col);
+    c->h_colptr.swap(ptr);
+    c->h_gshots.swap(ent);
     CK(cudaMemcpyAsync(c->d_colptr, c->h_colptr.data(), c->h_colptr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    if (!c->h_colshots.empty())
-        CK(cudaMemcpyAsync(c->d_colshots, c->h_colshots.data(), c->h_colshots.size() * sizeof(int),
+    if (!c->h_gshots.empty())
+        CK(cudaMemcpyAsync(c->d_gshots, c->h_gshots.data(), c->h_gshots.size() * sizeof(GatherShot),
                            cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->d_orig_map, c->tables_index.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
     return SF_OK;
 }
 
@@ -208,16 +219,14 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     g.nxx = c->nxx;
     g.nb = c->nb;
     g.nstrips = nstrips;
+    g.nshots = ns;
     g.dx = c->dx;
     g.dz = c->dz;
-    g.shots = c->d_shots;
-    g.shot_of_orig = c->d_orig_map;
-    g.colptr = c->d_colptr;
-    g.colshots = c->d_colshots;
+    g.blk_ptr = c->d_colptr;
+    g.blk_shots = c->d_gshots;
     g.tcode = c->d_tcode;
     g.vrec = c->d_tc2;
     g.lam_init = c->d_lam_init;
-    const size_t ncell = (size_t)c->nzz * c->nxx;
     A->kern = (const void*)k_adjoint;
     A->gkern = (const void*)k_gather;
     A->grid = dim3(NG * G);
@@ -225,7 +234,7 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     A->smem = smem;
     A->nctr = nctr;
     A->hand_bytes = (size_t)NG * 4 * nstrips * c->batch_maxcols * 2 * sizeof(unsigned long long);
-    A->ggrid = dim3((unsigned)std::min<size_t>((ncell + 255) / 256, (size_t)c->sms * 16));
+    A->ggrid = dim3((unsigned)(nstrips * ((c->nxx + kGT - 1) / kGT)));
     A->gblock = dim3(256);
     return SF_OK;
 }
@@ -244,7 +253,7 @@ int sf_adj_enqueue(sf_ctx* c, AdjLaunch& A, const float* d_pg, float* d_grad, un
     if (!rc) rc = sf_kt_begin(c, SF_KT_GATHER, st);
     if (rc) return rc;
     void* gargs[] = {&A.g};
-    CK(cudaLaunchKernel(A.gkern, A.ggrid, A.gblock, gargs, 0, st));
+    CK(cudaLaunchKernel(A.gkern, A.ggrid, A.gblock, gargs, sizeof(GatherSmem), st));
     return sf_kt_end(c, SF_KT_GATHER, st);
 }
 

@@ -329,49 +329,151 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
     }
 }
 
-// Tape index of node (i, j) (window coordinates) in forward sweep sw.
-__device__ __forceinline__ size_t tape_index(const ShotDev& sh, int sw, int i, int j, int nstrips, int nzz)
-{
-    const int k = i >> 5;
-    const bool szpos = !(sw == 1 || sw == 3);
-    const bool sxpos = sw < 2;
-    const int flane = szpos ? (i - 32 * k) : (32 * k + 31 - i);
-    const int fm = sxpos ? j : sh.ncols - 1 - j;
-    return tape_strip_base(sh.tape_off, sw, k, nstrips, sh.ncols) + (size_t)(fm + flane) * 32 + flane;
-}
-
 // g(a, b) = sum over shots (caller order, FP64) of the shot's FP32 sum over
 // sweeps 0..3 and corners (dr, dc) = (0,0),(0,1),(1,0),(1,1) of the matching
 // node terms, plus the 3x3 initialisation term lam_init * dist.
-__global__ void k_gather(GatherParams p)
+//
+// One CTA per tile of 32 rows (one strip) x kGT columns. The terms of node
+// (i, j) in a sweep sit in the tape in the forward strip's skewed step order,
+// so the nodes a tile reads (its rows and the first row of the next strip,
+// its columns and one more) are, per shot and sweep, one contiguous run of
+// kGT + 32 tape steps of the strip plus kGT + 1 entries of the next strip.
+// These runs stream through kGStages shared-memory stages (cp.async) while
+// the threads sum their cells' terms in the order above. The shots covering
+// the tile's columns come from a per-column-block list built on the host,
+// staged in shared memory kGChunk at a time.
+constexpr int kGT = 32;             // tile columns
+constexpr int kGSteps = kGT + 32;   // tape steps a tile's strip spans per sweep
+constexpr int kGStages = 3;
+constexpr int kGChunk = 128;
+
+struct __align__(16) GatherStage {
+    float v[kGSteps * 32];
+    uint32_t code[kGSteps * 8];      // code bytes
+    float v2[kGT + 1];               // next strip, first row
+    uint32_t code2[kGT + 1];         // the aligned words holding its code bytes
+};
+
+struct GatherSmem {
+    GatherStage stg[kGStages];
+    GatherShot shots[kGChunk];
+};
+
+__global__ void __launch_bounds__(256) k_gather(GatherParams p)
 {
-    const size_t ncell = (size_t)p.nzz * p.nxx;
-    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < ncell;
-         cell += (size_t)gridDim.x * blockDim.x) {
-        const int a = (int)(cell % p.nzz), bcol = (int)(cell / p.nzz);
-        double total = 0.0;
-        for (int q = p.colptr[bcol]; q < p.colptr[bcol + 1]; q++) {
-            const int orig = p.colshots[q];
-            const ShotDev sh = p.shots[p.shot_of_orig[orig]];
-            const int b = bcol - sh.c0;
-            float g = 0.0f;
-            for (int sw = 0; sw < 4; sw++)
+    extern __shared__ __align__(16) unsigned char gsm_raw[];
+    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(gsm_raw);
+    const int tid = threadIdx.x;
+    const int ntx = (p.nxx + kGT - 1) / kGT;
+    const int k = blockIdx.x / ntx, cb = blockIdx.x % ntx, c = cb * kGT;
+    const int rb = 32 * k;
+    const bool next_strip = k + 1 < p.nstrips;
+    const int a = rb + (tid & 31);   // the thread's cells: row a, columns c + (tid>>5) + 8q
+    const int cq = tid >> 5;
+
+    // node-column range of stage (shot entry e, sweep sw) in march order
+    auto fm_range = [&](const GatherShot& t, int sw, int& fmlo, int& fmhi) {
+        const int jlo = max(c - t.c0, 0);
+        const int jhi = min(c + kGT - t.c0, t.ncols - 1);   // covered cells' columns and one more
+        fmlo = (sw < 2) ? jlo : t.ncols - 1 - jhi;
+        fmhi = (sw < 2) ? jhi : t.ncols - 1 - jlo;
+    };
+    auto issue = [&](const GatherShot& t, int sw, GatherStage& S) {
+        int fmlo, fmhi;
+        fm_range(t, sw, fmlo, fmhi);
+        const int nst = t.ncols + 31;
+        const size_t base = tape_strip_base(t.tape_off, sw, k, p.nstrips, t.ncols);
+        for (int q = tid; q < kGSteps * 8; q += blockDim.x) {
+            const int st = fmlo + (q >> 3);
+            if (st < nst) cp_async16(&S.v[q * 4], p.vrec + base + (size_t)st * 32 + (q & 7) * 4);
+        }
+        for (int q = tid; q < kGSteps * 2; q += blockDim.x) {
+            const int st = fmlo + (q >> 1);
+            if (st < nst) cp_async16(&S.code[q * 4], p.tcode + base + (size_t)st * 32 + (q & 1) * 16);
+        }
+        if (next_strip) {
+            const size_t base2 = tape_strip_base(t.tape_off, sw, k + 1, p.nstrips, t.ncols);
+            const int fl2 = (sw == 1 || sw == 3) ? 31 : 0;
+            for (int q = tid; q <= fmhi - fmlo; q += blockDim.x) {
+                const size_t e = base2 + (size_t)(fmlo + q + fl2) * 32 + fl2;
+                cp_async4(&S.v2[q], p.vrec + e);
+                cp_async4(&S.code2[q], p.tcode + (e & ~(size_t)3));
+            }
+        }
+        cp_commit();
+    };
+
+    double total[4] = {0.0, 0.0, 0.0, 0.0};
+    float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int e_end = p.blk_ptr[cb + 1];
+#pragma unroll 1
+    for (int e0 = p.blk_ptr[cb]; e0 < e_end; e0 += kGChunk) {
+        const int n = min(kGChunk, e_end - e0);
+        __syncthreads();  // the previous chunk's list and stages are no longer read
+        for (int q = tid; q < n; q += blockDim.x) sm.shots[q] = p.blk_shots[e0 + q];
+        __syncthreads();
+        const int nst = 4 * n;  // stages (entry, sweep) of the chunk
+        for (int i = 0; i < kGStages - 1 && i < nst; i++) issue(sm.shots[i >> 2], i & 3, sm.stg[i]);
+#pragma unroll 1
+        for (int i = 0; i < nst; i++) {
+            const int ahead = min(kGStages - 1, nst - 1 - i);  // stages issued after stage i
+            if (i + kGStages - 1 < nst) {
+                const int j = i + kGStages - 1;
+                issue(sm.shots[j >> 2], j & 3, sm.stg[j % kGStages]);
+                cp_wait<kGStages - 1>();
+            } else if (ahead == 1) {
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();
+            const GatherShot& t = sm.shots[i >> 2];
+            const int sw = i & 3;
+            const bool szpos = !(sw == 1 || sw == 3), sxpos = sw < 2;
+            int fmlo, fmhi;
+            fm_range(t, sw, fmlo, fmhi);
+            const GatherStage& S = sm.stg[i % kGStages];
+            const unsigned char* cbytes = reinterpret_cast<const unsigned char*>(S.code);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int bc = c + cq + 8 * q;
+                const int bl = bc - t.c0;
+                if (a >= p.nzz || bc >= p.nxx || bl < 0 || bl >= t.ncols) continue;
                 for (int dr = 0; dr < 2; dr++)
                     for (int dc = 0; dc < 2; dc++) {
-                        const int i = a + 1 - dr, j = b + 1 - dc;
-                        if (i >= p.nzz || j >= sh.ncols) continue;
-                        const size_t t = tape_index(sh, sw, i, j, p.nstrips, p.nzz);
-                        const int cd = p.tcode[t];
-                        if ((cd & 7) && ((cd >> 3) & 1) == dr && ((cd >> 4) & 1) == dc) g = fadd(g, p.vrec[t]);
+                        const int ni = a + 1 - dr, nj = bl + 1 - dc;
+                        if (ni >= p.nzz || nj >= t.ncols) continue;
+                        const int fm = sxpos ? nj : t.ncols - 1 - nj;
+                        int cd;
+                        float v;
+                        if (ni < rb + 32) {
+                            const int fl = szpos ? ni - rb : rb + 31 - ni;
+                            const int idx = (fm + fl - fmlo) * 32 + fl;
+                            cd = cbytes[idx];
+                            v = S.v[idx];
+                        } else {
+                            const int q2 = fm - fmlo;
+                            cd = (S.code2[q2] >> (szpos ? 0 : 24)) & 0xff;
+                            v = S.v2[q2];
+                        }
+                        if ((cd & 7) && ((cd >> 3) & 1) == dr && ((cd >> 4) & 1) == dc) g[q] = fadd(g[q], v);
                     }
-            const int da = a - sh.sIdz + 1, db = bcol - sh.sIdx + 1;
-            if (da >= 0 && da < 3 && db >= 0 && db < 3) {
-                const double d = src_dist(a, bcol, p.nb, p.dx, p.dz, sh.sx, sh.sz);
-                g = fadd(g, fmul(p.lam_init[(size_t)orig * 9 + da + 3 * db], __double2float_rn(d)));
+                if (sw == 3) {
+                    const int da = a - t.sIdz + 1, db = bc - t.sIdx + 1;
+                    if (da >= 0 && da < 3 && db >= 0 && db < 3) {
+                        const double d = src_dist(a, bc, p.nb, p.dx, p.dz, t.sx, t.sz);
+                        g[q] = fadd(g[q], fmul(p.lam_init[(size_t)t.orig * 9 + da + 3 * db], __double2float_rn(d)));
+                    }
+                    total[q] += (double)g[q];
+                    g[q] = 0.0f;
+                }
             }
-            total += (double)g;
+            __syncthreads();  // stage i's buffer is refilled by stage i + kGStages
         }
-        p.grad[cell] = __double2float_rn(total);
+    }
+    for (int q = 0; q < 4; q++) {
+        const int bc = c + cq + 8 * q;
+        if (a < p.nzz && bc < p.nxx) p.grad[(size_t)a + (size_t)bc * p.nzz] = __double2float_rn(total[q]);
     }
 }
 

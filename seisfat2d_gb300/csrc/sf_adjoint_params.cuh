@@ -38,13 +38,21 @@ struct AdjParams {
     const float* seed_w;
 };
 
+// A shot as the gather sees it: one entry per (column block, shot covering
+// it), caller order within a block.
+struct GatherShot {
+    long long tape_off;
+    int c0, ncols;
+    int sIdx, sIdz;
+    float sx, sz;
+    int orig, pad_;
+};
+
 struct GatherParams {
-    int nzz, nxx, nb, nstrips;
+    int nzz, nxx, nb, nstrips, nshots;
+    const int* blk_ptr;            // entries of column block cb: [blk_ptr[cb], blk_ptr[cb+1])
+    const GatherShot* blk_shots;
     float dx, dz;
-    const ShotDev* shots;    // sorted table; shot_of_orig maps caller index -> table row
-    const int* shot_of_orig;
-    const int* colptr;       // CSR over padded columns: caller-order shot indices covering it
-    const int* colshots;
     const uint8_t* tcode;
     const float* vrec;       // v terms (tape c2 after the reverse sweeps)
     const float* lam_init;   // nshots x 9 (caller order)

@@ -84,13 +84,13 @@ struct sf_ctx {
     float* d_gshot = nullptr; size_t cap_gshot = 0;
     float* d_pg = nullptr; size_t cap_pg = 0;
     double* d_misfit = nullptr; size_t cap_misfit = 0;
-    int* d_colshots = nullptr; size_t cap_colshots = 0;
     int* d_colptr = nullptr; size_t cap_colptr = 0;
-    int* d_orig_map = nullptr; size_t cap_orig_map = 0;
     float* d_lam_init = nullptr; size_t cap_lam_init = 0;
     unsigned long long* d_hand2 = nullptr; size_t cap_hand2 = 0;
     unsigned* d_ctr2 = nullptr; size_t cap_ctr2 = 0;
-    std::vector<int> h_colptr, h_colshots;
+    std::vector<int> h_colptr;
+    sf::GatherShot* d_gshots = nullptr; size_t cap_gshots = 0;
+    std::vector<sf::GatherShot> h_gshots;
     // adjoint seed table (receivers of the batch): seeded nodes, CSR of
     // their (receiver, weight) entries in receiver order
     int* d_seed_i = nullptr; size_t cap_seed_i = 0;    // [ptr nn+1][row nn][gcol nn][rec ne][rec_jg nrec]
