@@ -267,7 +267,8 @@ def run_ours(a):
     w = workload(a.config)
     fa = a.config in FA_CONFIGS
     ani = w.cij is not None
-    shots = w.shots[rank::world]
+    from seisfat2d_gb300.shard import shard
+    shots = shard(w.shots, rank, world)
     nrec = len(w.rx)
     eng = Engine(w.nx, w.nz, w.dx, w.dz, device=local)
     eng.set_arithmetic(a.arith)

@@ -204,6 +204,27 @@ int sf_plan_autotune(sf_ctx* ctx, const float* t_obs, float* picks, double* misf
 int sf_set_kernel_timing(sf_ctx* ctx, int enable);
 int sf_kernel_times(sf_ctx* ctx, float* ms, int n);
 
+/* ---- tomography model update (src/inversion/inversion.cpp:347-447,
+ * src/inversion/tomography_iso.cpp:77-92) ----
+ *
+ * sf_smooth_model: the reference's Inversion::model_smoothing of a model-sized
+ * field (nz x nx, z fastest; in and out host or device per `mem`, distinct):
+ * zero padding of `samples` cells, normalised Gaussian taps 1/(pi stdv)
+ * exp(-r^2/(2 stdv^2)) over samples x samples cells (stdv 0: identity),
+ * FP32 products summed in the reference's tap order. samples must be odd
+ * (the reference indexes past its kernel for even counts); with host memory
+ * the call synchronises `stream`.
+ *
+ * sf_update_slowness: Tomography_ISO::model_update on the context's slowness:
+ * dS = scale * grad over the model interior of a padded gradient (as from
+ * sf_batch_misfit_gradient; grad_mem says where it is), smoothed as above
+ * unless samples is 0, then S += dS on the interior (the pad ring keeps its
+ * values, as in the reference). dS (model-sized, may be null) receives the
+ * applied update. Synchronises `stream`. */
+int sf_smooth_model(sf_ctx* ctx, const float* in, float* out, float stdv, int samples, int mem, void* stream);
+int sf_update_slowness(sf_ctx* ctx, const float* grad, int grad_mem, float scale, float stdv, int samples,
+                       float* dS, int dS_mem, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

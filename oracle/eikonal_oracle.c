@@ -1008,3 +1008,77 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
     free(off);
     return bad ? -1 : used;
 }
+
+/* ---------------------------------------------------- tomography update */
+
+#define ORC_PI 3.14159265358979323846 /* M_PI of the reference's math.h */
+
+/* Inversion::smooth_matrix's kernel (src/inversion/inversion.cpp:387-418):
+ * the prefactor 1/(M_PI*stdv) in double, expf of a float argument, the
+ * product rounded once to float; FP32 sum (x outer, z inner); division by it. */
+void orc_smooth_kernel(float stdv, int n, float* k)
+{
+    int mid = n / 2;
+    for (int q = 0; q < n * n; q++) k[q] = 0.0f;
+    k[mid + mid * n] = 1.0f;
+    if (stdv == 0.0f) return;
+    float sum = 0.0f;
+    for (int x = -mid; x <= mid; x++)
+        for (int z = -mid; z <= mid; z++) {
+            int index = (z + mid) + (x + mid) * n;
+            float r = sqrtf((float)(x * x + z * z));
+            k[index] = (float)(1.0f / (ORC_PI * stdv) * (double)expf(-((r * r) / (2.0f * stdv * stdv))));
+            sum += k[index];
+        }
+    for (int q = 0; q < n * n; q++) k[q] /= sum;
+}
+
+/* Inversion::model_smoothing + smooth_matrix (inversion.cpp:347-447) as
+ * written: the model (nz x nx) copied into a zero grid padded by `samples`
+ * cells, the padded grid smoothed where the kernel fits (FP32, xk outer, zk
+ * inner, product then sum), the model window copied back. */
+void orc_model_smoothing(const float* model, int nx, int nz, float stdv, int samples, float* out)
+{
+    int anx = nx + 2 * samples, anz = nz + 2 * samples;
+    size_t an = (size_t)anx * anz;
+    float* aux = (float*)calloc(an, sizeof(float));
+    float* sm = (float*)calloc(an, sizeof(float));
+    float* k = (float*)malloc(sizeof(float) * (size_t)samples * samples);
+    for (int j = 0; j < nx; j++)
+        for (int i = 0; i < nz; i++) aux[(i + samples) + (size_t)(j + samples) * anz] = model[i + (size_t)j * nz];
+    orc_smooth_kernel(stdv, samples, k);
+    for (size_t q = 0; q < an; q++) sm[q] = aux[q];
+    int mid = samples / 2;
+    for (int j = mid; j < anx - mid; j++)
+        for (int i = mid; i < anz - mid; i++) {
+            float accum = 0.0f;
+            for (int xk = 0; xk < samples; xk++)
+                for (int zk = 0; zk < samples; zk++) {
+                    float prod = aux[(i - mid + zk) + (size_t)(j - mid + xk) * anz] * k[zk + xk * samples];
+                    accum = accum + prod;
+                }
+            sm[i + (size_t)j * anz] = accum;
+        }
+    for (int j = 0; j < nx; j++)
+        for (int i = 0; i < nz; i++) out[i + (size_t)j * nz] = sm[(i + samples) + (size_t)(j + samples) * anz];
+    free(aux);
+    free(sm);
+    free(k);
+}
+
+/* Tomography_ISO::model_update (tomography_iso.cpp:77-92) on a padded
+ * slowness S (nzz x nxx): dS = scale * grad over the model interior,
+ * smoothed unless samples == 0, added to the interior; dS returned. */
+void orc_update_slowness(float* S, const float* grad, int nx, int nz, int nb, float scale, float stdv,
+                         int samples, float* dS)
+{
+    int nzz = nz + 2 * nb;
+    float* d = (float*)malloc(sizeof(float) * (size_t)nx * nz);
+    for (int j = 0; j < nx; j++)
+        for (int i = 0; i < nz; i++) d[i + (size_t)j * nz] = scale * grad[(i + nb) + (size_t)(j + nb) * nzz];
+    if (samples != 0) orc_model_smoothing(d, nx, nz, stdv, samples, dS);
+    else memcpy(dS, d, sizeof(float) * (size_t)nx * nz);
+    for (int j = 0; j < nx; j++)
+        for (int i = 0; i < nz; i++) S[(i + nb) + (size_t)(j + nb) * nzz] += dS[i + (size_t)j * nz];
+    free(d);
+}

@@ -147,6 +147,15 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
                            const float* rx, const float* rz, int nrec, const float* tobs,
                            float* picks, double* misfit, float* grad, int nthreads);
 
+/* Tomography update (inversion.cpp:347-447, tomography_iso.cpp:77-92):
+ * the Gaussian kernel of smooth_matrix (n x n, x major), model_smoothing of a
+ * model-sized field (nz x nx, z fastest) and the slowness update of a padded
+ * model (see the definitions for the arithmetic). */
+void orc_smooth_kernel(float stdv, int n, float* k);
+void orc_model_smoothing(const float* model, int nx, int nz, float stdv, int samples, float* out);
+void orc_update_slowness(float* S, const float* grad, int nx, int nz, int nb, float scale, float stdv,
+                         int samples, float* dS);
+
 /* Arithmetic of the FP32 solvers: 0 = every operation rounded once and the
  * 3x3 initialisation in FP64 (default); 1 = the reference build's arithmetic:
  * FP32 initialisation and fused multiply-adds where nvcc forms them in

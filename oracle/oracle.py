@@ -75,6 +75,10 @@ def lib():
                                              C.c_int, f32p, f32p, i32p, i32p, f32p, f32p, C.c_int,
                                              f32p, f32p, C.POINTER(C.c_double), f32p, C.c_int]
         L.orc_batch_gradient_f32.restype = C.c_int
+        L.orc_smooth_kernel.argtypes = [C.c_float, C.c_int, f32p]
+        L.orc_model_smoothing.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_int, f32p]
+        L.orc_update_slowness.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
+                                          f32p]
         _lib = L
     return _lib
 
@@ -274,6 +278,29 @@ def batch_misfit_gradient(S, dx, dz, shots, rx, rz, t_obs, nb=3, nthreads=0):
     if used < 0:
         raise ValueError("a source lies outside its window")
     return mis.value, grad, picks, used
+
+
+def smooth_kernel(stdv, samples):
+    k = np.zeros(samples * samples, np.float32)
+    lib().orc_smooth_kernel(stdv, samples, k)
+    return k.reshape(samples, samples)  # [x, z]
+
+
+def model_smoothing(model, stdv, samples):
+    """The reference's model_smoothing of an (nx, nz) field."""
+    m = _f32(model)
+    out = np.zeros_like(m)
+    lib().orc_model_smoothing(m, m.shape[0], m.shape[1], stdv, samples, out)
+    return out
+
+
+def update_slowness(S, grad, nx, nz, scale, stdv=0.0, samples=0, nb=3):
+    """Tomography_ISO::model_update on a copy of the padded slowness S;
+    returns (S_new, dS)."""
+    Sn = _f32(S).copy()
+    dS = np.zeros((nx, nz), np.float32)
+    lib().orc_update_slowness(Sn, _f32(grad), nx, nz, nb, scale, stdv, samples, dS)
+    return Sn, dS
 
 
 def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):

@@ -65,6 +65,8 @@ SIGNATURES = {
     "sf_plan_autotune": (C.c_int, [VP, VP, VP, VP, VP, C.c_int, VP, IP, IP, FP]),
     "sf_set_kernel_timing": (C.c_int, [VP, C.c_int]),
     "sf_kernel_times": (C.c_int, [VP, FP, C.c_int]),
+    "sf_smooth_model": (C.c_int, [VP, VP, VP, C.c_float, C.c_int, C.c_int, VP]),
+    "sf_update_slowness": (C.c_int, [VP, VP, C.c_int, C.c_float, C.c_float, C.c_int, VP, C.c_int, VP]),
 }
 
 _lib = None

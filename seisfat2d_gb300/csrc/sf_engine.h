@@ -99,6 +99,11 @@ struct sf_ctx {
     std::vector<int> h_seed_pack;
     std::vector<float> h_seed_w;
 
+    // model update (sf_smooth_model, sf_update_slowness)
+    float* d_skern = nullptr; size_t cap_skern = 0;
+    float* d_upd = nullptr; size_t cap_upd = 0;
+    std::vector<float> h_skern;
+
     // per-kernel timing (sf_set_kernel_timing)
     bool timing = false;
     cudaEvent_t kt_ev[SF_KT_N][2] = {};
@@ -148,6 +153,8 @@ int sf_upload_receivers(sf_ctx* c, const float* rx, const float* rz, int nrec, c
 int sf_kt_begin(sf_ctx* c, int k, cudaStream_t st);
 int sf_kt_end(sf_ctx* c, int k, cudaStream_t st);
 void sf_plan_release(sf_ctx* c);
+// Normalised Gaussian taps of the reference's smooth_matrix (n x n, x major).
+void sf_smooth_kernel(float stdv, int n, std::vector<float>& k);
 // Gang shape for nshots shots of nstrips strips: CTAs per gang and gangs, so
 // that every gang of the grid is resident at once.
 int sf_gang_shape(sf_ctx* c, const void* kernel, size_t smem, int nshots, int nstrips, int gang_warps, int* G,

@@ -191,6 +191,26 @@ class Engine:
                                                     p, mem, _stream_ptr(stream)), "sf_batch_misfit_gradient")
         return (mis.value if want_misfit else None), out
 
+    # ------------------------------------------------------- model update
+    def smooth_model(self, field, stdv, samples, out=None, stream=None):
+        """The reference's Gaussian model smoothing of an (nx, nz) field."""
+        if out is None:
+            out = np.zeros((self.nx, self.nz), np.float32)
+        pi, mem, k1 = _ptr(field)
+        po, _, k2 = _ptr(out)
+        self._check(self.L.sf_smooth_model(self._ctx, pi, po, float(stdv), int(samples), mem, _stream_ptr(stream)),
+                    "sf_smooth_model")
+        return out
+
+    def update_slowness(self, grad, scale, stdv=0.0, samples=0, want_dS=True, stream=None):
+        """S += smooth(scale * grad) on the model interior; returns dS (nx, nz)."""
+        pg, gmem, k1 = _ptr(grad)
+        dS = np.zeros((self.nx, self.nz), np.float32) if want_dS else None
+        pd = C.c_void_p(dS.ctypes.data) if want_dS else None
+        self._check(self.L.sf_update_slowness(self._ctx, pg, gmem, float(scale), float(stdv), int(samples), pd,
+                                              0, _stream_ptr(stream)), "sf_update_slowness")
+        return dS
+
     # -------------------------------------------------------- planned batches
     def plan_batch(self, shots, rx, rz, stream=None):
         """Fix an isotropic batch (shots as for batch_forward) for

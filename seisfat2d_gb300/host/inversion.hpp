@@ -36,9 +36,7 @@ protected:
     virtual void set_modeling_type() = 0;
     virtual void export_estimated_models() = 0;
 
-    void model_smoothing(float* model);                                 // inversion.cpp:347-383
-    void smooth_matrix(float* input, float* output, int nx, int nz);   // inversion.cpp:385-447
-    double misfit_of(const float* S_padded);                           // one forward, picks only
+    double misfit_of_current();  // one forward of the engine's current model, picks only
 
 public:
     bool converged = false;

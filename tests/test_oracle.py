@@ -264,3 +264,28 @@ def test_threaded_batch_gradient_matches_per_shot_path(oracle):
     assert np.array_equal(g, g2)
     r = pg.astype(np.float64)
     assert J == pytest.approx(0.5 * np.nansum(r * r), rel=1e-13)
+
+
+def test_smoothing_kernel_and_update(oracle):
+    """Restated model_smoothing / smooth_matrix (inversion.cpp:347-447): the
+    normalised kernel sums to 1 and is symmetric, a unit impulse spreads into
+    the kernel, stdv 0 is the identity, and the update without smoothing is
+    S += scale * grad on the interior only."""
+    k = oracle.smooth_kernel(5.0, 11)
+    assert abs(float(k.sum(dtype=np.float64)) - 1.0) < 1e-5
+    assert np.array_equal(k, k.T) and np.array_equal(k, k[::-1, ::-1])
+    m = np.zeros((30, 20), np.float32)
+    m[12, 9] = 1.0
+    s = oracle.model_smoothing(m, 5.0, 11)
+    assert np.array_equal(s[7:18, 4:15], k)
+    r = np.random.default_rng(1).standard_normal((17, 13)).astype(np.float32)
+    assert np.array_equal(oracle.model_smoothing(r, 0.0, 7), r)
+    nx, nz, nb = 12, 9, 3
+    S = np.random.default_rng(2).uniform(2e-4, 6e-4, (nx + 2 * nb, nz + 2 * nb)).astype(np.float32)
+    g = np.random.default_rng(3).standard_normal(S.shape).astype(np.float32)
+    Sn, dS = oracle.update_slowness(S, g, nx, nz, -1e-5)
+    inner = (slice(nb, nb + nx), slice(nb, nb + nz))
+    assert np.array_equal(dS, (np.float32(-1e-5) * g[inner]).astype(np.float32))
+    assert np.array_equal(Sn[inner], (S[inner] + dS).astype(np.float32))
+    Sn[inner] = S[inner]
+    assert np.array_equal(Sn, S)  # the pad ring keeps its values
