@@ -1,28 +1,31 @@
-// Strip-systolic fast sweeping on one CTA (GB300, sm_103a).
+// Strip-systolic fast sweeping (GB300, sm_103a).
 //
-// One CTA owns one shot window of nzz rows x ncols columns. The rows are cut
-// into 32-row strips; a warp sweeps a strip with lane l owning one row and
-// marching across the columns, lane l running l steps behind lane 0. At step s
-// lane l updates node (row(l), column of march index s-l), so the three upwind
-// values of the reference update (modeling.cu:324-326) are: the lane above's
-// result of the previous step (shfl), the lane's own previous result, and the
-// lane's own previous upwind value. Consecutive strips are chained through
+// A shot window of nzz rows x ncols columns is cut into 32-row strips; a warp
+// sweeps a strip with lane l owning one row and marching across the columns,
+// lane l running l steps behind lane 0. At step s lane l updates node (row(l),
+// column of march index s-l), so the three upwind values of the reference
+// update (modeling.cu:324-326) are: the lane above's result of the previous
+// step (shfl), the lane's own previous result, and the lane's own previous
+// upwind value. Consecutive strips (usually on other SMs) are chained through
 // global memory without fences: the last lane of strip p writes each value of
 // its row together with a tag (launch epoch and shot number) as one 64-bit
-// store; lane 0 of strip p+1 (usually on another SM) prefetches the pair
-// through the same cp.async pipeline as its own columns and checks the tag.
-// A stale pair (the producer has not got there yet) sends lane 0 into a
-// bounded spin on the pair itself, after which it waits kLook+4 columns
-// further ahead so later prefetches find their data. Producers never wait on
-// consumers, so every wait points to a lower strip and the schedule cannot
-// deadlock however strips are spread over warps and CTAs.
+// store; lane 0 of strip p+1 prefetches the pair through the same cp.async
+// pipeline as its own columns and checks the tag. A stale pair (the producer
+// has not got there yet) sends lane 0 into a bounded spin on the pair itself,
+// after which it waits until the producer is kAhead columns further on, so
+// later prefetches find their data. Producers never wait on consumers, so
+// every wait points to a lower strip and the schedule cannot deadlock however
+// strips are spread over warps and CTAs.
 //
-// Column chunks are staged into a per-warp shared-memory ring by cp.async:
-// at step s the warp fetches march column s+LOOK (32 consecutive rows = one
-// coalesced 128-byte request per field), and lane l reads its own row of
-// column s-l from the ring. With a slot pitch of 32 (T) and 34 (S) floats both
-// the coalesced fill and the skewed read are bank-conflict free. Finished
-// columns go back to global memory through the same ring, coalesced.
+// Column chunks are staged into a per-warp shared-memory ring by cp.async,
+// kLook march columns ahead (32 consecutive rows = one coalesced 128-byte
+// request per field), and lane l reads its own row of column s-l from the
+// ring. With slot pitches of 32 (T) and 36 (S, with the halo row and the
+// handoff pair) floats both the coalesced fill and the skewed read are
+// bank-conflict free. Finished columns go back to global memory through the
+// same ring, coalesced. The march runs in blocks of kU steps: one wait for
+// the staged columns per block, the block's ring reads, its kU node updates
+// (the only serial chain), then its stores.
 //
 // Any order of node updates that respects the sweep's dependency DAG gives the
 // same bits as the reference's anti-diagonal launches, so this schedule is a
