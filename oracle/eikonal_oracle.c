@@ -869,12 +869,13 @@ void orc_solve_tape_f64(int nzz, int ncols, const float* S, int ldS, double dx, 
             int j = (sx > 0) ? jj : ncols - 1 - jj;                                             \
             for (int ii = nzz - 1; ii >= 0; ii--) {                                             \
                 int i = (sz > 0) ? ii : nzz - 1 - ii;                                           \
-                REAL mu = lam[(size_t)i + (size_t)j * nzz];                                     \
                 int id = i + sz, jd = j + sx;                                                   \
-                if (id >= 0 && id < nzz) mu = mu + pv[(size_t)id + (size_t)j * nzz];            \
-                if (jd >= 0 && jd < ncols) mu = mu + pe[(size_t)i + (size_t)jd * nzz];          \
-                if (id >= 0 && id < nzz && jd >= 0 && jd < ncols)                               \
-                    mu = mu + pev[(size_t)id + (size_t)jd * nzz];                               \
+                int iok = id >= 0 && id < nzz, jok = jd >= 0 && jd < ncols;                     \
+                REAL tpv = iok ? pv[(size_t)id + (size_t)j * nzz] : (REAL)0;                    \
+                REAL tpev = (iok && jok) ? pev[(size_t)id + (size_t)jd * nzz] : (REAL)0;        \
+                REAL tpe = jok ? pe[(size_t)i + (size_t)jd * nzz] : (REAL)0;                    \
+                /* the upwind row's two pushes are summed first (one value per row) */         \
+                REAL mu = (lam[(size_t)i + (size_t)j * nzz] + (tpv + tpev)) + tpe;              \
                 int cd = code[TP(s, i, j)];                                                     \
                 int br = cd & 7;                                                                \
                 size_t here = (size_t)i + (size_t)j * nzz;                                      \

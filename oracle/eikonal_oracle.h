@@ -119,7 +119,9 @@ void orc_solve_tape_f64(int nzz, int ncols, const float* S, int ldS, double dx, 
 /* Reverse sweeps over a tape. lam: adjoint of the final T (nzz x ncols), in
  * place; on return it holds the adjoint of the initial field. grad (nzz x
  * ncols, column stride nzz) receives += dJ/dS for the window, including the
- * 3x3 initialisation term (dist[9] = node distances). */
+ * 3x3 initialisation term (dist[9] = node distances). Per node of a sweep
+ * with signs (sz, sx): mu = (lam + (pv(i+sz, j) + pev(i+sz, j+sx))) +
+ * pe(i, j+sx), missing neighbours contributing 0. */
 void orc_adjoint_f32(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* code,
                      const float* c1, const float* c2, const float dist[9], float* lam, float* grad);
 void orc_adjoint_f64(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* code,

@@ -6,15 +6,16 @@
 // include/seisfat2d.h). The discrete adjoint of one sweep is then the linear
 // recurrence, in pull form, for node n = (i, j) of a sweep with signs (sz, sx):
 //
-//   mu(n)  = ((lam(n) + pv(i+sz, j)) + pe(i, j+sx)) + pev(i+sz, j+sx)
+//   mu(n)  = (lam(n) + (pv(i+sz, j) + pev(i+sz, j+sx))) + pe(i, j+sx)
 //   lam(n) <- mu(n) if the node kept its value (code 0), else 0
 //   pv/pe/pev(n) = mu(n) * dT(n)/d{tv, te, tev}   (pushed to the upwind nodes)
 //   v(n)   = mu(n) * c2                           (term of the node's slowness cell)
 //
 // swept in the reverse order. It is the forward's dependency pattern with the
 // march reversed, so the same strip-systolic schedule runs it: lane l owns a
-// row, the lane above supplies pv/pev of the previous step by shfl, the lane's
-// own previous pe is kept in a register. The tape was written in the forward
+// row, the lane above supplies the sum of its pv of the previous step and its
+// pev of the step before by one shfl (the two pushes of the upwind row are
+// summed by their sender), the lane's own previous pe is kept in a register. The tape was written in the forward
 // strip's skewed step order, which makes the reverse read of one step 32
 // consecutive entries (lane l of the reverse march is lane 31-l of the
 // forward one).
@@ -105,7 +106,7 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     float* pV = a.tc2 + fs0 + flane;
     float* pW = lamg + (size_t)r + (long long)col_of(0) * (long long)nzz;
 
-    float my_pv = 0.0f, my_pe = 0.0f, my_pev = 0.0f, pev_hold = 0.0f;
+    float my_x = 0.0f, my_pe = 0.0f, my_pev = 0.0f, pev_hold = 0.0f;
     int b0 = 0, tb0 = 0;  // ring slots of march s0 (lambda, tape)
 
     // Blocks of kU steps, as in the forward: one wait per block, the block's
@@ -167,15 +168,15 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
             const int s = s0 + u;
             const int m = s - lane;
             const bool act = vrow && (m >= 0) && (m < ncols);
-            float pv_in = __shfl_up_sync(0xffffffffu, my_pv, 1);
-            float pev_in = __shfl_up_sync(0xffffffffu, my_pev, 1);
+            // pv of the upwind row's node in this column plus pev of its node in
+            // the previous column, summed by the lane above
+            float x_in = __shfl_up_sync(0xffffffffu, my_x, 1);
             if (lane == 0) {  // upwind row of the strip: the previous strip, or outside the grid
                 const bool have = consumer && s < ncols;
-                pv_in = have ? val_of(e0[u]) : 0.0f;
-                pev_in = have ? val_of(e1[u]) : 0.0f;
+                x_in = fadd(have ? val_of(e0[u]) : 0.0f, pev_hold);
+                pev_hold = have ? val_of(e1[u]) : 0.0f;
             }
-            const float mu = fadd(fadd(fadd(lam_in[u], pv_in), my_pe), pev_hold);
-            pev_hold = pev_in;
+            const float mu = fadd(fadd(lam_in[u], x_in), my_pe);
             float npv = 0.0f, npe = 0.0f, npev = 0.0f, l = mu, v = 0.0f;
             const int br = code[u] & 7;
             if (act && br != 0) {
@@ -195,7 +196,7 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
             opv[u] = npv;
             opev[u] = npev;
             actv[u] = act;
-            my_pv = npv;
+            my_x = fadd(npv, my_pev);  // this node's pv + the previous node's pev
             my_pe = npe;
             my_pev = npev;
         }
