@@ -26,7 +26,12 @@
 namespace sf {
 
 constexpr int kLP = 36;    // lambda slot pitch: 32 rows, then the {pv,tag},{pev,tag} handoff pairs
-constexpr int kTR = 16;    // tape ring slots (a multiple of kU, > kLook + kU)
+// The reverse sweeps stage 4 columns ahead (one block): their tape rows come
+// from DRAM, but a shorter lead keeps consecutive strips closer together,
+// which measured faster than 8 or 12.
+constexpr int kLookA = 4;
+constexpr int kAheadA = kLookA + 2 * kU;  // a consumer's fall-back distance after a stall
+constexpr int kTR = 12;    // tape ring slots (a multiple of kU, > kLookA + kU)
 constexpr int kTPitch = 72;  // c1[32], c2[32], code bytes (8 words)
 
 struct AdjRing {
@@ -95,11 +100,11 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         pTc -= 32;
     };
 
-    // let the previous strip get kAhead columns ahead before the first prefetches
-    if (consumer) wait_pair(a.h_in + 2 * (size_t)min(kAhead, ncols - 1) + 1, a.tag, sh, a.err);
+    // let the previous strip get kAheadA columns ahead before the first prefetches
+    if (consumer) wait_pair(a.h_in + 2 * (size_t)min(kAheadA, ncols - 1) + 1, a.tag, sh, a.err);
     __syncwarp();
 #pragma unroll 1
-    for (int q = 0; q < kLook; q++) prefetch(q, q, q % kTR);
+    for (int q = 0; q < kLookA; q++) prefetch(q, q, q % kTR);
 
     // running destinations: the term v of forward tape step ncols+30-s, and
     // the write-back of march column s-31 (row r)
@@ -114,14 +119,14 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
 #pragma unroll 1
     for (int s0 = 0; s0 < nsteps; s0 += kU) {
         {
-            int pf0 = b0 + kLook;
+            int pf0 = b0 + kLookA;
             if (pf0 >= kRing) pf0 -= kRing;
-            int tf0 = tb0 + kLook;
+            int tf0 = tb0 + kLookA;
             if (tf0 >= kTR) tf0 -= kTR;
 #pragma unroll
-            for (int u = 0; u < kU; u++) prefetch(s0 + kLook + u, pf0 + u, tf0 + u);
+            for (int u = 0; u < kU; u++) prefetch(s0 + kLookA + u, pf0 + u, tf0 + u);
         }
-        cp_wait<kLook>();
+        cp_wait<kLookA>();
         __syncwarp();
 
         int ml = b0 - lane;  // slot of march s0 - lane
@@ -149,14 +154,14 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         }
         if (consumer) {
             // pairs the previous strip had not written when they were prefetched:
-            // wait for them, then fall kAhead columns behind so later prefetches hit
+            // wait for them, then fall kAheadA columns behind so later prefetches hit
 #pragma unroll
             for (int u = 0; u < kU; u++) {
                 const int s = s0 + u;
                 if (s < ncols && (tag_of(e0[u]) != a.tag || tag_of(e1[u]) != a.tag)) {
                     e0[u] = pack_tag(wait_pair(a.h_in + 2 * (size_t)s, a.tag, sh, a.err), a.tag);
                     e1[u] = pack_tag(wait_pair(a.h_in + 2 * (size_t)s + 1, a.tag, sh, a.err), a.tag);
-                    wait_pair(a.h_in + 2 * (size_t)min(s + kAhead, ncols - 1) + 1, a.tag, sh, a.err);
+                    wait_pair(a.h_in + 2 * (size_t)min(s + kAheadA, ncols - 1) + 1, a.tag, sh, a.err);
                 }
             }
         }

@@ -12,19 +12,19 @@
 // store; lane 0 of strip p+1 prefetches the pair through the same cp.async
 // pipeline as its own columns and checks the tag. A stale pair (the producer
 // has not got there yet) sends lane 0 into a bounded spin on the pair itself,
-// after which it waits until the producer is kAhead columns further on, so
+// after which it waits until the producer is some columns further on, so
 // later prefetches find their data. Producers never wait on consumers, so
 // every wait points to a lower strip and the schedule cannot deadlock however
 // strips are spread over warps and CTAs.
 //
 // Column chunks are staged into a per-warp shared-memory ring by cp.async,
-// kLook march columns ahead (32 consecutive rows = one coalesced 128-byte
+// a few march columns ahead (32 consecutive rows = one coalesced 128-byte
 // request per field), and lane l reads its own row of column s-l from the
 // ring. With slot pitches of 32 (T) and 36 (S, with the halo row and the
 // handoff pair) floats both the coalesced fill and the skewed read are
 // bank-conflict free. Finished columns go back to global memory through the
-// same ring, coalesced. The march runs in blocks of kU steps: one wait for
-// the staged columns per block, the block's ring reads, its kU node updates
+// same ring, coalesced. The march runs in blocks of a few steps: one wait for
+// the staged columns per block, the block's ring reads, its node updates
 // (the only serial chain), then its stores.
 //
 // Any order of node updates that respects the sweep's dependency DAG gives the
@@ -37,10 +37,21 @@
 
 namespace sf {
 
-constexpr int kU = 4;       // march steps per block of the strip loop
-constexpr int kLook = 8;    // prefetch distance in march columns (a multiple of kU)
-constexpr int kRing = 48;   // column slots per warp ring (a multiple of kU, >= 32 + kLook + kU)
-constexpr int kAhead = kLook + 2 * kU;  // columns a consumer lets its producer get ahead after a stall
+constexpr int kU = 4;       // march steps per block of the reverse sweeps' strip loop
+constexpr int kRing = 48;   // column slots per warp ring (a multiple of every block size, >= 32 + lead + block)
+
+// Block size and staging lead (march columns, a multiple of the block) of a
+// forward strip loop: 4 and 8 for the plain solve; 2 and 4 for the taped one,
+// which keeps a tape record per step of the block in registers (measured
+// 19% faster than 4 and 8 there). After a stall a consumer lets its producer
+// get lead + block columns ahead.
+template <bool TAPE>
+struct FwdBlock {
+    static constexpr int U = TAPE ? 2 : 4;
+    static constexpr int LOOK = TAPE ? 4 : 8;
+    static constexpr int AHEAD = LOOK + U;
+    static_assert(LOOK % U == 0 && kRing % U == 0 && kRing >= 32 + LOOK + U, "ring too small");
+};
 constexpr int kSP = 36;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff pair at 34..35
 constexpr int kTP = 32;     // T slot pitch
 constexpr int kMaxWarps = 16;
@@ -185,6 +196,7 @@ __device__ __forceinline__ unsigned wait_counter(const unsigned* p, unsigned tar
 template <int SZ, int SX, bool SW0, bool TAPE, bool REF>
 __device__ __forceinline__ void run_strip(const StripArgs& a)
 {
+    constexpr int kU = FwdBlock<TAPE>::U, kLook = FwdBlock<TAPE>::LOOK, kAhead = FwdBlock<TAPE>::AHEAD;
     const int lane = threadIdx.x & 31;
     const int nzz = a.nzz, ncols = a.ncols;
     const int rb = 32 * a.k;
