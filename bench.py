@@ -391,7 +391,10 @@ def run_ours(a):
     h2d = model.nbytes + len(shots) * 16 + w.rx.nbytes + w.rz.nbytes + (host_obs.nbytes if fa else 0)
     d2h = host_picks.nbytes + (host_grad.nbytes + 8 if fa else 0)
 
-    # --- plain: one shot at a time, spread over the batch
+    # --- plain: one shot at a time, spread over the batch, with the engine's
+    # default launch shape (the autotuned one belongs to the batch)
+    launch_used = eng.get_launch()
+    eng.set_launch(1, 0)
     nplain = max(1, min(a.nplain, len(shots)))
     sel = [shots[q * len(shots) // nplain] for q in range(nplain)]
     Tdev = torch.empty((eng.nxx, eng.nzz), dtype=torch.float32, device=dev)
@@ -463,7 +466,7 @@ def run_ours(a):
                             if fa else ("VTI forward (2 solves + qP pass) + picks" if ani else "forward + picks")),
                    "parallelism": f"shots sharded over {world} GPU(s)",
                    "l2": "flushed between timed steps (512 MB write)",
-                   "launch": {"warps_per_cta": eng.get_launch()[0], "warps_per_shot": eng.get_launch()[1] or "auto",
+                   "launch": {"warps_per_cta": launch_used[0], "warps_per_shot": launch_used[1] or "auto",
                               "chosen_by": "sf_plan_autotune" if tuned else ("flags" if (a.warps or a.gang) else
                                                                              "default")},
                    "timed_path": ("sf_plan_graph_launch (CUDA graph of the planned iteration)" if fa
