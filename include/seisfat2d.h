@@ -225,6 +225,31 @@ int sf_smooth_model(sf_ctx* ctx, const float* in, float* out, float stdv, int sa
 int sf_update_slowness(sf_ctx* ctx, const float* grad, int grad_mem, float scale, float stdv, int samples,
                        float* dS, int dS_mem, void* stream);
 
+/* ---- Kirchhoff depth migration, image domain (src/migration/KDM.cu:3-55,
+ * IDKDM.cu:19-22, migration.cu:54-71, :173-228, :398-483) ----
+ *
+ * sf_adjoint_convolution: Migration::adjoint_convolution of ntr traces of nt
+ * samples (trace-major, host or device per `mem`): cross-correlation with the
+ * reference's wavelet for max_frequency fmax (Migration::set_wavelet), as
+ * its FFTW product A*conj(B) and unnormalised inverse give it (scaled by the
+ * FFT length), shifted by nw/2 + nw/10 samples; earlier samples are 0.
+ * Computed directly in FP64 and rounded once to FP32.
+ *
+ * sf_kirchhoff_image: the image (nz x nx, z fastest; host or device per
+ * image_mem) = sum over sources s and receivers r with |xsrc[s] - xrec[r]| <
+ * max_offset, in that order, of the reference's image-domain weight times
+ * the correlated trace sample at t = Ts + Tr (data: nsrc x nrec x nt, host or
+ * device per data_mem). Ts and Tr are device arrays of nsrc and nrec padded
+ * traveltime tables (nzz x nxx each, as sf_batch_table writes them); the
+ * context's slowness is the model. The reference sums the traces with one
+ * launch and one atomicAdd per trace; this is one launch that sums each
+ * cell's terms in the same order. Host outputs synchronise `stream`. */
+int sf_adjoint_convolution(sf_ctx* ctx, const float* traces, float* out, int ntr, int nt, float dt, float fmax,
+                           int mem, void* stream);
+int sf_kirchhoff_image(sf_ctx* ctx, const float* Ts, const float* Tr, int nsrc, int nrec, const float* xsrc,
+                       const float* xrec, const float* data, int data_mem, int nt, float dt, float aperture,
+                       float max_offset, float* image, int image_mem, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

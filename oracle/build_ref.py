@@ -2,10 +2,11 @@
 
 Compiles the kernels of phbastosa/SeisFAT2D's modeling path -- time_set,
 time_init, inner_sweep (src/modeling/modeling.cu) and get_quasi_slowness
-(src/modeling/eikonal_ani.cu) -- from the reference sources where they lie,
+(src/modeling/eikonal_ani.cu) -- and its Kirchhoff imaging kernels
+(src/migration/migration.cu) from the reference sources where they lie,
 into ``oracle/_ref/*.cubin`` (device code only, sm_103a). The reference
-includes <fftw3.h> unconditionally (src/admin/admin.hpp:10) although the
-modeling path never calls FFTW, which is not installed: an empty stub header
+includes <fftw3.h> unconditionally (src/admin/admin.hpp:10); FFTW is not
+installed and no device code calls it, so a stub header of declarations
 generated under ``oracle/_ref/stub`` satisfies the include.
 
 Differences from the reference's own build line (run/program.sh:51): device
@@ -23,7 +24,21 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.environ.get("SF_REFERENCE_ROOT", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 BUILD = os.path.join(HERE, "_build")
-CUBINS = {"modeling": "src/modeling/modeling.cu", "eikonal_ani": "src/modeling/eikonal_ani.cu"}
+CUBINS = {"modeling": "src/modeling/modeling.cu", "eikonal_ani": "src/modeling/eikonal_ani.cu",
+          "migration": "src/migration/migration.cu"}
+# Declarations of the FFTW3 interface the reference's host code names
+# (src/migration/migration.cu:173-261). Only the device code ends up in the
+# cubins, but the compiler parses the host code too.
+FFTW_STUB = """#pragma once
+#include <cstddef>
+typedef double fftw_complex[2];
+typedef struct fftw_plan_opaque* fftw_plan;
+#define FFTW_ESTIMATE (1U << 6)
+void* fftw_malloc(size_t n);
+fftw_plan fftw_plan_dft_r2c_1d(int n, double* in, fftw_complex* out, unsigned flags);
+fftw_plan fftw_plan_dft_c2r_1d(int n, fftw_complex* in, double* out, unsigned flags);
+void fftw_execute(const fftw_plan p);
+"""
 HARNESS_SRC = os.path.join(HERE, "ref_harness.cpp")
 HARNESS = os.path.join(BUILD, "libref_harness.so")
 
@@ -37,7 +52,8 @@ def build_cubins():
         return False
     stub = os.path.join(OUT, "stub")
     os.makedirs(stub, exist_ok=True)
-    open(os.path.join(stub, "fftw3.h"), "w").close()
+    with open(os.path.join(stub, "fftw3.h"), "w") as f:
+        f.write(FFTW_STUB)
     for name, rel in CUBINS.items():
         src = os.path.join(REF, rel)
         out = cubin_path(name)

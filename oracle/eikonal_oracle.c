@@ -5,6 +5,7 @@
  */
 #include "eikonal_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1082,4 +1083,118 @@ void orc_update_slowness(float* S, const float* grad, int nx, int nz, int nb, fl
     for (int j = 0; j < nx; j++)
         for (int i = 0; i < nz; i++) S[(i + nb) + (size_t)(j + nb) * nzz] += dS[i + (size_t)j * nz];
     free(d);
+}
+
+/* ------------------------------------------------------------- Kirchhoff */
+
+/* Migration::set_wavelet (src/migration/migration.cu:54-71) as written: the
+ * offsets and the centre frequency in float, the phase term in double, expf
+ * of it rounded to float. Returns nw; w must hold it (nw <= wmax). */
+int orc_kirchhoff_wavelet(float fmax, float dt, float* w, int wmax)
+{
+    float t0 = 2.0f * sqrtf((float)ORC_PI) / fmax;
+    float fc = fmax / (3.0f * sqrtf((float)ORC_PI));
+    int nw = 2 * ((int)((t0 - 0.5f * dt) / dt));
+    if (nw > wmax) return -nw;
+    for (int k = 0; k < nw; k++) {
+        float td = k * dt - t0;
+        float arg = (float)(ORC_PI * ORC_PI * ORC_PI * fc * fc * td * td);
+        w[k] = (1.0f - 2.0f * arg) * expf(-arg);
+    }
+    return nw;
+}
+
+/* Migration::adjoint_convolution (migration.cu:197-228) without the FFT: the
+ * product A conj(B) of the zero-padded spectra and FFTW's unnormalised
+ * inverse are the linear cross-correlation times nfft (nfft >= nt + nw - 1),
+ * summed here directly in FP64; out[t] for t >= nw/2 + nw/10, else 0. */
+void orc_adjoint_convolution(const float* in, float* out, int ntr, int nt, const float* w, int nw)
+{
+    int nfft = 1;
+    while (nfft < nt + nw - 1) nfft <<= 1;
+    int shift = nw / 2 + nw / 10;
+    for (int q = 0; q < ntr; q++) {
+        const float* a = in + (size_t)q * nt;
+        float* o = out + (size_t)q * nt;
+        for (int t = 0; t < nt; t++) {
+            if (t < shift) {
+                o[t] = 0.0f;
+                continue;
+            }
+            int l = t - shift;
+            double acc = 0.0;
+            for (int m = 0; m < nw && l + m < nt; m++) acc += (double)a[l + m] * (double)w[m];
+            o[t] = (float)(acc * (double)nfft);
+        }
+    }
+}
+
+/* The reference accumulates with a float atomicAdd, which flushes subnormal
+ * operands and results to zero (sign kept). */
+static float ftz(float x) { return fabsf(x) < FLT_MIN ? copysignf(0.0f, x) : x; }
+
+/* KDM::kirchhoff_depth_migration + image_domain_adjoint_kernel
+ * (KDM.cu:3-55, migration.cu:398-483): for every source, every receiver
+ * within max_offset (in that order), every model cell with T = Ts + Tr below
+ * nt*dt: image += weight * trace[floor(T/dt)], FP32, the kernel's formulas
+ * with libm functions (the GPU uses CUDA's; agreement is to rounding). */
+void orc_kirchhoff_image(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr, int nsrc,
+                         int nrec, const float* xsrc, const float* xrec, const float* data, int nt, float dt,
+                         float dx, float dz, float aperture, float max_offset, float* image)
+{
+    const float EPSK = 1e-6f;
+    size_t matsize = (size_t)nxx * nzz;
+    int nz = nzz - 2 * nb, nx = nxx - 2 * nb;
+    for (size_t q = 0; q < (size_t)nx * nz; q++) image[q] = 0.0f;
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            float offset = fabsf(xsrc[s] - xrec[r]);
+            if (!(offset < max_offset)) continue;
+            float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            const float* ts = Ts + matsize * s;
+            const float* tr = Tr + matsize * r;
+            const float* trace = data + ((size_t)s * nrec + r) * nt;
+            for (int j = nb; j < nxx - nb; j++)
+                for (int i = nb; i < nzz - nb; i++) {
+                    size_t index = (size_t)i + (size_t)j * nzz;
+                    float z = (float)(i - nb) * dz, x = (float)(j - nb) * dx;
+                    float T = ts[index] + tr[index];
+                    int tId = (int)floorf(T / dt);
+                    if (tId >= nt) continue;
+#define ORC_D(A)                                                                                      \
+    float A##_dz = 0.5f * (A[(i + 1) + j * nzz] - A[(i - 1) + j * nzz]) / dz;                        \
+    float A##_dx = 0.5f * (A[i + (j + 1) * nzz] - A[i + (j - 1) * nzz]) / dx;                        \
+    float A##_dz2 = (A[(i + 1) + j * nzz] - 2.0f * A[i + j * nzz] + A[(i - 1) + j * nzz]) / (dz * dz); \
+    float A##_dx2 = (A[i + (j + 1) * nzz] - 2.0f * A[i + j * nzz] + A[i + (j - 1) * nzz]) / (dx * dx); \
+    float A##_dxdz = (A[(i + 1) + (j + 1) * nzz] - A[(i - 1) + (j + 1) * nzz] - A[(i + 1) + (j - 1) * nzz] + \
+                      A[(i - 1) + (j - 1) * nzz]) / (4.0f * dx * dz);
+                    ORC_D(ts)
+                    ORC_D(tr)
+#undef ORC_D
+                    float norm_s = sqrtf(ts_dx * ts_dx + ts_dz * ts_dz) + EPSK;
+                    float norm_r = sqrtf(tr_dx * tr_dx + tr_dz * tr_dz) + EPSK;
+                    float detHs = fabsf(ts_dx2 * ts_dz2 - ts_dxdz * ts_dxdz) + EPSK;
+                    float detHr = fabsf(tr_dx2 * tr_dz2 - tr_dxdz * tr_dxdz) + EPSK;
+                    float Jterm = sqrtf(detHs * detHr) * S[index] / (norm_s * norm_r);
+                    float ux_s = ts_dx / norm_s, uz_s = ts_dz / norm_s;
+                    float ux_r = tr_dx / norm_r, uz_r = tr_dz / norm_r;
+                    float nxn = 0.0f, nzn = -1.0f;
+                    float cos_s = fabsf(ux_s * nxn + uz_s * nzn);
+                    float cos_r = fabsf(ux_r * nxn + uz_r * nzn);
+                    float obl = sqrtf(fmaxf(0.0f, cos_s) * fmaxf(0.0f, cos_r));
+                    float R_s = fmaxf(ts[index] / S[index], EPSK);
+                    float R_r = fmaxf(tr[index] / S[index], EPSK);
+                    float G = 1.0f / sqrtf(R_s * R_r);
+                    float th_s = acosf(fminf(1.0f, fmaxf(-1.0f, ux_s * nxn + uz_s * nzn)));
+                    float th_r = acosf(fminf(1.0f, fmaxf(-1.0f, ux_r * nxn + uz_r * nzn)));
+                    float R = 1.0f + 0.2f * cosf(0.5f * (th_s + th_r));
+                    float scale_const = (float)(1.0f / (2.0f * ORC_PI));
+                    float sigma = tanf((float)(aperture * ORC_PI / 180.0f)) * z;
+                    float u = (x - cmp) / (sigma + EPSK);
+                    float taper = expf(-0.5f * u * u);
+                    float wgt = scale_const * Jterm * obl * G * R * taper;
+                    size_t mId = (size_t)(i - nb) + (size_t)(j - nb) * nz;
+                    image[mId] = ftz(ftz(image[mId]) + ftz(wgt * trace[tId]));
+                }
+        }
 }

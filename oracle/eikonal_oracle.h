@@ -158,6 +158,16 @@ void orc_model_smoothing(const float* model, int nx, int nz, float stdv, int sam
 void orc_update_slowness(float* S, const float* grad, int nx, int nz, int nb, float scale, float stdv,
                          int samples, float* dS);
 
+/* Kirchhoff image-domain migration (src/migration/migration.cu:54-71,
+ * :197-228, :398-483, KDM.cu:3-55): the wavelet (returns its length, or
+ * minus it when wmax is too small), the trace cross-correlation, and the
+ * image (nz x nx) from padded tables Ts (nsrc) and Tr (nrec). */
+int orc_kirchhoff_wavelet(float fmax, float dt, float* w, int wmax);
+void orc_adjoint_convolution(const float* in, float* out, int ntr, int nt, const float* w, int nw);
+void orc_kirchhoff_image(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr, int nsrc,
+                         int nrec, const float* xsrc, const float* xrec, const float* data, int nt, float dt,
+                         float dx, float dz, float aperture, float max_offset, float* image);
+
 /* Arithmetic of the FP32 solvers: 0 = every operation rounded once and the
  * 3x3 initialisation in FP64 (default); 1 = the reference build's arithmetic:
  * FP32 initialisation and fused multiply-adds where nvcc forms them in

@@ -77,6 +77,12 @@ def lib():
         L.orc_batch_gradient_f32.restype = C.c_int
         L.orc_smooth_kernel.argtypes = [C.c_float, C.c_int, f32p]
         L.orc_model_smoothing.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_int, f32p]
+        L.orc_kirchhoff_wavelet.argtypes = [C.c_float, C.c_float, f32p, C.c_int]
+        L.orc_kirchhoff_wavelet.restype = C.c_int
+        L.orc_adjoint_convolution.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p, C.c_int]
+        L.orc_kirchhoff_image.argtypes = [C.c_int, C.c_int, C.c_int, f32p, f32p, f32p, C.c_int, C.c_int, f32p,
+                                          f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                          C.c_float, f32p]
         L.orc_update_slowness.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
                                           f32p]
         _lib = L
@@ -301,6 +307,36 @@ def update_slowness(S, grad, nx, nz, scale, stdv=0.0, samples=0, nb=3):
     dS = np.zeros((nx, nz), np.float32)
     lib().orc_update_slowness(Sn, _f32(grad), nx, nz, nb, scale, stdv, samples, dS)
     return Sn, dS
+
+
+def kirchhoff_wavelet(fmax, dt):
+    w = np.zeros(1 << 16, np.float32)
+    nw = lib().orc_kirchhoff_wavelet(fmax, dt, w, len(w))
+    if nw < 0:
+        raise ValueError("wavelet too long")
+    return w[:nw].copy()
+
+
+def adjoint_convolution(traces, dt, fmax):
+    """Migration::adjoint_convolution of (ntr, nt) traces."""
+    a = _f32(traces)
+    w = kirchhoff_wavelet(fmax, dt)
+    out = np.zeros_like(a)
+    lib().orc_adjoint_convolution(a.ravel(), out.ravel(), a.shape[0], a.shape[1], w, len(w))
+    return out
+
+
+def kirchhoff_image(S, Ts, Tr, xsrc, xrec, data, dt, dx, dz, aperture, max_offset, nb=3):
+    """Image-domain Kirchhoff migration; S (nxx, nzz), Ts (nsrc, nxx, nzz),
+    Tr (nrec, nxx, nzz), data (nsrc, nrec, nt). Returns the (nx, nz) image."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    img = np.zeros((nxx - 2 * nb, nzz - 2 * nb), np.float32)
+    d = _f32(data)
+    lib().orc_kirchhoff_image(nxx, nzz, nb, S, _f32(Ts).ravel(), _f32(Tr).ravel(), len(xsrc), len(xrec),
+                              _f32(xsrc), _f32(xrec), d.ravel(), d.shape[-1], dt, dx, dz, aperture, max_offset,
+                              img)
+    return img
 
 
 def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):

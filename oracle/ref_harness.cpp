@@ -11,13 +11,15 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <vector>
 
 namespace {
-CUmodule g_mod = nullptr, g_ani = nullptr;
+CUmodule g_mod = nullptr, g_ani = nullptr, g_mig = nullptr;
+CUfunction f_img = nullptr;
 CUfunction f_set = nullptr, f_init = nullptr, f_sweep = nullptr, f_qs = nullptr;
 CUcontext g_ctx = nullptr;
 CUdevice g_dev = 0;
@@ -67,7 +69,8 @@ extern "C" int ref_close()
 {
     if (g_mod) cuModuleUnload(g_mod);
     if (g_ani) cuModuleUnload(g_ani);
-    g_mod = g_ani = nullptr;
+    if (g_mig) cuModuleUnload(g_mig);
+    g_mod = g_ani = g_mig = nullptr;
     if (g_ctx) cuDevicePrimaryCtxRelease(g_dev);
     g_ctx = nullptr;
     return 0;
@@ -214,5 +217,65 @@ extern "C" int ref_init(int nxx, int nzz, int nb, const float* S, float dx, floa
     DR(cuMemcpyDtoH(T_out, dT, sizeof(float) * matsize));
     cuMemFree(dT);
     cuMemFree(dS);
+    return 0;
+}
+
+// ---------------------------------------------------------------- Kirchhoff
+//
+// KDM::kirchhoff_depth_migration (src/migration/KDM.cu:3-55) with the image-
+// domain kernel (IDKDM::perform_adjoint, src/migration/IDKDM.cu:19-22): for
+// every source, for every receiver within max_offset, one launch of
+// image_domain_adjoint_kernel over the padded grid with that pair's tables and
+// (already correlated) trace, CMP = (sx + rx) / 2. Tables are padded nzz x nxx
+// fields, z fastest; data is nsrc x nrec x nt.
+extern "C" int ref_kirchhoff_open(const char* migration_cubin)
+{
+    if (!g_ctx) return -1;
+    DR(cuCtxSetCurrent(g_ctx));
+    if (!g_mig) {
+        DR(cuModuleLoad(&g_mig, migration_cubin));
+        const char* n_img[] = {"_Z27image_domain_adjoint_kernelPfS_S_S_S_fiffiiiff", nullptr};
+        DR(get_fn(g_mig, n_img, &f_img));
+    }
+    return 0;
+}
+
+extern "C" int ref_kirchhoff_adjoint(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr,
+                                     int nsrc, int nrec, const float* xsrc, const float* xrec, const float* data,
+                                     int nt, float dt, float dx, float dz, float aperture, float max_offset,
+                                     float* image)
+{
+    DR(cuCtxSetCurrent(g_ctx));
+    const size_t matsize = (size_t)nxx * nzz;
+    const int nx = nxx - 2 * nb, nz = nzz - 2 * nb;
+    CUdeviceptr dS, dTs, dTr, dd, dm;
+    DR(cuMemAlloc(&dS, sizeof(float) * matsize));
+    DR(cuMemAlloc(&dTs, sizeof(float) * matsize * nsrc));
+    DR(cuMemAlloc(&dTr, sizeof(float) * matsize * nrec));
+    DR(cuMemAlloc(&dd, sizeof(float) * (size_t)nsrc * nrec * nt));
+    DR(cuMemAlloc(&dm, sizeof(float) * (size_t)nx * nz));
+    DR(cuMemcpyHtoD(dS, S, sizeof(float) * matsize));
+    DR(cuMemcpyHtoD(dTs, Ts, sizeof(float) * matsize * nsrc));
+    DR(cuMemcpyHtoD(dTr, Tr, sizeof(float) * matsize * nrec));
+    DR(cuMemcpyHtoD(dd, data, sizeof(float) * (size_t)nsrc * nrec * nt));
+    DR(cuMemsetD32(dm, 0, (size_t)nx * nz));
+    const unsigned nblocks = (unsigned)((matsize + 255) / 256);
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            const float offset = fabsf(xsrc[s] - xrec[r]);
+            if (!(offset < max_offset)) continue;
+            float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            CUdeviceptr ts = dTs + sizeof(float) * matsize * s, tr = dTr + sizeof(float) * matsize * r;
+            CUdeviceptr tdat = dd + sizeof(float) * ((size_t)s * nrec + r) * nt;
+            void* args[] = {&dS, &ts, &tr, &tdat, &dm, &dt, &nt, &dx, &dz, &nxx, &nzz, &nb, &aperture, &cmp};
+            DR(cuLaunchKernel(f_img, nblocks, 1, 1, 256, 1, 1, 0, nullptr, args, nullptr));
+        }
+    DR(cuCtxSynchronize());
+    DR(cuMemcpyDtoH(image, dm, sizeof(float) * (size_t)nx * nz));
+    cuMemFree(dS);
+    cuMemFree(dTs);
+    cuMemFree(dTr);
+    cuMemFree(dd);
+    cuMemFree(dm);
     return 0;
 }

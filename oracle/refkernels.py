@@ -64,3 +64,32 @@ def init(S_padded, dx, dz, sx, sz, nb=3):
     if rc != 0:
         raise RuntimeError(f"ref_init failed ({rc})")
     return T
+
+
+def kirchhoff_adjoint(S_padded, Ts, Tr, xsrc, xrec, data, dt, dx, dz, aperture, max_offset, nb=3):
+    """The reference's IDKDM trace loop (KDM.cu:3-55) with its own
+    image_domain_adjoint_kernel on correlated traces data (nsrc, nrec, nt);
+    tables (n, nxx, nzz). Returns the (nx, nz) image."""
+    h = _handle()
+    if not getattr(h, "_kirch", False):
+        h.ref_kirchhoff_open.argtypes = [C.c_char_p]
+        h.ref_kirchhoff_adjoint.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_int] + \
+            [C.c_void_p] * 3 + [C.c_int] + [C.c_float] * 5 + [C.c_void_p]
+        rc = h.ref_kirchhoff_open(build_ref.cubin_path("migration").encode())
+        if rc != 0:
+            raise RuntimeError(f"ref_kirchhoff_open failed ({rc})")
+        h._kirch = True
+    S = np.ascontiguousarray(S_padded, np.float32)
+    nxx, nzz = S.shape
+    Ts = np.ascontiguousarray(Ts, np.float32)
+    Tr = np.ascontiguousarray(Tr, np.float32)
+    xs = np.ascontiguousarray(xsrc, np.float32)
+    xr = np.ascontiguousarray(xrec, np.float32)
+    d = np.ascontiguousarray(data, np.float32)
+    img = np.zeros((nxx - 2 * nb, nzz - 2 * nb), np.float32)
+    rc = h.ref_kirchhoff_adjoint(nxx, nzz, nb, S.ctypes.data, Ts.ctypes.data, Tr.ctypes.data, len(xs), len(xr),
+                                 xs.ctypes.data, xr.ctypes.data, d.ctypes.data, d.shape[-1], dt, dx, dz, aperture,
+                                 max_offset, img.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"ref_kirchhoff_adjoint failed ({rc})")
+    return img

@@ -67,6 +67,9 @@ SIGNATURES = {
     "sf_kernel_times": (C.c_int, [VP, FP, C.c_int]),
     "sf_smooth_model": (C.c_int, [VP, VP, VP, C.c_float, C.c_int, C.c_int, VP]),
     "sf_update_slowness": (C.c_int, [VP, VP, C.c_int, C.c_float, C.c_float, C.c_int, VP, C.c_int, VP]),
+    "sf_adjoint_convolution": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, VP]),
+    "sf_kirchhoff_image": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP, VP, VP, C.c_int, C.c_int, C.c_float,
+                                     C.c_float, C.c_float, VP, C.c_int, VP]),
 }
 
 _lib = None

@@ -20,7 +20,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-O2",
 ]
-UNITS = ["sf_engine.cu", "sf_adjoint.cu", "sf_plan.cu", "sf_update.cu"]
+UNITS = ["sf_engine.cu", "sf_adjoint.cu", "sf_plan.cu", "sf_update.cu", "sf_migration.cu"]
 
 
 def _nvcc():

@@ -104,6 +104,13 @@ struct sf_ctx {
     float* d_upd = nullptr; size_t cap_upd = 0;
     std::vector<float> h_skern;
 
+    // Kirchhoff migration (sf_kirchhoff_image, sf_adjoint_convolution)
+    double* d_wav = nullptr; size_t cap_wav = 0;
+    float* d_mig = nullptr; size_t cap_mig = 0;
+    float* d_kgeo = nullptr; size_t cap_kgeo = 0;
+    std::vector<double> h_wav;
+    std::vector<float> h_kgeo;
+
     // per-kernel timing (sf_set_kernel_timing)
     bool timing = false;
     cudaEvent_t kt_ev[SF_KT_N][2] = {};
@@ -155,6 +162,8 @@ int sf_kt_end(sf_ctx* c, int k, cudaStream_t st);
 void sf_plan_release(sf_ctx* c);
 // Normalised Gaussian taps of the reference's smooth_matrix (n x n, x major).
 void sf_smooth_kernel(float stdv, int n, std::vector<float>& k);
+// The reference's Ricker-type wavelet of Migration::set_wavelet.
+void sf_kirchhoff_wavelet(float fmax, float dt, std::vector<float>& w);
 // Gang shape for nshots shots of nstrips strips: CTAs per gang and gangs, so
 // that every gang of the grid is resident at once.
 int sf_gang_shape(sf_ctx* c, const void* kernel, size_t smem, int nshots, int nstrips, int gang_warps, int* G,

@@ -211,6 +211,37 @@ class Engine:
                                               0, _stream_ptr(stream)), "sf_update_slowness")
         return dS
 
+    # ----------------------------------------------------------- migration
+    def adjoint_convolution(self, traces, dt, fmax, out=None, stream=None):
+        """The reference's wavelet cross-correlation of (ntr, nt) traces."""
+        pi, mem, k1 = _ptr(traces)
+        shape = tuple(traces.shape)
+        if out is None:
+            out = np.zeros(shape, np.float32)
+        po, _, k2 = _ptr(out)
+        self._check(self.L.sf_adjoint_convolution(self._ctx, pi, po, int(shape[0]), int(shape[1]), float(dt),
+                                                  float(fmax), mem, _stream_ptr(stream)), "sf_adjoint_convolution")
+        return out
+
+    def kirchhoff_image(self, Ts, Tr, xsrc, xrec, data, dt, aperture, max_offset, out=None, stream=None):
+        """Image-domain Kirchhoff migration. Ts (nsrc, nxx, nzz) and Tr
+        (nrec, nxx, nzz) are CUDA tensors of padded tables; data (nsrc, nrec,
+        nt) correlated traces; returns the (nx, nz) image."""
+        xs = np.ascontiguousarray(xsrc, np.float32)
+        xr = np.ascontiguousarray(xrec, np.float32)
+        pts = self._dev_ptr(Ts, "Ts")
+        ptr = self._dev_ptr(Tr, "Tr")
+        pd, dmem, k1 = _ptr(data)
+        if out is None:
+            out = np.zeros((self.nx, self.nz), np.float32)
+        po, omem, k2 = _ptr(out)
+        nt = int(data.shape[-1])
+        self._check(self.L.sf_kirchhoff_image(self._ctx, pts, ptr, len(xs), len(xr), C.c_void_p(xs.ctypes.data),
+                                              C.c_void_p(xr.ctypes.data), pd, dmem, nt, float(dt), float(aperture),
+                                              float(max_offset), po, omem, _stream_ptr(stream)),
+                    "sf_kirchhoff_image")
+        return out
+
     # -------------------------------------------------------- planned batches
     def plan_batch(self, shots, rx, rz, stream=None):
         """Fix an isotropic batch (shots as for batch_forward) for

@@ -12,6 +12,7 @@ OUT = os.path.join(HERE, "_build")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 LIBSRC = ["admin.cpp", "geometry.cpp", "modeling.cpp", "inversion.cpp"]
 EXES = {"modeling.exe": "modeling_main.cpp", "inversion.exe": "inversion_main.cpp",
+        "migration.exe": "migration_main.cpp",
         "traveltime_tables.exe": "tables_main.cpp"}
 FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-I", lib_build.INC,
          "-I", os.path.join(CUDA, "include")]

@@ -38,6 +38,15 @@ inv_data_folder = {d}/
 inv_data_prefix = obs_shot_
 anisotropy = {aniso}
 mig_tables_folder = {d}/tab_
+mig_type = 0
+time_samples = 400
+time_spacing = 2e-3
+max_frequency = 25.0
+mig_aperture = 35
+mig_max_offset = 600
+mig_data_folder = {d}/
+mig_data_prefix = mig_shot_
+mig_seismic_folder = {d}/
 """
 
 
@@ -45,7 +54,8 @@ mig_tables_folder = {d}/tab_
 def exes(engine_lib):
     from seisfat2d_gb300.host import build as hb
     out = hb.build()
-    return {k: os.path.join(out, k) for k in ("modeling.exe", "inversion.exe", "traveltime_tables.exe")}
+    return {k: os.path.join(out, k) for k in ("modeling.exe", "inversion.exe", "traveltime_tables.exe",
+                                              "migration.exe")}
 
 
 def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False):
@@ -161,3 +171,35 @@ def test_inversion_exe_reduces_residual(oracle, cuda, exes, tmp_path):
     assert len(res) == 4 and res[-1] < res[0]
     vp = np.fromfile(os.path.join(d, f"tomography_iso_final_model_vp_{nz}x{nx}.bin"), np.float32)
     assert np.isfinite(vp).all() and vp.size == nx * nz
+
+
+def test_migration_exe_matches_engine(cuda, exes, tmp_path):
+    """migration.exe (image-domain Kirchhoff) writes the image the engine's
+    batched tables, correlation and imaging give through the Python mirror."""
+    from seisfat2d_gb300 import Engine
+    nx, nz, dx, dz = 60, 25, 10.0, 10.0
+    m = smooth_model(nx, nz, dx, seed=21)
+    shots = [(100.0, 0.0), (300.0, 0.0), (480.0, 0.0)]
+    recs = [(float(x), 0.0) for x in range(0, 590, 40)]
+    d = str(tmp_path)
+    p = write_case(d, nx, nz, dx, dz, m, shots, recs)
+    rng = np.random.default_rng(4)
+    data = rng.standard_normal((len(shots), len(recs), 400)).astype(np.float32)
+    for k in range(len(shots)):
+        data[k].tofile(os.path.join(d, f"mig_shot_{k + 1}.bin"))  # nt x nrec, trace-major
+    run(exes["migration.exe"], p)
+    img = np.fromfile(os.path.join(d, f"IDKDM_result_{nz}x{nx}.bin"), np.float32).reshape(nx, nz)
+    e = Engine(nx, nz, dx, dz)
+    e.set_slowness(m)
+    dev = cuda.device("cuda", 0)
+    tabs = []
+    for pts in (shots, recs):
+        e.batch_forward(pts, np.zeros(0, np.float32), np.zeros(0, np.float32), keep_tables=True)
+        t = cuda.empty((len(pts), e.nxx, e.nzz), dtype=cuda.float32, device=dev)
+        for k in range(len(pts)):
+            e.batch_table(k, e.nxx, out=t[k])
+        tabs.append(t)
+    corr = e.adjoint_convolution(data.reshape(-1, 400), 2e-3, 25.0).reshape(data.shape)
+    ref = e.kirchhoff_image(tabs[0], tabs[1], [s[0] for s in shots], [r[0] for r in recs], corr, 2e-3, 35.0, 600.0)
+    assert np.abs(ref).max() > 0
+    assert np.array_equal(img, ref)

@@ -289,3 +289,43 @@ def test_smoothing_kernel_and_update(oracle):
     assert np.array_equal(Sn[inner], (S[inner] + dS).astype(np.float32))
     Sn[inner] = S[inner]
     assert np.array_equal(Sn, S)  # the pad ring keeps its values
+
+
+def test_kirchhoff_correlation_matches_fft_form(oracle):
+    """The direct FP64 cross-correlation restates Migration::adjoint_convolution
+    (migration.cu:173-228): zero-padded FFT, product A conj(B), unnormalised
+    inverse (FFTW), shift nw/2 + nw/10."""
+    dt, fmax, nt = 0.002, 25.0, 300
+    w = oracle.kirchhoff_wavelet(fmax, dt)
+    nw = len(w)
+    assert nw > 4 and nw % 2 == 0
+    tr = np.random.default_rng(5).standard_normal((3, nt)).astype(np.float32)
+    got = oracle.adjoint_convolution(tr, dt, fmax)
+    nfft = 1
+    while nfft < nt + nw - 1:
+        nfft *= 2
+    W = np.fft.rfft(np.concatenate([w.astype(np.float64), np.zeros(nfft - nw)]))
+    shift = nw // 2 + nw // 10
+    for q in range(3):
+        A = np.fft.rfft(np.concatenate([tr[q].astype(np.float64), np.zeros(nfft - nt)]))
+        c = np.fft.irfft(A * np.conj(W), nfft) * nfft
+        ref = np.zeros(nt)
+        ref[shift:] = c[:nt - shift]
+        assert np.allclose(got[q], ref.astype(np.float32), rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+
+
+def test_kirchhoff_image_is_linear_in_the_traces(oracle):
+    rng = np.random.default_rng(2)
+    nx, nz, nb = 24, 16, 3
+    S = oracle.expand_boundary((1.0 / rng.uniform(1800, 2500, (nx, nz))).astype(np.float32))
+    xs = np.array([60.0, 150.0], np.float32)
+    xr = np.array([30.0, 90.0, 170.0], np.float32)
+    Ts = np.stack([oracle.solve_f32(S, 10.0, 10.0, float(x), 0.0) for x in xs])
+    Tr = np.stack([oracle.solve_f32(S, 10.0, 10.0, float(x), 0.0) for x in xr])
+    d = rng.standard_normal((2, 3, 200)).astype(np.float32)
+    a = oracle.kirchhoff_image(S, Ts, Tr, xs, xr, d, 0.001, 10.0, 10.0, 30.0, 1000.0)
+    b = oracle.kirchhoff_image(S, Ts, Tr, xs, xr, 2 * d, 0.001, 10.0, 10.0, 30.0, 1000.0)
+    assert np.isfinite(a).all() and np.abs(a).max() > 0
+    assert np.array_equal(b, 2 * a)
+    c = oracle.kirchhoff_image(S, Ts, Tr, xs, xr, d, 0.001, 10.0, 10.0, 30.0, 50.0)  # offset cut
+    assert not np.array_equal(a, c)
