@@ -250,6 +250,23 @@ int sf_kirchhoff_image(sf_ctx* ctx, const float* Ts, const float* Tr, int nsrc, 
                        const float* xrec, const float* data, int data_mem, int nt, float dt, float aperture,
                        float max_offset, float* image, int image_mem, void* stream);
 
+/* Angle-domain Kirchhoff migration (the reference's ADKDM: KDM.cu:3-55 with
+ * angle_domain_adjoint_kernel, migration.cu:572-663; bins of
+ * Migration::set_gathers, migration.cu:73-97): gathers (nz x nang x ncmp,
+ * z fastest, then angle, then CMP bin) of the same trace terms as
+ * sf_kirchhoff_image, each added to the bin of its trace's midpoint
+ * ((xsrc + xrec)/2 from the smallest midpoint in steps of half the smaller
+ * first source / receiver spacing) and of its reflection angle (steps of
+ * da up to max_angle). The reference adds with atomics from all columns at
+ * once; here each (depth, CMP) bin sums its traces in trace order and each
+ * trace's cells left to right, so bins agree with the reference to rounding.
+ * With gathers null the call only reports nang and ncmp. At most 256 angle
+ * bins. Host outputs synchronise `stream`. */
+int sf_kirchhoff_angle_gathers(sf_ctx* ctx, const float* Ts, const float* Tr, int nsrc, int nrec,
+                               const float* xsrc, const float* xrec, const float* data, int data_mem, int nt,
+                               float dt, float aperture, float max_offset, float max_angle, float da,
+                               float* gathers, int gathers_mem, int* nang, int* ncmp, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -279,3 +279,53 @@ extern "C" int ref_kirchhoff_adjoint(int nxx, int nzz, int nb, const float* S, c
     cuMemFree(dm);
     return 0;
 }
+
+// ADKDM (src/migration/ADKDM.cu:17-20 in the KDM.cu:3-55 loop): one launch of
+// angle_domain_adjoint_kernel per trace within max_offset, with that trace's
+// CMP and CMP bin (cmpId = (int)((CMP - minCMP) / dCMP)).
+extern "C" int ref_kirchhoff_angles(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr,
+                                    int nsrc, int nrec, const float* xsrc, const float* xrec, const float* data,
+                                    int nt, float dt, float dx, float dz, float aperture, float max_offset, float da,
+                                    int na, int ncmp, float mincmp, float dcmp, float* gathers)
+{
+    DR(cuCtxSetCurrent(g_ctx));
+    static CUfunction f_ang = nullptr;
+    if (!f_ang) {
+        const char* n_ang[] = {"_Z27angle_domain_adjoint_kernelPfS_S_S_S_ffffiiiiiffi", nullptr};
+        DR(get_fn(g_mig, n_ang, &f_ang));
+    }
+    const size_t matsize = (size_t)nxx * nzz;
+    const int nz = nzz - 2 * nb;
+    const size_t ng = (size_t)nz * na * ncmp;
+    CUdeviceptr dS, dTs, dTr, dd, dm;
+    DR(cuMemAlloc(&dS, sizeof(float) * matsize));
+    DR(cuMemAlloc(&dTs, sizeof(float) * matsize * nsrc));
+    DR(cuMemAlloc(&dTr, sizeof(float) * matsize * nrec));
+    DR(cuMemAlloc(&dd, sizeof(float) * (size_t)nsrc * nrec * nt));
+    DR(cuMemAlloc(&dm, sizeof(float) * ng));
+    DR(cuMemcpyHtoD(dS, S, sizeof(float) * matsize));
+    DR(cuMemcpyHtoD(dTs, Ts, sizeof(float) * matsize * nsrc));
+    DR(cuMemcpyHtoD(dTr, Tr, sizeof(float) * matsize * nrec));
+    DR(cuMemcpyHtoD(dd, data, sizeof(float) * (size_t)nsrc * nrec * nt));
+    DR(cuMemsetD32(dm, 0, ng));
+    const unsigned nblocks = (unsigned)((matsize + 255) / 256);
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            if (!(fabsf(xsrc[s] - xrec[r]) < max_offset)) continue;
+            float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            int cmpId = (int)((cmp - mincmp) / dcmp);
+            CUdeviceptr ts = dTs + sizeof(float) * matsize * s, tr = dTr + sizeof(float) * matsize * r;
+            CUdeviceptr tdat = dd + sizeof(float) * ((size_t)s * nrec + r) * nt;
+            void* args[] = {&dS, &ts, &tr, &tdat, &dm, &dx, &dz, &dt, &da, &nxx, &nzz, &nt, &na, &nb, &aperture, &cmp,
+                            &cmpId};
+            DR(cuLaunchKernel(f_ang, nblocks, 1, 1, 256, 1, 1, 0, nullptr, args, nullptr));
+        }
+    DR(cuCtxSynchronize());
+    DR(cuMemcpyDtoH(gathers, dm, sizeof(float) * ng));
+    cuMemFree(dS);
+    cuMemFree(dTs);
+    cuMemFree(dTr);
+    cuMemFree(dd);
+    cuMemFree(dm);
+    return 0;
+}

@@ -93,3 +93,40 @@ def kirchhoff_adjoint(S_padded, Ts, Tr, xsrc, xrec, data, dt, dx, dz, aperture, 
     if rc != 0:
         raise RuntimeError(f"ref_kirchhoff_adjoint failed ({rc})")
     return img
+
+
+def kirchhoff_angles(S_padded, Ts, Tr, xsrc, xrec, data, dt, dx, dz, aperture, max_offset, max_angle, da, nb=3):
+    """The reference's ADKDM trace loop with its own angle_domain_adjoint_kernel;
+    returns gathers (ncmp, nang, nz). CMP bins as Migration::set_gathers with
+    the largest CMP started from the first pair's (the reference leaves it
+    uninitialised)."""
+    h = _handle()
+    if not getattr(h, "_kirch", False):
+        h.ref_kirchhoff_open.argtypes = [C.c_char_p]
+        if h.ref_kirchhoff_open(build_ref.cubin_path("migration").encode()) != 0:
+            raise RuntimeError("ref_kirchhoff_open failed")
+        h.ref_kirchhoff_adjoint.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_int] + \
+            [C.c_void_p] * 3 + [C.c_int] + [C.c_float] * 5 + [C.c_void_p]
+        h._kirch = True
+    h.ref_kirchhoff_angles.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_int] + \
+        [C.c_void_p] * 3 + [C.c_int] + [C.c_float] * 6 + [C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p]
+    xs = np.ascontiguousarray(xsrc, np.float32)
+    xr = np.ascontiguousarray(xrec, np.float32)
+    f32 = np.float32
+    d = f32(0.5) * min(f32(xs[1] - xs[0]), f32(xr[1] - xr[0]))
+    cmps = (f32(0.5) * (xs[:, None] + xr[None, :])).astype(np.float32)
+    mn, mx = f32(min(f32(1e6), cmps.min())), f32(cmps.max())
+    na = int(f32(max_angle) / f32(da)) + 1
+    nc = int(f32(mx - mn) / d) + 1
+    S = np.ascontiguousarray(S_padded, np.float32)
+    nxx, nzz = S.shape
+    Ts = np.ascontiguousarray(Ts, np.float32)
+    Tr = np.ascontiguousarray(Tr, np.float32)
+    dd = np.ascontiguousarray(data, np.float32)
+    g = np.zeros((nc, na, nzz - 2 * nb), np.float32)
+    rc = h.ref_kirchhoff_angles(nxx, nzz, nb, S.ctypes.data, Ts.ctypes.data, Tr.ctypes.data, len(xs), len(xr),
+                                xs.ctypes.data, xr.ctypes.data, dd.ctypes.data, dd.shape[-1], dt, dx, dz, aperture,
+                                max_offset, da, na, nc, float(mn), float(d), g.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"ref_kirchhoff_angles failed ({rc})")
+    return g

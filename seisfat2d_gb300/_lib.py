@@ -70,6 +70,9 @@ SIGNATURES = {
     "sf_adjoint_convolution": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, VP]),
     "sf_kirchhoff_image": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP, VP, VP, C.c_int, C.c_int, C.c_float,
                                      C.c_float, C.c_float, VP, C.c_int, VP]),
+    "sf_kirchhoff_angle_gathers": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP, VP, VP, C.c_int, C.c_int,
+                                             C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, VP, C.c_int,
+                                             IP, IP, VP]),
 }
 
 _lib = None

@@ -108,6 +108,8 @@ struct sf_ctx {
     double* d_wav = nullptr; size_t cap_wav = 0;
     float* d_mig = nullptr; size_t cap_mig = 0;
     float* d_kgeo = nullptr; size_t cap_kgeo = 0;
+    int* d_kint = nullptr; size_t cap_kint = 0;
+    std::vector<int> h_kint;
     std::vector<double> h_wav;
     std::vector<float> h_kgeo;
 

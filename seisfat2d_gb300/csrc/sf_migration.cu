@@ -154,6 +154,83 @@ __global__ void k_correlate(const float* __restrict__ in, float* __restrict__ ou
     }
 }
 
+constexpr int kMaxAngles = 256;
+
+struct AngleParams {
+    const float* S;
+    const float* Ts;
+    const float* Tr;
+    const float* xs;
+    const float* xr;
+    const float* data;      // nsrc x nrec x nt correlated traces
+    const int* cmp_ptr;     // traces of CMP bin b: [cmp_ptr[b], cmp_ptr[b+1]) of cmp_tr
+    const int* cmp_tr;      // trace s * nrec + r, trace order within a bin
+    float* gathers;         // nz x nang x ncmp
+    int nsrc, nrec, nt, nxx, nzz, nb, nang, ncmp;
+    float dt, dx, dz, da, aperture;
+};
+
+// ADKDM's angle_domain_adjoint_kernel (migration.cu:572-663) as a gather: one
+// thread per (depth row, CMP bin) walks the bin's traces in trace order and,
+// for each, the row's cells left to right, adding each term to its
+// reflection-angle bin. The reference adds with atomics from all columns of a
+// launch at once, so its order within a bin is not fixed; the terms are the
+// same.
+__global__ void k_kirchhoff_angles(AngleParams p)
+{
+    const int nz = p.nzz - 2 * p.nb;
+    const size_t nthr = (size_t)nz * p.ncmp;
+    float acc[kMaxAngles];
+    for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < nthr; w += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(w % nz), b = (int)(w / nz);
+        const int i = iz + p.nb;
+        for (int a = 0; a < p.nang; a++) acc[a] = 0.0f;
+        const size_t matsize = (size_t)p.nzz * p.nxx;
+        const float z = __int2float_rd(i - p.nb) * p.dz;
+        const float scale_const = 1.0f / (2.0f * M_PI);
+        const float sigma = tanf(p.aperture * M_PI / 180.0f) * z;
+        for (int e = p.cmp_ptr[b]; e < p.cmp_ptr[b + 1]; e++) {
+            const int tr_id = p.cmp_tr[e];
+            const int s = tr_id / p.nrec, r = tr_id % p.nrec;
+            const float cmp = 0.5f * (p.xs[s] + p.xr[r]);
+            const float* Ts = p.Ts + matsize * s;
+            const float* Tr = p.Tr + matsize * r;
+            const float* trace = p.data + (size_t)tr_id * p.nt;
+            for (int j = p.nb; j < p.nxx - p.nb; j++) {
+                const size_t index = (size_t)i + (size_t)j * p.nzz;
+                const float x = __int2float_rd(j - p.nb) * p.dx;
+                const float T = Ts[index] + Tr[index];
+                const int tId = __float2int_rd(T / p.dt);
+                if (tId >= p.nt) continue;
+                const TableTerms ts = table_terms(Ts, i, j, p.nzz, p.dx, p.dz);
+                const TableTerms tr = table_terms(Tr, i, j, p.nzz, p.dx, p.dz);
+                const float Sc = p.S[index];
+                const float Jterm = sqrtf(ts.detH * tr.detH) * Sc / (ts.norm * tr.norm);
+                const float ux_s = ts.dx1 / ts.norm, uz_s = ts.dz1 / ts.norm;
+                const float ux_r = tr.dx1 / tr.norm, uz_r = tr.dz1 / tr.norm;
+                const float nx_norm = 0.0f, nz_norm = -1.0f;
+                const float cos_s = fabs(ux_s * nx_norm + uz_s * nz_norm);
+                const float cos_r = fabs(ux_r * nx_norm + uz_r * nz_norm);
+                const float obliquity = sqrt(max(0.0f, cos_s) * max(0.0f, cos_r));
+                const float R_s = max(Ts[index] / Sc, kEps);
+                const float R_r = max(Tr[index] / Sc, kEps);
+                const float G = 1.0f / sqrt(R_s * R_r);
+                const float theta_s = acosf(min(1.0f, max(-1.0f, ux_s * nx_norm + uz_s * nz_norm)));
+                const float theta_r = acosf(min(1.0f, max(-1.0f, ux_r * nx_norm + uz_r * nz_norm)));
+                const float theta = 0.5f * (theta_s + theta_r);
+                const float R = 1.0f + 0.2f * cosf(theta);
+                const float taper = expf(-0.5f * ((x - cmp) / (sigma + kEps)) * ((x - cmp) / (sigma + kEps)));
+                const float weights = scale_const * Jterm * obliquity * G * R * taper;
+                const float reflection_angle = 0.5f * acos((ts.dx1 * tr.dx1 + ts.dz1 * tr.dz1) / (ts.norm * tr.norm));
+                const float ang = 180.0f * reflection_angle / M_PI;
+                const int aId = __float2int_rd(ang / p.da);
+                if (aId >= 0 && aId < p.nang) acc[aId] = add_ftz(acc[aId], __fmul_rn(weights, trace[tId]));
+            }
+        }
+        for (int a = 0; a < p.nang; a++) p.gathers[(size_t)iz + (size_t)a * nz + (size_t)b * p.nang * nz] = acc[a];
+    }
+}
+
 }  // namespace
 
 // Migration::set_wavelet (migration.cu:54-71) as its source computes it.
@@ -260,6 +337,118 @@ extern "C" int sf_kirchhoff_image(sf_ctx* c, const float* Ts, const float* Tr, i
     CK(cudaGetLastError());
     if (image_mem == SF_MEM_HOST) {
         CK(cudaMemcpyAsync(image, di, ni * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return SF_OK;
+}
+
+// Migration::set_gathers (migration.cu:73-97): CMP spacing half the smaller of
+// the first source and receiver spacings, bins from the smallest CMP of all
+// pairs. The reference starts the largest CMP from an uninitialised value
+// (it assigns minCMP twice); here it starts from the first pair's CMP.
+static int angle_dims(const float* xsrc, int nsrc, const float* xrec, int nrec, float max_angle, float da,
+                      int* nang, int* ncmp, float* mincmp, float* dcmp)
+{
+    if (nsrc < 2 || nrec < 2 || !(da > 0.0f)) return SF_ERR_ARG;
+    const float ds = xsrc[1] - xsrc[0], dr = xrec[1] - xrec[0];
+    const float d = 0.5f * std::min(ds, dr);
+    if (!(d > 0.0f)) return SF_ERR_ARG;
+    float mn = 1e6f, mx = 0.5f * (xsrc[0] + xrec[0]);
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            const float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            mn = (cmp < mn) ? cmp : mn;
+            mx = (cmp > mx) ? cmp : mx;
+        }
+    *nang = (int)(max_angle / da) + 1;
+    *ncmp = (int)((mx - mn) / d) + 1;
+    *mincmp = mn;
+    *dcmp = d;
+    return SF_OK;
+}
+
+extern "C" int sf_kirchhoff_angle_gathers(sf_ctx* c, const float* Ts, const float* Tr, int nsrc, int nrec,
+                                          const float* xsrc, const float* xrec, const float* data, int data_mem, int nt,
+                                          float dt, float aperture, float max_offset, float max_angle, float da,
+                                          float* gathers, int gathers_mem, int* nang_out, int* ncmp_out, void* stream)
+{
+    if (!c || !xsrc || !xrec) return sf_fail(c, SF_ERR_ARG, "null argument");
+    int nang, ncmp;
+    float mincmp, dcmp;
+    if (angle_dims(xsrc, nsrc, xrec, nrec, max_angle, da, &nang, &ncmp, &mincmp, &dcmp))
+        return sf_fail(c, SF_ERR_ARG, "angle gathers need two sources, two receivers, increasing positions, da > 0");
+    if (nang > kMaxAngles) return sf_fail(c, SF_ERR_RANGE, "more than 256 angle bins");
+    if (nang_out) *nang_out = nang;
+    if (ncmp_out) *ncmp_out = ncmp;
+    if (!gathers) return SF_OK;  // dimensions only
+    if (!Ts || !Tr || !data || nt < 1 || !(dt > 0.0f)) return sf_fail(c, SF_ERR_ARG, "bad Kirchhoff arguments");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    // traces by CMP bin, trace order kept (KDM.cu:28-53)
+    std::vector<int> cnt(ncmp + 1, 0), ids;
+    std::vector<std::pair<int, int>> tr;
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            if (!(fabsf(xsrc[s] - xrec[r]) < max_offset)) continue;
+            const float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            const int b = (int)((cmp - mincmp) / dcmp);
+            if (b < 0 || b >= ncmp) continue;
+            tr.push_back({b, s * nrec + r});
+            cnt[b + 1]++;
+        }
+    for (int b = 0; b < ncmp; b++) cnt[b + 1] += cnt[b];
+    ids.resize(tr.size());
+    {
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (auto& t : tr) ids[fill[t.first]++] = t.second;
+    }
+    const size_t nd = (size_t)nsrc * nrec * nt, ng = (size_t)(c->nzz - 2 * c->nb) * nang * ncmp;
+    c->h_kgeo.assign(xsrc, xsrc + nsrc);
+    c->h_kgeo.insert(c->h_kgeo.end(), xrec, xrec + nrec);
+    c->h_kint.assign(cnt.begin(), cnt.end());
+    c->h_kint.insert(c->h_kint.end(), ids.begin(), ids.end());
+    int rc = sf_dev_reserve(c, (void**)&c->d_kgeo, &c->cap_kgeo, c->h_kgeo.size() * sizeof(float));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_kint, &c->cap_kint, c->h_kint.size() * sizeof(int));
+    if (!rc && (data_mem == SF_MEM_HOST || gathers_mem == SF_MEM_HOST))
+        rc = sf_dev_reserve(c, (void**)&c->d_mig, &c->cap_mig, (nd + ng) * sizeof(float));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->d_kgeo, c->h_kgeo.data(), c->h_kgeo.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_kint, c->h_kint.data(), c->h_kint.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    const float* dd = data;
+    float* dg = gathers;
+    if (data_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(c->d_mig, data, nd * sizeof(float), cudaMemcpyHostToDevice, st));
+        dd = c->d_mig;
+    }
+    if (gathers_mem == SF_MEM_HOST) dg = c->d_mig + nd;
+    AngleParams p;
+    p.S = c->d_S;
+    p.Ts = Ts;
+    p.Tr = Tr;
+    p.xs = c->d_kgeo;
+    p.xr = c->d_kgeo + nsrc;
+    p.data = dd;
+    p.cmp_ptr = c->d_kint;
+    p.cmp_tr = c->d_kint + ncmp + 1;
+    p.gathers = dg;
+    p.nsrc = nsrc;
+    p.nrec = nrec;
+    p.nt = nt;
+    p.nxx = c->nxx;
+    p.nzz = c->nzz;
+    p.nb = c->nb;
+    p.nang = nang;
+    p.ncmp = ncmp;
+    p.dt = dt;
+    p.dx = c->dx;
+    p.dz = c->dz;
+    p.da = da;
+    p.aperture = aperture;
+    const size_t nthr = (size_t)(c->nzz - 2 * c->nb) * ncmp;
+    k_kirchhoff_angles<<<(unsigned)std::min<size_t>((nthr + 127) / 128, (size_t)c->sms * 64), 128, 0, st>>>(p);
+    CK(cudaGetLastError());
+    if (gathers_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(gathers, dg, ng * sizeof(float), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
     }
     return SF_OK;

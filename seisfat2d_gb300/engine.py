@@ -242,6 +242,27 @@ class Engine:
                     "sf_kirchhoff_image")
         return out
 
+    def kirchhoff_angle_gathers(self, Ts, Tr, xsrc, xrec, data, dt, aperture, max_offset, max_angle, da,
+                                stream=None):
+        """Angle-domain Kirchhoff migration; returns gathers (ncmp, nang, nz)."""
+        xs = np.ascontiguousarray(xsrc, np.float32)
+        xr = np.ascontiguousarray(xrec, np.float32)
+        na, nc = C.c_int(), C.c_int()
+        args = (C.c_void_p(xs.ctypes.data), C.c_void_p(xr.ctypes.data))
+        self._check(self.L.sf_kirchhoff_angle_gathers(self._ctx, None, None, len(xs), len(xr), *args, None, 0, 1,
+                                                      1.0, float(aperture), float(max_offset), float(max_angle),
+                                                      float(da), None, 0, C.byref(na), C.byref(nc), None),
+                    "sf_kirchhoff_angle_gathers")
+        out = np.zeros((nc.value, na.value, self.nz), np.float32)
+        pd, dmem, k1 = _ptr(data)
+        self._check(self.L.sf_kirchhoff_angle_gathers(self._ctx, self._dev_ptr(Ts, "Ts"), self._dev_ptr(Tr, "Tr"),
+                                                      len(xs), len(xr), *args, pd, dmem, int(data.shape[-1]),
+                                                      float(dt), float(aperture), float(max_offset),
+                                                      float(max_angle), float(da), C.c_void_p(out.ctypes.data), 0,
+                                                      None, None, _stream_ptr(stream)),
+                    "sf_kirchhoff_angle_gathers")
+        return out
+
     # -------------------------------------------------------- planned batches
     def plan_batch(self, shots, rx, rz, stream=None):
         """Fix an isotropic batch (shots as for batch_forward) for

@@ -6,8 +6,11 @@
 // cross-correlated with the reference's wavelet (sf_adjoint_convolution) and
 // the image is summed over all traces in one launch (sf_kirchhoff_image,
 // bit-identical to the reference's launch-per-trace kernel on the same
-// tables and traces). Writes <mig_seismic_folder>IDKDM_result_<nz>x<nx>.bin.
-// The angle-domain and least-squares variants (mig_type 1-3) are not built.
+// tables and traces). mig_type = 0 writes the image
+// <mig_seismic_folder>IDKDM_result_<nz>x<nx>.bin; mig_type = 1 (ADKDM,
+// ADKDM.cu:3-20) writes angle gathers <mig_seismic_folder>ADKDM_result_
+// <nz>x<nCMP>x<nang>.bin (sf_kirchhoff_angle_gathers). The least-squares
+// variants (mig_type 2, 3) are not built.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -43,8 +46,9 @@ int main(int argc, char** argv)
     }
     try {
         const std::string file = argv[1];
-        if (std::stoi(catch_parameter("mig_type", file)) != 0)
-            throw std::invalid_argument("only mig_type = 0 (image-domain Kirchhoff) is built");
+        const int mig_type = std::stoi(catch_parameter("mig_type", file));
+        if (mig_type != 0 && mig_type != 1)
+            throw std::invalid_argument("only mig_type = 0 (image domain) and 1 (angle domain) are built");
         const int nt = std::stoi(catch_parameter("time_samples", file));
         const float dt = std::stof(catch_parameter("time_spacing", file));
         const float fmax = std::stof(catch_parameter("max_frequency", file));
@@ -66,21 +70,40 @@ int main(int argc, char** argv)
         tables_on_device(m, m->geometry->xsrc, m->geometry->zsrc, ns, d_Ts);
         tables_on_device(m, m->geometry->xrec, m->geometry->zrec, nr, d_Tr);
         // traces: per source nt x nrec, trace-major (KDM.cu:14-15, :46-47)
-        std::vector<float> data((size_t)ns * nr * nt), corr(data.size()), image((size_t)m->nPoints);
+        std::vector<float> data((size_t)ns * nr * nt), corr(data.size());
         for (int s = 0; s < ns; s++)
             import_binary_float(data_folder + data_prefix + std::to_string(s + 1) + ".bin",
                                 data.data() + (size_t)s * nr * nt, nr * nt);
         sf_check(sf_adjoint_convolution(m->engine(), data.data(), corr.data(), ns * nr, nt, dt, fmax, SF_MEM_HOST,
                                         nullptr),
                  m->engine(), "sf_adjoint_convolution");
-        sf_check(sf_kirchhoff_image(m->engine(), d_Ts, d_Tr, ns, nr, m->geometry->xsrc, m->geometry->xrec,
-                                    corr.data(), SF_MEM_HOST, nt, dt, aperture, max_offset, image.data(),
-                                    SF_MEM_HOST, nullptr),
-                 m->engine(), "sf_kirchhoff_image");
+        std::string out_path;
+        std::vector<float> out;
+        if (mig_type == 0) {
+            out.resize((size_t)m->nPoints);
+            sf_check(sf_kirchhoff_image(m->engine(), d_Ts, d_Tr, ns, nr, m->geometry->xsrc, m->geometry->xrec,
+                                        corr.data(), SF_MEM_HOST, nt, dt, aperture, max_offset, out.data(),
+                                        SF_MEM_HOST, nullptr),
+                     m->engine(), "sf_kirchhoff_image");
+            out_path = seismic_folder + "IDKDM_result_" + std::to_string(m->nz) + "x" + std::to_string(m->nx) + ".bin";
+        } else {
+            const float max_angle = std::stof(catch_parameter("mig_max_angle", file));
+            const float da = std::stof(catch_parameter("mig_angle_spacing", file));
+            int nang = 0, ncmp = 0;
+            sf_check(sf_kirchhoff_angle_gathers(m->engine(), d_Ts, d_Tr, ns, nr, m->geometry->xsrc, m->geometry->xrec,
+                                                nullptr, SF_MEM_HOST, nt, dt, aperture, max_offset, max_angle, da,
+                                                nullptr, SF_MEM_HOST, &nang, &ncmp, nullptr),
+                     m->engine(), "sf_kirchhoff_angle_gathers");
+            out.resize((size_t)m->nz * nang * ncmp);
+            sf_check(sf_kirchhoff_angle_gathers(m->engine(), d_Ts, d_Tr, ns, nr, m->geometry->xsrc, m->geometry->xrec,
+                                                corr.data(), SF_MEM_HOST, nt, dt, aperture, max_offset, max_angle, da,
+                                                out.data(), SF_MEM_HOST, nullptr, nullptr, nullptr),
+                     m->engine(), "sf_kirchhoff_angle_gathers");
+            out_path = seismic_folder + "ADKDM_result_" + std::to_string(m->nz) + "x" + std::to_string(ncmp) + "x" +
+                       std::to_string(nang) + ".bin";
+        }
         auto tf = std::chrono::system_clock::now();
-        export_binary_float(seismic_folder + "IDKDM_result_" + std::to_string(m->nz) + "x" + std::to_string(m->nx) +
-                                ".bin",
-                            image.data(), m->nPoints);
+        export_binary_float(out_path, out.data(), (int)out.size());
         cudaFree(d_Ts);
         cudaFree(d_Tr);
         std::chrono::duration<double> elapsed = tf - ti;

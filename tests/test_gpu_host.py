@@ -38,7 +38,9 @@ inv_data_folder = {d}/
 inv_data_prefix = obs_shot_
 anisotropy = {aniso}
 mig_tables_folder = {d}/tab_
-mig_type = 0
+mig_type = {migtype}
+mig_max_angle = 60
+mig_angle_spacing = 2.0
 time_samples = 400
 time_spacing = 2e-3
 max_frequency = 25.0
@@ -58,7 +60,7 @@ def exes(engine_lib):
                                               "migration.exe")}
 
 
-def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False):
+def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False, migtype=0):
     m.astype(np.float32).tofile(os.path.join(d, "slowness.bin"))
     with open(os.path.join(d, "sps.txt"), "w") as f:
         f.write("".join(f"{x},{z}\n" for x, z in shots))
@@ -67,7 +69,7 @@ def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=Fa
     p = os.path.join(d, "parameters.txt")
     with open(p, "w") as f:
         f.write(PARAMS.format(nx=nx, nz=nz, dx=dx, dz=dz, d=d, mtype=mtype, batch="true" if batch else "false",
-                              aniso="true" if aniso else "false"))
+                              aniso="true" if aniso else "false", migtype=migtype))
     return p
 
 
@@ -173,22 +175,23 @@ def test_inversion_exe_reduces_residual(oracle, cuda, exes, tmp_path):
     assert np.isfinite(vp).all() and vp.size == nx * nz
 
 
-def test_migration_exe_matches_engine(cuda, exes, tmp_path):
-    """migration.exe (image-domain Kirchhoff) writes the image the engine's
-    batched tables, correlation and imaging give through the Python mirror."""
+@pytest.mark.parametrize("migtype", [0, 1])
+def test_migration_exe_matches_engine(cuda, exes, tmp_path, migtype):
+    """migration.exe (image-domain or angle-domain Kirchhoff) writes what the
+    engine's batched tables, correlation and imaging give through the Python
+    mirror."""
     from seisfat2d_gb300 import Engine
     nx, nz, dx, dz = 60, 25, 10.0, 10.0
     m = smooth_model(nx, nz, dx, seed=21)
     shots = [(100.0, 0.0), (300.0, 0.0), (480.0, 0.0)]
     recs = [(float(x), 0.0) for x in range(0, 590, 40)]
     d = str(tmp_path)
-    p = write_case(d, nx, nz, dx, dz, m, shots, recs)
+    p = write_case(d, nx, nz, dx, dz, m, shots, recs, migtype=migtype)
     rng = np.random.default_rng(4)
     data = rng.standard_normal((len(shots), len(recs), 400)).astype(np.float32)
     for k in range(len(shots)):
         data[k].tofile(os.path.join(d, f"mig_shot_{k + 1}.bin"))  # nt x nrec, trace-major
     run(exes["migration.exe"], p)
-    img = np.fromfile(os.path.join(d, f"IDKDM_result_{nz}x{nx}.bin"), np.float32).reshape(nx, nz)
     e = Engine(nx, nz, dx, dz)
     e.set_slowness(m)
     dev = cuda.device("cuda", 0)
@@ -200,6 +203,13 @@ def test_migration_exe_matches_engine(cuda, exes, tmp_path):
             e.batch_table(k, e.nxx, out=t[k])
         tabs.append(t)
     corr = e.adjoint_convolution(data.reshape(-1, 400), 2e-3, 25.0).reshape(data.shape)
-    ref = e.kirchhoff_image(tabs[0], tabs[1], [s[0] for s in shots], [r[0] for r in recs], corr, 2e-3, 35.0, 600.0)
+    xs, xr = [s[0] for s in shots], [r[0] for r in recs]
+    if migtype == 0:
+        img = np.fromfile(os.path.join(d, f"IDKDM_result_{nz}x{nx}.bin"), np.float32).reshape(nx, nz)
+        ref = e.kirchhoff_image(tabs[0], tabs[1], xs, xr, corr, 2e-3, 35.0, 600.0)
+    else:
+        ref = e.kirchhoff_angle_gathers(tabs[0], tabs[1], xs, xr, corr, 2e-3, 35.0, 600.0, 60.0, 2.0)
+        nc, na, _ = ref.shape
+        img = np.fromfile(os.path.join(d, f"ADKDM_result_{nz}x{nc}x{na}.bin"), np.float32).reshape(ref.shape)
     assert np.abs(ref).max() > 0
     assert np.array_equal(img, ref)
