@@ -84,55 +84,50 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
     float t1d1 = REF ? __fmaf_rn(k.dz, m1, tv) : fadd(tv, fmul(k.dz, m1));
     float t1d2 = REF ? __fmaf_rn(k.dx, m2, te) : fadd(te, fmul(k.dx, m2));
     float t1D = fminf(t1d1, t1d2);
-    float t1 = kBig, t2 = kBig, t3 = kBig;
-    float dte = fsub(te, tev);
-    float dtv = fsub(tv, tev);
-    int br = 0;
-    float rr = 0.0f, dd = 0.0f, q = 0.0f, qq = 0.0f;
-    if ((tv <= fadd(te, fmul(k.dx, sref))) && (te <= fadd(tv, fmul(k.dz, sref))) &&
-        (dte >= 0.0f) && (dtv >= 0.0f)) {
-        float ta = fsub(fadd(tev, te), tv);
-        float tb = fadd(fsub(tev, te), tv);
-        dd = fsub(ta, tb);
-        float num;
-        if (REF) {
-            rr = fsqrt(__fmaf_rn(fmul(fmul(4.0f, sref), sref), k.D, -fmul(fmul(k.K, dd), dd)));
-            num = fadd(__fmaf_rn(tb, k.dz2i, fmul(ta, k.dx2i)), rr);
-        } else {
-            rr = fsqrt(fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd)));
-            num = fadd(fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i)), rr);
-        }
-        t1 = fdiv_k<EXACT>(num, k.D, k.rD, k.mflags & 8, bad);
-        br = 3;
+    const float dte = fsub(te, tev);
+    const float dtv = fsub(tv, tev);
+    // The 2D candidate (modeling.cu:328-339) and the edge candidates (:342-353)
+    // through one code path, so that the lanes of a warp do not diverge: the
+    // edge update divides first, then takes a root; the 2D one takes a root,
+    // then divides. Each lane selects the operands of the candidate the
+    // reference's branches would take (same operations, same bits); the
+    // operations of the other candidate get operands that keep them on their
+    // fast paths.
+    const bool c2d = (tv <= fadd(te, fmul(k.dx, sref))) && (te <= fadd(tv, fmul(k.dz, sref))) &&
+                     (dte >= 0.0f) && (dtv >= 0.0f);
+    const float thz = fdiv_k<EXACT>(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4, bad);
+    const float thx = fdiv_k<EXACT>(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4, bad);
+    const bool c2 = !c2d && (dte <= thz) && (dte > 0.0f);        // t2: from te, step dz
+    const bool c3 = !c2d && !c2 && (dtv <= thx) && (dtv > 0.0f);  // t3: from tv, step dx
+    const bool ce = c2 || c3;
+    const float hq = c2 ? k.dz : k.dx;  // step the difference is divided by
+    const float rq = c2 ? k.rdz : k.rdx;
+    const bool vq = c2 ? (k.mflags & 2) : (k.mflags & 1);
+    const float hx = c2 ? k.dx : k.dz;  // step that multiplies the root
+    const float bs = c2 ? te : tv;
+    const float qe = fdiv_k<EXACT>(ce ? (c2 ? dte : dtv) : hq, hq, rq, vq, bad);
+    const float ta = fsub(fadd(tev, te), tv);
+    const float tb = fadd(fsub(tev, te), tv);
+    const float dde = fsub(ta, tb);
+    float disc, earg, num0;
+    if (REF) {
+        disc = __fmaf_rn(fmul(fmul(4.0f, sref), sref), k.D, -fmul(fmul(k.K, dde), dde));
+        earg = __fmaf_rn(-qe, qe, fmul(sref, sref));
+        num0 = __fmaf_rn(tb, k.dz2i, fmul(ta, k.dx2i));
     } else {
-        // the two edge candidates of modeling.cu:342-353 share one code path:
-        // t2 (from te, step dz) is tried first, t3 (from tv, step dx) otherwise
-        const bool c2 = (dte <= fdiv_k<EXACT>(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4, bad)) &&
-                         (dte > 0.0f);
-        bool c3 = false;
-        if (!c2)
-            c3 = (dtv <= fdiv_k<EXACT>(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4, bad)) &&
-                     (dtv > 0.0f);
-        if (c2 || c3) {
-            const float dn = c2 ? dte : dtv;    // te - tev or tv - tev
-            const float hq = c2 ? k.dz : k.dx;  // step the difference is divided by
-            const float rq = c2 ? k.rdz : k.rdx;
-            const bool vq = c2 ? (k.mflags & 2) : (k.mflags & 1);
-            const float hx = c2 ? k.dx : k.dz;  // step that multiplies the root
-            const float bs = c2 ? te : tv;
-            q = fdiv_k<EXACT>(dn, hq, rq, vq, bad);
-            float t;
-            if (REF) {
-                qq = fsqrt(__fmaf_rn(-q, q, fmul(sref, sref)));
-                t = __fmaf_rn(hx, qq, bs);
-            } else {
-                qq = fsqrt(fsub(fmul(sref, sref), fmul(q, q)));
-                t = fadd(bs, fmul(hx, qq));
-            }
-            if (c2) { t2 = t; br = 4; }
-            else { t3 = t; br = 5; }
-        }
+        disc = fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dde), dde));
+        earg = fsub(fmul(sref, sref), fmul(qe, qe));
+        num0 = fadd(fmul(tb, k.dz2i), fmul(ta, k.dx2i));
     }
+    const float root = fsqrt(c2d ? disc : (ce ? earg : 1.0f));
+    const float t1v = fdiv_k<EXACT>(c2d ? fadd(num0, root) : k.D, k.D, k.rD, k.mflags & 8, bad);
+    const float tq = REF ? __fmaf_rn(hx, root, bs) : fadd(bs, fmul(hx, root));
+    const float t1 = c2d ? t1v : kBig;
+    const float t2 = c2 ? tq : kBig;
+    const float t3 = c3 ? tq : kBig;
+    const int br = c2d ? 3 : (c2 ? 4 : (c3 ? 5 : 0));
+    const float rr = c2d ? root : 0.0f, dd = c2d ? dde : 0.0f;
+    const float q = ce ? qe : 0.0f, qq = ce ? root : 0.0f;
     float t2D = fminf(t1, fminf(t2, t3));
     float cand = fminf(t1D, t2D);
     float tnew = fminf(told, cand);
