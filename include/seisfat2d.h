@@ -267,6 +267,43 @@ int sf_kirchhoff_angle_gathers(sf_ctx* ctx, const float* Ts, const float* Tr, in
                                float dt, float aperture, float max_offset, float max_angle, float da,
                                float* gathers, int gathers_mem, int* nang, int* ncmp, void* stream);
 
+/* ---- Least-squares Kirchhoff migration's operators (the reference's IDLSKDM
+ * and ADLSKDM: LSKDM.cu:3-245 driving IDLSKDM.cu:24-37 / ADLSKDM.cu:43-59;
+ * kernels image_domain_forward_kernel, migration.cu:485-570, and
+ * angle_domain_forward_kernel, :665-756; Migration::forward_convolution,
+ * :230-261). The adjoints are sf_kirchhoff_image and
+ * sf_kirchhoff_angle_gathers with sf_adjoint_convolution. ----
+ *
+ * sf_forward_convolution: convolution of ntr traces of nt samples with the
+ * reference's wavelet for fmax, as its FFTW product A*B and unnormalised
+ * inverse give it (scaled by the FFT length), output sample t taken from
+ * t + nw/2 + nw/10. Computed directly in FP64 and rounded once to FP32.
+ *
+ * sf_kirchhoff_image_forward: traces (nsrc x nrec x nt, host or device per
+ * data_mem) from an image (nz x nx, z fastest, per image_mem): for each pair
+ * with |xsrc - xrec| < max_offset, each image cell adds its image-domain
+ * weight times its value to sample floor((Ts + Tr)/dt) when that is below nt;
+ * the other traces are 0. The reference adds with one atomicAdd per cell and
+ * launch; here each trace's terms are summed in a fixed order that depends on
+ * the sizes only, so results agree with the reference to rounding and repeat
+ * bit for bit. Tables as for sf_kirchhoff_image. At most about 51,000 time
+ * samples (SF_ERR_RANGE beyond).
+ *
+ * sf_kirchhoff_angle_forward: the same from angle gathers (nz x nang x ncmp,
+ * bins as sf_kirchhoff_angle_gathers): each cell reads the gather of its
+ * trace's CMP bin at its depth and reflection-angle bin.
+ *
+ * Host outputs synchronise `stream`. */
+int sf_forward_convolution(sf_ctx* ctx, const float* traces, float* out, int ntr, int nt, float dt, float fmax,
+                           int mem, void* stream);
+int sf_kirchhoff_image_forward(sf_ctx* ctx, const float* Ts, const float* Tr, int nsrc, int nrec, const float* xsrc,
+                               const float* xrec, const float* image, int image_mem, int nt, float dt,
+                               float aperture, float max_offset, float* data, int data_mem, void* stream);
+int sf_kirchhoff_angle_forward(sf_ctx* ctx, const float* Ts, const float* Tr, int nsrc, int nrec, const float* xsrc,
+                               const float* xrec, const float* gathers, int gathers_mem, int nt, float dt,
+                               float aperture, float max_offset, float max_angle, float da, float* data,
+                               int data_mem, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

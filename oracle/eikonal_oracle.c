@@ -1133,16 +1133,62 @@ void orc_adjoint_convolution(const float* in, float* out, int ntr, int nt, const
  * operands and results to zero (sign kept). */
 static float ftz(float x) { return fabsf(x) < FLT_MIN ? copysignf(0.0f, x) : x; }
 
+/* One cell's Kirchhoff weight and reflection angle (degrees), as the
+ * reference's four kernels compute them (migration.cu:418-466, :505-553,
+ * :592-645, :685-738), FP32 with libm functions (the GPU uses CUDA's;
+ * agreement is to rounding). */
+static float orc_kweight(const float* S, const float* ts, const float* tr, int i, int j, int nzz, int nb, float dx,
+                         float dz, float aperture, float cmp, float* ang_deg)
+{
+    const float EPSK = 1e-6f;
+    size_t index = (size_t)i + (size_t)j * nzz;
+    float z = (float)(i - nb) * dz, x = (float)(j - nb) * dx;
+#define ORC_D(A)                                                                                      \
+    float A##_dz = 0.5f * (A[(i + 1) + j * nzz] - A[(i - 1) + j * nzz]) / dz;                        \
+    float A##_dx = 0.5f * (A[i + (j + 1) * nzz] - A[i + (j - 1) * nzz]) / dx;                        \
+    float A##_dz2 = (A[(i + 1) + j * nzz] - 2.0f * A[i + j * nzz] + A[(i - 1) + j * nzz]) / (dz * dz); \
+    float A##_dx2 = (A[i + (j + 1) * nzz] - 2.0f * A[i + j * nzz] + A[i + (j - 1) * nzz]) / (dx * dx); \
+    float A##_dxdz = (A[(i + 1) + (j + 1) * nzz] - A[(i - 1) + (j + 1) * nzz] - A[(i + 1) + (j - 1) * nzz] + \
+                      A[(i - 1) + (j - 1) * nzz]) / (4.0f * dx * dz);
+    ORC_D(ts)
+    ORC_D(tr)
+#undef ORC_D
+    float norm_s = sqrtf(ts_dx * ts_dx + ts_dz * ts_dz) + EPSK;
+    float norm_r = sqrtf(tr_dx * tr_dx + tr_dz * tr_dz) + EPSK;
+    float detHs = fabsf(ts_dx2 * ts_dz2 - ts_dxdz * ts_dxdz) + EPSK;
+    float detHr = fabsf(tr_dx2 * tr_dz2 - tr_dxdz * tr_dxdz) + EPSK;
+    float Jterm = sqrtf(detHs * detHr) * S[index] / (norm_s * norm_r);
+    float ux_s = ts_dx / norm_s, uz_s = ts_dz / norm_s;
+    float ux_r = tr_dx / norm_r, uz_r = tr_dz / norm_r;
+    float nxn = 0.0f, nzn = -1.0f;
+    float cos_s = fabsf(ux_s * nxn + uz_s * nzn);
+    float cos_r = fabsf(ux_r * nxn + uz_r * nzn);
+    float obl = sqrtf(fmaxf(0.0f, cos_s) * fmaxf(0.0f, cos_r));
+    float R_s = fmaxf(ts[index] / S[index], EPSK);
+    float R_r = fmaxf(tr[index] / S[index], EPSK);
+    float G = 1.0f / sqrtf(R_s * R_r);
+    float th_s = acosf(fminf(1.0f, fmaxf(-1.0f, ux_s * nxn + uz_s * nzn)));
+    float th_r = acosf(fminf(1.0f, fmaxf(-1.0f, ux_r * nxn + uz_r * nzn)));
+    float R = 1.0f + 0.2f * cosf(0.5f * (th_s + th_r));
+    float scale_const = (float)(1.0f / (2.0f * ORC_PI));
+    float sigma = tanf((float)(aperture * ORC_PI / 180.0f)) * z;
+    float u = (x - cmp) / (sigma + EPSK);
+    float taper = expf(-0.5f * u * u);
+    if (ang_deg) {
+        float refl = 0.5f * acosf((ts_dx * tr_dx + ts_dz * tr_dz) / (norm_s * norm_r));
+        *ang_deg = (float)(180.0f * refl / ORC_PI);
+    }
+    return scale_const * Jterm * obl * G * R * taper;
+}
+
 /* KDM::kirchhoff_depth_migration + image_domain_adjoint_kernel
  * (KDM.cu:3-55, migration.cu:398-483): for every source, every receiver
  * within max_offset (in that order), every model cell with T = Ts + Tr below
- * nt*dt: image += weight * trace[floor(T/dt)], FP32, the kernel's formulas
- * with libm functions (the GPU uses CUDA's; agreement is to rounding). */
+ * nt*dt: image += weight * trace[floor(T/dt)], FP32. */
 void orc_kirchhoff_image(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr, int nsrc,
                          int nrec, const float* xsrc, const float* xrec, const float* data, int nt, float dt,
                          float dx, float dz, float aperture, float max_offset, float* image)
 {
-    const float EPSK = 1e-6f;
     size_t matsize = (size_t)nxx * nzz;
     int nz = nzz - 2 * nb, nx = nxx - 2 * nb;
     for (size_t q = 0; q < (size_t)nx * nz; q++) image[q] = 0.0f;
@@ -1157,44 +1203,82 @@ void orc_kirchhoff_image(int nxx, int nzz, int nb, const float* S, const float* 
             for (int j = nb; j < nxx - nb; j++)
                 for (int i = nb; i < nzz - nb; i++) {
                     size_t index = (size_t)i + (size_t)j * nzz;
-                    float z = (float)(i - nb) * dz, x = (float)(j - nb) * dx;
                     float T = ts[index] + tr[index];
                     int tId = (int)floorf(T / dt);
                     if (tId >= nt) continue;
-#define ORC_D(A)                                                                                      \
-    float A##_dz = 0.5f * (A[(i + 1) + j * nzz] - A[(i - 1) + j * nzz]) / dz;                        \
-    float A##_dx = 0.5f * (A[i + (j + 1) * nzz] - A[i + (j - 1) * nzz]) / dx;                        \
-    float A##_dz2 = (A[(i + 1) + j * nzz] - 2.0f * A[i + j * nzz] + A[(i - 1) + j * nzz]) / (dz * dz); \
-    float A##_dx2 = (A[i + (j + 1) * nzz] - 2.0f * A[i + j * nzz] + A[i + (j - 1) * nzz]) / (dx * dx); \
-    float A##_dxdz = (A[(i + 1) + (j + 1) * nzz] - A[(i - 1) + (j + 1) * nzz] - A[(i + 1) + (j - 1) * nzz] + \
-                      A[(i - 1) + (j - 1) * nzz]) / (4.0f * dx * dz);
-                    ORC_D(ts)
-                    ORC_D(tr)
-#undef ORC_D
-                    float norm_s = sqrtf(ts_dx * ts_dx + ts_dz * ts_dz) + EPSK;
-                    float norm_r = sqrtf(tr_dx * tr_dx + tr_dz * tr_dz) + EPSK;
-                    float detHs = fabsf(ts_dx2 * ts_dz2 - ts_dxdz * ts_dxdz) + EPSK;
-                    float detHr = fabsf(tr_dx2 * tr_dz2 - tr_dxdz * tr_dxdz) + EPSK;
-                    float Jterm = sqrtf(detHs * detHr) * S[index] / (norm_s * norm_r);
-                    float ux_s = ts_dx / norm_s, uz_s = ts_dz / norm_s;
-                    float ux_r = tr_dx / norm_r, uz_r = tr_dz / norm_r;
-                    float nxn = 0.0f, nzn = -1.0f;
-                    float cos_s = fabsf(ux_s * nxn + uz_s * nzn);
-                    float cos_r = fabsf(ux_r * nxn + uz_r * nzn);
-                    float obl = sqrtf(fmaxf(0.0f, cos_s) * fmaxf(0.0f, cos_r));
-                    float R_s = fmaxf(ts[index] / S[index], EPSK);
-                    float R_r = fmaxf(tr[index] / S[index], EPSK);
-                    float G = 1.0f / sqrtf(R_s * R_r);
-                    float th_s = acosf(fminf(1.0f, fmaxf(-1.0f, ux_s * nxn + uz_s * nzn)));
-                    float th_r = acosf(fminf(1.0f, fmaxf(-1.0f, ux_r * nxn + uz_r * nzn)));
-                    float R = 1.0f + 0.2f * cosf(0.5f * (th_s + th_r));
-                    float scale_const = (float)(1.0f / (2.0f * ORC_PI));
-                    float sigma = tanf((float)(aperture * ORC_PI / 180.0f)) * z;
-                    float u = (x - cmp) / (sigma + EPSK);
-                    float taper = expf(-0.5f * u * u);
-                    float wgt = scale_const * Jterm * obl * G * R * taper;
+                    float wgt = orc_kweight(S, ts, tr, i, j, nzz, nb, dx, dz, aperture, cmp, NULL);
                     size_t mId = (size_t)(i - nb) + (size_t)(j - nb) * nz;
                     image[mId] = ftz(ftz(image[mId]) + ftz(wgt * trace[tId]));
                 }
         }
+}
+
+/* The least-squares variants' forward operators (image_domain_forward_kernel,
+ * migration.cu:485-570, nang = 0; angle_domain_forward_kernel, :665-756,
+ * nang > 0 with model = gathers nz x nang x ncmp): for every source, every
+ * receiver within max_offset, every cell with floor((Ts + Tr)/dt) in
+ * [0, nt) (and its reflection-angle bin in [0, nang)), trace sample += the
+ * FP32 product weight * model value. The reference adds with atomics in no
+ * fixed order; here each sample's terms are summed in FP64 and rounded once,
+ * an order-free value every FP32 summation order approximates. */
+void orc_kirchhoff_forward(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr, int nsrc,
+                           int nrec, const float* xsrc, const float* xrec, const float* model, int nt, float dt,
+                           float dx, float dz, float aperture, float max_offset, int nang, float da, float mincmp,
+                           float dcmp, float* data)
+{
+    size_t matsize = (size_t)nxx * nzz;
+    int nz = nzz - 2 * nb;
+    double* acc = (double*)malloc(sizeof(double) * (size_t)(nt > 0 ? nt : 1));
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            float* out = data + ((size_t)s * nrec + r) * nt;
+            for (int t = 0; t < nt; t++) out[t] = 0.0f;
+            float offset = fabsf(xsrc[s] - xrec[r]);
+            if (!(offset < max_offset)) continue;
+            float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            int cmpId = nang > 0 ? (int)((cmp - mincmp) / dcmp) : 0;
+            const float* ts = Ts + matsize * s;
+            const float* tr = Tr + matsize * r;
+            for (int t = 0; t < nt; t++) acc[t] = 0.0;
+            for (int j = nb; j < nxx - nb; j++)
+                for (int i = nb; i < nzz - nb; i++) {
+                    size_t index = (size_t)i + (size_t)j * nzz;
+                    float T = ts[index] + tr[index];
+                    int tId = (int)floorf(T / dt);
+                    if (tId < 0 || tId >= nt) continue;
+                    float ang = 0.0f;
+                    float wgt = orc_kweight(S, ts, tr, i, j, nzz, nb, dx, dz, aperture, cmp, nang > 0 ? &ang : NULL);
+                    size_t mId = (size_t)(i - nb) + (size_t)(j - nb) * nz;
+                    if (nang > 0) {
+                        int aId = (int)floorf(ang / da);
+                        if (aId < 0 || aId >= nang) continue;
+                        mId = (size_t)(i - nb) + (size_t)aId * nz + (size_t)cmpId * nang * nz;
+                    }
+                    acc[tId] += (double)ftz(wgt * model[mId]);
+                }
+            for (int t = 0; t < nt; t++) out[t] = (float)acc[t];
+        }
+    free(acc);
+}
+
+/* Migration::forward_convolution (migration.cu:230-261) without the FFT: the
+ * product A B of the zero-padded spectra and FFTW's unnormalised inverse are
+ * the linear convolution times nfft; out[t] = that at t + nw/2 + nw/10,
+ * summed directly in FP64 (m ascending). */
+void orc_forward_convolution(const float* in, float* out, int ntr, int nt, const float* w, int nw)
+{
+    int nfft = 1;
+    while (nfft < nt + nw - 1) nfft <<= 1;
+    int shift = nw / 2 + nw / 10;
+    for (int q = 0; q < ntr; q++) {
+        const float* a = in + (size_t)q * nt;
+        float* o = out + (size_t)q * nt;
+        for (int t = 0; t < nt; t++) {
+            int c = t + shift;
+            double acc = 0.0;
+            for (int m = (c - nt + 1 > 0 ? c - nt + 1 : 0); m < nw && m <= c; m++)
+                acc += (double)a[c - m] * (double)w[m];
+            o[t] = (float)(acc * (double)nfft);
+        }
+    }
 }

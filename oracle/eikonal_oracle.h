@@ -167,6 +167,11 @@ void orc_adjoint_convolution(const float* in, float* out, int ntr, int nt, const
 void orc_kirchhoff_image(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr, int nsrc,
                          int nrec, const float* xsrc, const float* xrec, const float* data, int nt, float dt,
                          float dx, float dz, float aperture, float max_offset, float* image);
+void orc_kirchhoff_forward(int nxx, int nzz, int nb, const float* S, const float* Ts, const float* Tr, int nsrc,
+                           int nrec, const float* xsrc, const float* xrec, const float* model, int nt, float dt,
+                           float dx, float dz, float aperture, float max_offset, int nang, float da, float mincmp,
+                           float dcmp, float* data);
+void orc_forward_convolution(const float* in, float* out, int ntr, int nt, const float* w, int nw);
 
 /* Arithmetic of the FP32 solvers: 0 = every operation rounded once and the
  * 3x3 initialisation in FP64 (default); 1 = the reference build's arithmetic:

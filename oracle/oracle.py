@@ -83,6 +83,10 @@ def lib():
         L.orc_kirchhoff_image.argtypes = [C.c_int, C.c_int, C.c_int, f32p, f32p, f32p, C.c_int, C.c_int, f32p,
                                           f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
                                           C.c_float, f32p]
+        L.orc_kirchhoff_forward.argtypes = [C.c_int, C.c_int, C.c_int, f32p, f32p, f32p, C.c_int, C.c_int, f32p,
+                                            f32p, f32p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                            C.c_float, C.c_int, C.c_float, C.c_float, C.c_float, f32p]
+        L.orc_forward_convolution.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p, C.c_int]
         L.orc_update_slowness.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
                                           f32p]
         _lib = L
@@ -337,6 +341,53 @@ def kirchhoff_image(S, Ts, Tr, xsrc, xrec, data, dt, dx, dz, aperture, max_offse
                               _f32(xsrc), _f32(xrec), d.ravel(), d.shape[-1], dt, dx, dz, aperture, max_offset,
                               img)
     return img
+
+
+def forward_convolution(traces, dt, fmax):
+    """Migration::forward_convolution of (ntr, nt) traces."""
+    a = _f32(traces)
+    w = kirchhoff_wavelet(fmax, dt)
+    out = np.zeros_like(a)
+    lib().orc_forward_convolution(a.ravel(), out.ravel(), a.shape[0], a.shape[1], w, len(w))
+    return out
+
+
+def angle_bins(xsrc, xrec, max_angle, da):
+    """(nang, ncmp, min CMP, CMP spacing) of Migration::set_gathers
+    (migration.cu:73-97), the largest CMP started from the first pair's."""
+    f32 = np.float32
+    xs, xr = _f32(xsrc), _f32(xrec)
+    d = f32(0.5) * min(f32(xs[1] - xs[0]), f32(xr[1] - xr[0]))
+    cmps = (f32(0.5) * (xs[:, None] + xr[None, :])).astype(np.float32)
+    mn, mx = f32(min(f32(1e6), cmps.min())), f32(cmps.max())
+    return int(f32(max_angle) / f32(da)) + 1, int(f32(mx - mn) / d) + 1, float(mn), float(d)
+
+
+def kirchhoff_image_forward(S, Ts, Tr, xsrc, xrec, image, nt, dt, dx, dz, aperture, max_offset, nb=3):
+    """Image-domain forward operator: image (nx, nz) -> traces (nsrc, nrec, nt),
+    each sample's terms summed in FP64 and rounded once."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    out = np.zeros((len(xsrc), len(xrec), int(nt)), np.float32)
+    lib().orc_kirchhoff_forward(nxx, nzz, nb, S, _f32(Ts).ravel(), _f32(Tr).ravel(), len(xsrc), len(xrec),
+                                _f32(xsrc), _f32(xrec), _f32(image).ravel(), int(nt), dt, dx, dz, aperture,
+                                max_offset, 0, 1.0, 0.0, 1.0, out)
+    return out
+
+
+def kirchhoff_angle_forward(S, Ts, Tr, xsrc, xrec, gathers, nt, dt, dx, dz, aperture, max_offset, max_angle, da,
+                            nb=3):
+    """Angle-domain forward operator: gathers (ncmp, nang, nz) -> traces."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    na, nc, mn, d = angle_bins(xsrc, xrec, max_angle, da)
+    g = _f32(gathers)
+    assert g.shape == (nc, na, nzz - 2 * nb), (g.shape, (nc, na, nzz - 2 * nb))
+    out = np.zeros((len(xsrc), len(xrec), int(nt)), np.float32)
+    lib().orc_kirchhoff_forward(nxx, nzz, nb, S, _f32(Ts).ravel(), _f32(Tr).ravel(), len(xsrc), len(xrec),
+                                _f32(xsrc), _f32(xrec), g.ravel(), int(nt), dt, dx, dz, aperture, max_offset, na, da,
+                                mn, d, out)
+    return out
 
 
 def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):

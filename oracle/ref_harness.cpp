@@ -329,3 +329,64 @@ extern "C" int ref_kirchhoff_angles(int nxx, int nzz, int nb, const float* S, co
     cuMemFree(dm);
     return 0;
 }
+
+// The least-squares variants' forward operators as LSKDM::compute_gradient
+// runs them (LSKDM.cu:52-90): per source, per receiver within max_offset, the
+// trace buffer zeroed, then one launch of image_domain_forward_kernel
+// (migration.cu:485-570; angle = 0, model nz x nx) or
+// angle_domain_forward_kernel (:665-756; angle = 1, model nz x na x ncmp,
+// cmpId = (cmp - mincmp) / dcmp). data (nsrc x nrec x nt) gets the raw
+// (unconvolved) traces; the other traces are 0.
+extern "C" int ref_kirchhoff_forward(int angle, int nxx, int nzz, int nb, const float* S, const float* Ts,
+                                     const float* Tr, int nsrc, int nrec, const float* xsrc, const float* xrec,
+                                     const float* model, size_t nmodel, int nt, float dt, float dx, float dz,
+                                     float aperture, float max_offset, float da, int na, float mincmp, float dcmp,
+                                     float* data)
+{
+    DR(cuCtxSetCurrent(g_ctx));
+    static CUfunction f_fimg = nullptr, f_fang = nullptr;
+    if (!f_fimg) {
+        const char* n1[] = {"_Z27image_domain_forward_kernelPfS_S_S_S_fiffiiiff", nullptr};
+        const char* n2[] = {"_Z27angle_domain_forward_kernelPfS_S_S_S_ffffiiiiiffi", nullptr};
+        DR(get_fn(g_mig, n1, &f_fimg));
+        DR(get_fn(g_mig, n2, &f_fang));
+    }
+    const size_t matsize = (size_t)nxx * nzz;
+    CUdeviceptr dS, dTs, dTr, dd, dm;
+    DR(cuMemAlloc(&dS, sizeof(float) * matsize));
+    DR(cuMemAlloc(&dTs, sizeof(float) * matsize * nsrc));
+    DR(cuMemAlloc(&dTr, sizeof(float) * matsize * nrec));
+    DR(cuMemAlloc(&dd, sizeof(float) * (size_t)nt));
+    DR(cuMemAlloc(&dm, sizeof(float) * nmodel));
+    DR(cuMemcpyHtoD(dS, S, sizeof(float) * matsize));
+    DR(cuMemcpyHtoD(dTs, Ts, sizeof(float) * matsize * nsrc));
+    DR(cuMemcpyHtoD(dTr, Tr, sizeof(float) * matsize * nrec));
+    DR(cuMemcpyHtoD(dm, model, sizeof(float) * nmodel));
+    const unsigned nblocks = (unsigned)((matsize + 255) / 256);
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            float* out = data + ((size_t)s * nrec + r) * nt;
+            for (int t = 0; t < nt; t++) out[t] = 0.0f;
+            if (!(fabsf(xsrc[s] - xrec[r]) < max_offset)) continue;
+            float cmp = 0.5f * (xsrc[s] + xrec[r]);
+            CUdeviceptr ts = dTs + sizeof(float) * matsize * s, tr = dTr + sizeof(float) * matsize * r;
+            DR(cuMemsetD32(dd, 0, (size_t)nt));
+            if (angle) {
+                int cmpId = (int)((cmp - mincmp) / dcmp);
+                void* args[] = {&dS, &ts, &tr, &dd, &dm, &dx, &dz, &dt, &da, &nxx, &nzz, &nt, &na, &nb, &aperture, &cmp,
+                                &cmpId};
+                DR(cuLaunchKernel(f_fang, nblocks, 1, 1, 256, 1, 1, 0, nullptr, args, nullptr));
+            } else {
+                void* args[] = {&dS, &ts, &tr, &dd, &dm, &dt, &nt, &dx, &dz, &nxx, &nzz, &nb, &aperture, &cmp};
+                DR(cuLaunchKernel(f_fimg, nblocks, 1, 1, 256, 1, 1, 0, nullptr, args, nullptr));
+            }
+            DR(cuCtxSynchronize());
+            DR(cuMemcpyDtoH(out, dd, sizeof(float) * (size_t)nt));
+        }
+    cuMemFree(dS);
+    cuMemFree(dTs);
+    cuMemFree(dTr);
+    cuMemFree(dd);
+    cuMemFree(dm);
+    return 0;
+}

@@ -130,3 +130,44 @@ def kirchhoff_angles(S_padded, Ts, Tr, xsrc, xrec, data, dt, dx, dz, aperture, m
     if rc != 0:
         raise RuntimeError(f"ref_kirchhoff_angles failed ({rc})")
     return g
+
+
+def kirchhoff_forward(S_padded, Ts, Tr, xsrc, xrec, model, nt, dt, dx, dz, aperture, max_offset, max_angle=None,
+                      da=None, nb=3):
+    """The reference's least-squares forward operator per trace
+    (LSKDM.cu:52-90) with its own image_domain_forward_kernel (model (nx, nz))
+    or, with max_angle and da, angle_domain_forward_kernel (model = gathers
+    (ncmp, nang, nz)); returns raw traces (nsrc, nrec, nt)."""
+    h = _handle()
+    if not getattr(h, "_kirch", False):
+        h.ref_kirchhoff_open.argtypes = [C.c_char_p]
+        if h.ref_kirchhoff_open(build_ref.cubin_path("migration").encode()) != 0:
+            raise RuntimeError("ref_kirchhoff_open failed")
+        h.ref_kirchhoff_adjoint.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_int] + \
+            [C.c_void_p] * 3 + [C.c_int] + [C.c_float] * 5 + [C.c_void_p]
+        h._kirch = True
+    h.ref_kirchhoff_forward.argtypes = [C.c_int] * 4 + [C.c_void_p] * 3 + [C.c_int, C.c_int] + [C.c_void_p] * 3 + \
+        [C.c_size_t, C.c_int] + [C.c_float] * 6 + [C.c_int, C.c_float, C.c_float, C.c_void_p]
+    xs = np.ascontiguousarray(xsrc, np.float32)
+    xr = np.ascontiguousarray(xrec, np.float32)
+    S = np.ascontiguousarray(S_padded, np.float32)
+    nxx, nzz = S.shape
+    m = np.ascontiguousarray(model, np.float32)
+    angle = max_angle is not None
+    na, mn, d = 0, 0.0, 1.0
+    if angle:
+        f32 = np.float32
+        d = f32(0.5) * min(f32(xs[1] - xs[0]), f32(xr[1] - xr[0]))
+        cmps = (f32(0.5) * (xs[:, None] + xr[None, :])).astype(np.float32)
+        mn = f32(min(f32(1e6), cmps.min()))
+        na = int(f32(max_angle) / f32(da)) + 1
+    out = np.zeros((len(xs), len(xr), int(nt)), np.float32)
+    Ts = np.ascontiguousarray(Ts, np.float32)
+    Tr = np.ascontiguousarray(Tr, np.float32)
+    rc = h.ref_kirchhoff_forward(1 if angle else 0, nxx, nzz, nb, S.ctypes.data, Ts.ctypes.data, Tr.ctypes.data,
+                                 len(xs), len(xr), xs.ctypes.data, xr.ctypes.data, m.ctypes.data, m.size, int(nt),
+                                 dt, dx, dz, aperture, max_offset, float(da or 1.0), na, float(mn), float(d),
+                                 out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"ref_kirchhoff_forward failed ({rc})")
+    return out

@@ -73,6 +73,12 @@ SIGNATURES = {
     "sf_kirchhoff_angle_gathers": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP, VP, VP, C.c_int, C.c_int,
                                              C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, VP, C.c_int,
                                              IP, IP, VP]),
+    "sf_forward_convolution": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, VP]),
+    "sf_kirchhoff_image_forward": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP, VP, VP, C.c_int, C.c_int,
+                                             C.c_float, C.c_float, C.c_float, VP, C.c_int, VP]),
+    "sf_kirchhoff_angle_forward": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP, VP, VP, C.c_int, C.c_int,
+                                             C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, VP, C.c_int,
+                                             VP]),
 }
 
 _lib = None

@@ -109,6 +109,7 @@ struct sf_ctx {
     float* d_mig = nullptr; size_t cap_mig = 0;
     float* d_kgeo = nullptr; size_t cap_kgeo = 0;
     int* d_kint = nullptr; size_t cap_kint = 0;
+    float* d_kpart = nullptr; size_t cap_kpart = 0;  // forward operator chunk partials
     std::vector<int> h_kint;
     std::vector<double> h_wav;
     std::vector<float> h_kgeo;

@@ -231,6 +231,162 @@ __global__ void k_kirchhoff_angles(AngleParams p)
     }
 }
 
+// The trace-independent part of one cell's weight, as the reference's four
+// Kirchhoff kernels compute it (migration.cu:418-466, :505-553, :592-640,
+// :685-733), from both tables' terms at the cell; sigma = tan(aperture) z.
+__device__ __forceinline__ float kirchhoff_weight(const TableTerms& ts, const TableTerms& tr, float Tsc, float Trc,
+                                                  float Sc, float x, float cmp, float sigma)
+{
+    const float Jterm = sqrtf(ts.detH * tr.detH) * Sc / (ts.norm * tr.norm);
+    const float ux_s = ts.dx1 / ts.norm, uz_s = ts.dz1 / ts.norm;
+    const float ux_r = tr.dx1 / tr.norm, uz_r = tr.dz1 / tr.norm;
+    const float nx_norm = 0.0f, nz_norm = -1.0f;
+    const float cos_s = fabs(ux_s * nx_norm + uz_s * nz_norm);
+    const float cos_r = fabs(ux_r * nx_norm + uz_r * nz_norm);
+    const float obliquity = sqrt(max(0.0f, cos_s) * max(0.0f, cos_r));
+    const float R_s = max(Tsc / Sc, kEps);
+    const float R_r = max(Trc / Sc, kEps);
+    const float G = 1.0f / sqrt(R_s * R_r);
+    const float theta_s = acosf(min(1.0f, max(-1.0f, ux_s * nx_norm + uz_s * nz_norm)));
+    const float theta_r = acosf(min(1.0f, max(-1.0f, ux_r * nx_norm + uz_r * nz_norm)));
+    const float theta = 0.5f * (theta_s + theta_r);
+    const float R = 1.0f + 0.2f * cosf(theta);
+    const float scale_const = 1.0f / (2.0f * M_PI);
+    const float taper = expf(-0.5f * ((x - cmp) / (sigma + kEps)) * ((x - cmp) / (sigma + kEps)));
+    return scale_const * Jterm * obliquity * G * R * taper;
+}
+
+struct KirchFwdParams {
+    const float* S;
+    const float* Ts;
+    const float* Tr;
+    const float* xs;
+    const float* xr;
+    const float* model;  // image (nz x nx) or angle gathers (nz x nang x ncmp)
+    const int* trace;    // work trace e -> s * nrec + r, in trace order
+    const int* cmp;      // work trace e -> CMP bin (angle domain)
+    float* part;         // ntrace x nchunk x nt partial traces (nchunk > 1)
+    float* data;         // nsrc x nrec x nt
+    int nchunk, chunk, nrec, nt, nxx, nzz, nb, nang, warps;
+    float dt, dx, dz, da, aperture;
+};
+
+// The forward (demigration) operator of the least-squares variants:
+// image_domain_forward_kernel / angle_domain_forward_kernel
+// (migration.cu:485-570, :665-756) add weight * model[cell] to sample
+// floor((Ts + Tr)/dt) of the trace with a global atomicAdd per cell, in no
+// fixed order. Here one CTA takes one chunk of one trace's cells. Each warp
+// walks 32 consecutive cells (z fastest) at a time; lanes that hit the same
+// sample are summed in lane order and the sum is added to the warp's own
+// histogram of the trace in shared memory (one adder per sample, no
+// atomics). The warps' histograms are summed in warp order, the chunks in
+// chunk order: a fixed order that depends only on the sizes, so the traces
+// are reproducible bit for bit.
+template <bool ANGLE>
+__global__ void k_kirchhoff_forward(KirchFwdParams p)
+{
+    extern __shared__ float smem[];
+    const int W = p.warps, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* hist = smem + (size_t)warp * p.nt;
+    int* st_t = reinterpret_cast<int*>(smem + (size_t)W * p.nt) + warp * 32;
+    float* st_v = smem + (size_t)W * p.nt + W * 32 + warp * 32;
+    for (int q = threadIdx.x; q < W * p.nt; q += blockDim.x) smem[q] = 0.0f;
+    __syncthreads();
+    const int e = blockIdx.x / p.nchunk, ck = blockIdx.x % p.nchunk;
+    const int tid = p.trace[e], s = tid / p.nrec, r = tid % p.nrec;
+    const float cmp = 0.5f * (p.xs[s] + p.xr[r]);
+    const int cmpId = ANGLE ? p.cmp[e] : 0;
+    const size_t matsize = (size_t)p.nzz * p.nxx;
+    const float* Ts = p.Ts + matsize * s;
+    const float* Tr = p.Tr + matsize * r;
+    const int nz = p.nzz - 2 * p.nb;
+    const long ncell = (long)nz * (p.nxx - 2 * p.nb);
+    const long m0 = (long)ck * p.chunk, m1 = min(m0 + (long)p.chunk, ncell);
+    for (long g = m0 + 32L * warp; g < m1; g += 32L * W) {
+        const long m = g + lane;
+        int tq = -1;
+        float v = 0.0f;
+        if (m < m1) {
+            const int i = (int)(m % nz) + p.nb, j = (int)(m / nz) + p.nb;
+            const size_t index = (size_t)i + (size_t)j * p.nzz;
+            const float T = Ts[index] + Tr[index];
+            const int tId = __float2int_rd(T / p.dt);
+            if (tId >= 0 && tId < p.nt) {
+                const float z = __int2float_rd(i - p.nb) * p.dz;
+                const float x = __int2float_rd(j - p.nb) * p.dx;
+                const float sigma = tanf(p.aperture * M_PI / 180.0f) * z;
+                const TableTerms ts = table_terms(Ts, i, j, p.nzz, p.dx, p.dz);
+                const TableTerms tr = table_terms(Tr, i, j, p.nzz, p.dx, p.dz);
+                const float weights = kirchhoff_weight(ts, tr, Ts[index], Tr[index], p.S[index], x, cmp, sigma);
+                if (ANGLE) {
+                    const float reflection_angle =
+                        0.5f * acos((ts.dx1 * tr.dx1 + ts.dz1 * tr.dz1) / (ts.norm * tr.norm));
+                    const float ang = 180.0f * reflection_angle / M_PI;
+                    const int aId = __float2int_rd(ang / p.da);
+                    if (aId >= 0 && aId < p.nang) {
+                        const size_t mId = (size_t)(i - p.nb) + (size_t)aId * nz + (size_t)cmpId * p.nang * nz;
+                        v = __fmul_rn(weights, p.model[mId]);
+                        tq = tId;
+                    }
+                } else {
+                    v = __fmul_rn(weights, p.model[m]);
+                    tq = tId;
+                }
+            }
+        }
+        st_t[lane] = tq;
+        st_v[lane] = v;
+        __syncwarp();
+        const unsigned grp = __match_any_sync(0xffffffffu, tq);
+        if (tq >= 0 && lane == __ffs(grp) - 1) {
+            float sum = v;
+            for (unsigned rest = grp & (grp - 1); rest; rest &= rest - 1) sum = add_ftz(sum, st_v[__ffs(rest) - 1]);
+            hist[tq] = add_ftz(hist[tq], sum);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    float* out = (p.nchunk == 1) ? p.data + (size_t)tid * p.nt : p.part + ((size_t)e * p.nchunk + ck) * p.nt;
+    for (int t = threadIdx.x; t < p.nt; t += blockDim.x) {
+        float a = smem[t];
+        for (int w = 1; w < W; w++) a = add_ftz(a, smem[(size_t)w * p.nt + t]);
+        out[t] = a;
+    }
+}
+
+// Chunk partials of each work trace summed in chunk order.
+__global__ void k_sum_chunks(const float* __restrict__ part, const int* __restrict__ trace, float* __restrict__ data,
+                             int ntrace, int nchunk, int nt)
+{
+    const size_t n = (size_t)ntrace * nt;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const int e = (int)(q / nt), t = (int)(q % nt);
+        const float* pp = part + (size_t)e * nchunk * nt + t;
+        float a = pp[0];
+        for (int c = 1; c < nchunk; c++) a = add_ftz(a, pp[(size_t)c * nt]);
+        data[(size_t)trace[e] * nt + t] = a;
+    }
+}
+
+// Convolution of each trace with the wavelet as the reference's FFT product
+// A B with FFTW's unnormalised inverse gives it (Migration::
+// forward_convolution, migration.cu:230-261): for output sample t,
+// nfft * sum_m trace[t + shift - m] * w[m] over the samples inside the trace,
+// in FP64 (m ascending), rounded once to FP32.
+__global__ void k_convolve(const float* __restrict__ in, float* __restrict__ out, int ntr, int nt,
+                           const double* __restrict__ w, int nw, int shift, double nfft)
+{
+    const size_t n = (size_t)ntr * nt;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const int t = (int)(q % nt);
+        const float* a = in + (q - t);
+        const int c = t + shift;
+        double acc = 0.0;
+        for (int m = max(0, c - nt + 1); m < nw && m <= c; m++) acc = __dadd_rn(acc, __dmul_rn((double)a[c - m], w[m]));
+        out[q] = __double2float_rn(__dmul_rn(acc, nfft));
+    }
+}
+
 }  // namespace
 
 // Migration::set_wavelet (migration.cu:54-71) as its source computes it.
@@ -254,8 +410,10 @@ static int next_pow2(int n)
     return p;
 }
 
-extern "C" int sf_adjoint_convolution(sf_ctx* c, const float* traces, float* out, int ntr, int nt, float dt,
-                                      float fmax, int mem, void* stream)
+// The wavelet correlation (forward = false) or convolution (forward = true)
+// of ntr traces, as Migration::adjoint_convolution / forward_convolution.
+static int wavelet_filter(sf_ctx* c, const float* traces, float* out, int ntr, int nt, float dt, float fmax, int mem,
+                          void* stream, bool forward)
 {
     if (!c || !traces || !out || ntr < 0 || nt < 1 || !(dt > 0.0f) || !(fmax > 0.0f))
         return sf_fail(c, SF_ERR_ARG, "bad convolution arguments");
@@ -280,8 +438,12 @@ extern "C" int sf_adjoint_convolution(sf_ctx* c, const float* traces, float* out
     }
     const size_t n = (size_t)ntr * nt;
     if (n) {
-        k_correlate<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->sms * 16), 256, 0, st>>>(
-            din, dout, ntr, nt, c->d_wav, nw, nw / 2 + nw / 10, (double)next_pow2(nt + nw - 1));
+        const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->sms * 16);
+        const double nfft = (double)next_pow2(nt + nw - 1);
+        if (forward)
+            k_convolve<<<grid, 256, 0, st>>>(din, dout, ntr, nt, c->d_wav, nw, nw / 2 + nw / 10, nfft);
+        else
+            k_correlate<<<grid, 256, 0, st>>>(din, dout, ntr, nt, c->d_wav, nw, nw / 2 + nw / 10, nfft);
         CK(cudaGetLastError());
     }
     if (mem == SF_MEM_HOST) {
@@ -289,6 +451,18 @@ extern "C" int sf_adjoint_convolution(sf_ctx* c, const float* traces, float* out
         CK(cudaStreamSynchronize(st));
     }
     return SF_OK;
+}
+
+extern "C" int sf_adjoint_convolution(sf_ctx* c, const float* traces, float* out, int ntr, int nt, float dt,
+                                      float fmax, int mem, void* stream)
+{
+    return wavelet_filter(c, traces, out, ntr, nt, dt, fmax, mem, stream, false);
+}
+
+extern "C" int sf_forward_convolution(sf_ctx* c, const float* traces, float* out, int ntr, int nt, float dt,
+                                      float fmax, int mem, void* stream)
+{
+    return wavelet_filter(c, traces, out, ntr, nt, dt, fmax, mem, stream, true);
 }
 
 extern "C" int sf_kirchhoff_image(sf_ctx* c, const float* Ts, const float* Tr, int nsrc, int nrec, const float* xsrc,
@@ -452,4 +626,145 @@ extern "C" int sf_kirchhoff_angle_gathers(sf_ctx* c, const float* Ts, const floa
         CK(cudaStreamSynchronize(st));
     }
     return SF_OK;
+}
+
+// Shared memory of one forward CTA: per warp a histogram of nt samples and 32
+// staged (sample, term) pairs.
+constexpr size_t kFwdSmem = 200 * 1024;
+// Work traces times chunks the forward aims at when traces are few; a fixed
+// number, so the summation order depends on the sizes only.
+constexpr long kFwdCtas = 2432;
+
+// The forward operator over the pairs LSKDM::compute_gradient and
+// compute_stepLength visit (LSKDM.cu:52-90, :168-201): every source, every
+// receiver with |xsrc - xrec| < max_offset, in that order; the other traces
+// of data are zero.
+static int kirchhoff_forward(sf_ctx* c, bool angle, const float* Ts, const float* Tr, int nsrc, int nrec,
+                             const float* xsrc, const float* xrec, const float* model, int model_mem, size_t nmodel,
+                             int nt, float dt, float aperture, float max_offset, int nang, int ncmp, float mincmp,
+                             float dcmp, float da, float* data, int data_mem, void* stream)
+{
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<int> ids, bins;
+    for (int s = 0; s < nsrc; s++)
+        for (int r = 0; r < nrec; r++) {
+            if (!(fabsf(xsrc[s] - xrec[r]) < max_offset)) continue;
+            if (angle) {
+                const float cmp = 0.5f * (xsrc[s] + xrec[r]);
+                const int b = (int)((cmp - mincmp) / dcmp);
+                if (b < 0 || b >= ncmp) continue;
+                bins.push_back(b);
+            }
+            ids.push_back(s * nrec + r);
+        }
+    const int ntrace = (int)ids.size();
+    const size_t per_warp = (size_t)nt * sizeof(float) + 64 * sizeof(float);
+    const int W = (int)std::min<size_t>(8, kFwdSmem / per_warp);
+    if (W < 1) return sf_fail(c, SF_ERR_RANGE, "too many time samples for the forward operator");
+    const int nz = c->nzz - 2 * c->nb;
+    const long ncell = (long)nz * (c->nxx - 2 * c->nb);
+    const int nchunk = (int)std::max<long>(
+        1, std::min<long>((kFwdCtas + std::max(ntrace, 1) - 1) / std::max(ntrace, 1), (ncell + 4095) / 4096));
+    const int chunk = (int)((ncell + nchunk - 1) / nchunk);
+    const size_t nd = (size_t)nsrc * nrec * nt;
+    c->h_kgeo.assign(xsrc, xsrc + nsrc);
+    c->h_kgeo.insert(c->h_kgeo.end(), xrec, xrec + nrec);
+    c->h_kint.assign(ids.begin(), ids.end());
+    c->h_kint.insert(c->h_kint.end(), bins.begin(), bins.end());
+    int rc = sf_dev_reserve(c, (void**)&c->d_kgeo, &c->cap_kgeo, c->h_kgeo.size() * sizeof(float));
+    if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_kint, &c->cap_kint, std::max<size_t>(1, c->h_kint.size()) * sizeof(int));
+    if (!rc && (model_mem == SF_MEM_HOST || data_mem == SF_MEM_HOST))
+        rc = sf_dev_reserve(c, (void**)&c->d_mig, &c->cap_mig, (nd + nmodel) * sizeof(float));
+    if (!rc && nchunk > 1)
+        rc = sf_dev_reserve(c, (void**)&c->d_kpart, &c->cap_kpart, (size_t)ntrace * nchunk * nt * sizeof(float));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->d_kgeo, c->h_kgeo.data(), c->h_kgeo.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    if (!c->h_kint.empty())
+        CK(cudaMemcpyAsync(c->d_kint, c->h_kint.data(), c->h_kint.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    const float* dm = model;
+    float* dd = data;
+    if (model_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(c->d_mig + nd, model, nmodel * sizeof(float), cudaMemcpyHostToDevice, st));
+        dm = c->d_mig + nd;
+    }
+    if (data_mem == SF_MEM_HOST) dd = c->d_mig;
+    CK(cudaMemsetAsync(dd, 0, nd * sizeof(float), st));
+    if (ntrace > 0) {
+        KirchFwdParams p;
+        p.S = c->d_S;
+        p.Ts = Ts;
+        p.Tr = Tr;
+        p.xs = c->d_kgeo;
+        p.xr = c->d_kgeo + nsrc;
+        p.model = dm;
+        p.trace = c->d_kint;
+        p.cmp = c->d_kint + ntrace;
+        p.part = c->d_kpart;
+        p.data = dd;
+        p.nchunk = nchunk;
+        p.chunk = chunk;
+        p.nrec = nrec;
+        p.nt = nt;
+        p.nxx = c->nxx;
+        p.nzz = c->nzz;
+        p.nb = c->nb;
+        p.nang = nang;
+        p.warps = W;
+        p.dt = dt;
+        p.dx = c->dx;
+        p.dz = c->dz;
+        p.da = da;
+        p.aperture = aperture;
+        const size_t smem = (size_t)W * per_warp;
+        const unsigned grid = (unsigned)((long)ntrace * nchunk);
+        if (angle) {
+            CK(cudaFuncSetAttribute(k_kirchhoff_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_kirchhoff_forward<true><<<grid, 32 * W, smem, st>>>(p);
+        } else {
+            CK(cudaFuncSetAttribute(k_kirchhoff_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+            k_kirchhoff_forward<false><<<grid, 32 * W, smem, st>>>(p);
+        }
+        CK(cudaGetLastError());
+        if (nchunk > 1) {
+            const size_t n = (size_t)ntrace * nt;
+            k_sum_chunks<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->sms * 16), 256, 0, st>>>(
+                c->d_kpart, c->d_kint, dd, ntrace, nchunk, nt);
+            CK(cudaGetLastError());
+        }
+    }
+    if (data_mem == SF_MEM_HOST) {
+        CK(cudaMemcpyAsync(data, dd, nd * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return SF_OK;
+}
+
+extern "C" int sf_kirchhoff_image_forward(sf_ctx* c, const float* Ts, const float* Tr, int nsrc, int nrec,
+                                          const float* xsrc, const float* xrec, const float* image, int image_mem,
+                                          int nt, float dt, float aperture, float max_offset, float* data,
+                                          int data_mem, void* stream)
+{
+    if (!c || !Ts || !Tr || !xsrc || !xrec || !image || !data || nsrc < 1 || nrec < 1 || nt < 1 || !(dt > 0.0f))
+        return sf_fail(c, SF_ERR_ARG, "bad Kirchhoff arguments");
+    return kirchhoff_forward(c, false, Ts, Tr, nsrc, nrec, xsrc, xrec, image, image_mem, (size_t)c->nx * c->nz, nt,
+                             dt, aperture, max_offset, 0, 0, 0.0f, 1.0f, 1.0f, data, data_mem, stream);
+}
+
+extern "C" int sf_kirchhoff_angle_forward(sf_ctx* c, const float* Ts, const float* Tr, int nsrc, int nrec,
+                                          const float* xsrc, const float* xrec, const float* gathers,
+                                          int gathers_mem, int nt, float dt, float aperture, float max_offset,
+                                          float max_angle, float da, float* data, int data_mem, void* stream)
+{
+    if (!c || !xsrc || !xrec) return sf_fail(c, SF_ERR_ARG, "null argument");
+    int nang, ncmp;
+    float mincmp, dcmp;
+    if (angle_dims(xsrc, nsrc, xrec, nrec, max_angle, da, &nang, &ncmp, &mincmp, &dcmp))
+        return sf_fail(c, SF_ERR_ARG, "angle gathers need two sources, two receivers, increasing positions, da > 0");
+    if (!Ts || !Tr || !gathers || !data || nt < 1 || !(dt > 0.0f))
+        return sf_fail(c, SF_ERR_ARG, "bad Kirchhoff arguments");
+    const size_t ng = (size_t)(c->nzz - 2 * c->nb) * nang * ncmp;
+    return kirchhoff_forward(c, true, Ts, Tr, nsrc, nrec, xsrc, xrec, gathers, gathers_mem, ng, nt, dt, aperture,
+                             max_offset, nang, ncmp, mincmp, dcmp, da, data, data_mem, stream);
 }

@@ -263,6 +263,54 @@ class Engine:
                     "sf_kirchhoff_angle_gathers")
         return out
 
+    def forward_convolution(self, traces, dt, fmax, out=None, stream=None):
+        """The reference's wavelet convolution (Migration::forward_convolution)
+        of (ntr, nt) traces."""
+        pi, mem, k1 = _ptr(traces)
+        shape = tuple(traces.shape)
+        if out is None:
+            out = np.zeros(shape, np.float32)
+        po, _, k2 = _ptr(out)
+        self._check(self.L.sf_forward_convolution(self._ctx, pi, po, int(shape[0]), int(shape[1]), float(dt),
+                                                  float(fmax), mem, _stream_ptr(stream)), "sf_forward_convolution")
+        return out
+
+    def kirchhoff_image_forward(self, Ts, Tr, xsrc, xrec, image, nt, dt, aperture, max_offset, out=None,
+                                stream=None):
+        """Image-domain Kirchhoff forward operator (the least-squares
+        variant's demigration): image (nx, nz) -> traces (nsrc, nrec, nt)."""
+        xs = np.ascontiguousarray(xsrc, np.float32)
+        xr = np.ascontiguousarray(xrec, np.float32)
+        pm, mmem, k1 = _ptr(image)
+        if out is None:
+            out = np.zeros((len(xs), len(xr), int(nt)), np.float32)
+        po, omem, k2 = _ptr(out)
+        self._check(self.L.sf_kirchhoff_image_forward(self._ctx, self._dev_ptr(Ts, "Ts"), self._dev_ptr(Tr, "Tr"),
+                                                      len(xs), len(xr), C.c_void_p(xs.ctypes.data),
+                                                      C.c_void_p(xr.ctypes.data), pm, mmem, int(nt), float(dt),
+                                                      float(aperture), float(max_offset), po, omem,
+                                                      _stream_ptr(stream)),
+                    "sf_kirchhoff_image_forward")
+        return out
+
+    def kirchhoff_angle_forward(self, Ts, Tr, xsrc, xrec, gathers, nt, dt, aperture, max_offset, max_angle, da,
+                                out=None, stream=None):
+        """Angle-domain Kirchhoff forward operator: gathers (ncmp, nang, nz)
+        -> traces (nsrc, nrec, nt)."""
+        xs = np.ascontiguousarray(xsrc, np.float32)
+        xr = np.ascontiguousarray(xrec, np.float32)
+        pm, mmem, k1 = _ptr(gathers)
+        if out is None:
+            out = np.zeros((len(xs), len(xr), int(nt)), np.float32)
+        po, omem, k2 = _ptr(out)
+        self._check(self.L.sf_kirchhoff_angle_forward(self._ctx, self._dev_ptr(Ts, "Ts"), self._dev_ptr(Tr, "Tr"),
+                                                      len(xs), len(xr), C.c_void_p(xs.ctypes.data),
+                                                      C.c_void_p(xr.ctypes.data), pm, mmem, int(nt), float(dt),
+                                                      float(aperture), float(max_offset), float(max_angle),
+                                                      float(da), po, omem, _stream_ptr(stream)),
+                    "sf_kirchhoff_angle_forward")
+        return out
+
     # -------------------------------------------------------- planned batches
     def plan_batch(self, shots, rx, rz, stream=None):
         """Fix an isotropic batch (shots as for batch_forward) for

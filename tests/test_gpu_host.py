@@ -49,6 +49,9 @@ mig_max_offset = 600
 mig_data_folder = {d}/
 mig_data_prefix = mig_shot_
 mig_seismic_folder = {d}/
+mig_max_iteration = 3
+mig_residuo_folder = {d}/
+mig_smooth_lambda = 0.5
 """
 
 
@@ -213,3 +216,117 @@ def test_migration_exe_matches_engine(cuda, exes, tmp_path, migtype):
         img = np.fromfile(os.path.join(d, f"ADKDM_result_{nz}x{nc}x{na}.bin"), np.float32).reshape(ref.shape)
     assert np.abs(ref).max() > 0
     assert np.array_equal(img, ref)
+
+
+def _seq_sum(acc, x):
+    """FP32 running sum in index order, as the reference's host loops add."""
+    return np.cumsum(np.concatenate([[np.float32(acc)], np.ravel(x).astype(np.float32)]), dtype=np.float32)[-1]
+
+
+def least_squares_mirror(e, Ts, Tr, xs, xr, dobs, dt, fmax, aperture, max_off, max_it, angle=False, max_ang=0.0,
+                         da=1.0, smooth=0.0):
+    """LSKDM (LSKDM.cu:3-235) step by step on the engine's operators: FP32
+    host vectors, sums in the reference's order."""
+    f32 = np.float32
+    EPS = f32(1e-6)
+    ns, nr, nt = dobs.shape
+    inside = np.abs(xs[:, None] - xr[None, :]) < max_off
+
+    def F(model):
+        if angle:
+            tr = e.kirchhoff_angle_forward(Ts, Tr, xs, xr, model, nt, dt, aperture, max_off, max_ang, da)
+        else:
+            tr = e.kirchhoff_image_forward(Ts, Tr, xs, xr, model, nt, dt, aperture, max_off)
+        return e.forward_convolution(tr.reshape(-1, nt), dt, fmax).reshape(tr.shape)
+
+    def Ft(res):
+        c = e.adjoint_convolution(res.reshape(-1, nt), dt, fmax).reshape(res.shape)
+        if angle:
+            return e.kirchhoff_angle_gathers(Ts, Tr, xs, xr, c, dt, aperture, max_off, max_ang, da)
+        return e.kirchhoff_image(Ts, Tr, xs, xr, c, dt, aperture, max_off)
+
+    shape = Ft(np.zeros_like(dobs)).shape
+    model = np.zeros(shape, f32)
+    direction = np.zeros(shape, f32)
+    gold = np.zeros(shape, f32)
+    residuo, it = [], 0
+    while True:
+        pred = F(model)
+        res = np.where(np.abs(dobs) > EPS, dobs - pred, f32(0)).astype(f32)
+        res[~inside] = 0
+        acc = f32(0)
+        for s in range(ns):
+            for r in range(nr):
+                if inside[s, r]:
+                    acc = _seq_sum(acc, res[s, r] * res[s, r])
+        g = Ft(res)
+        it += 1
+        residuo.append(np.sqrt(acc))
+        if it > max_it:
+            break
+        beta = f32(_seq_sum(0, g * g) / f32(_seq_sum(0, gold * gold) + EPS))
+        direction = (g + beta * direction).astype(f32)
+        alpha_num = _seq_sum(0, g * direction)
+        gold = g.copy()
+        Fd = F(direction)
+        aden = f32(0)
+        for s in range(ns):
+            for r in range(nr):
+                if inside[s, r]:
+                    aden = _seq_sum(aden, Fd[s, r] * Fd[s, r])
+        alpha = f32(alpha_num / f32(aden + EPS))
+        if angle:
+            na = shape[1]
+            fw = np.concatenate([model[:, 1:], model[:, -2:-1]], axis=1)
+            bw = np.concatenate([model[:, 1:2], model[:, :-1]], axis=1)
+            lap = ((fw - f32(2) * model) + bw).astype(f32)
+            direction = (direction + (f32(smooth) * lap) / f32(f32(da) * f32(da))).astype(f32)
+        model = (model + alpha * direction).astype(f32)
+    return model, np.array(residuo, np.float32)
+
+
+@pytest.mark.parametrize("migtype", [2, 3])
+def test_migration_exe_least_squares(cuda, exes, tmp_path, migtype):
+    """migration.exe with mig_type 2 (IDLSKDM) / 3 (ADLSKDM) writes what the
+    reference's least-squares loop gives on the engine's operators, and the
+    residual norm falls."""
+    from seisfat2d_gb300 import Engine
+    nx, nz, dx, dz = 60, 25, 10.0, 10.0
+    m = smooth_model(nx, nz, dx, seed=21)
+    shots = [(100.0, 0.0), (300.0, 0.0), (480.0, 0.0)]
+    recs = [(float(x), 0.0) for x in range(0, 590, 40)]
+    d = str(tmp_path)
+    p = write_case(d, nx, nz, dx, dz, m, shots, recs, migtype=migtype)
+    e = Engine(nx, nz, dx, dz)
+    e.set_slowness(m)
+    dev = cuda.device("cuda", 0)
+    tabs = []
+    for pts in (shots, recs):
+        e.batch_forward(pts, np.zeros(0, np.float32), np.zeros(0, np.float32), keep_tables=True)
+        t = cuda.empty((len(pts), e.nxx, e.nzz), dtype=cuda.float32, device=dev)
+        for k in range(len(pts)):
+            e.batch_table(k, e.nxx, out=t[k])
+        tabs.append(t)
+    xs = np.array([s[0] for s in shots], np.float32)
+    xr = np.array([r[0] for r in recs], np.float32)
+    # observed traces: a two-reflector image through the forward operator
+    refl = np.zeros((nx, nz), np.float32)
+    refl[:, 10] = 1.0
+    refl[:, 18] = -0.5
+    raw = e.kirchhoff_image_forward(tabs[0], tabs[1], xs, xr, refl, 400, 2e-3, 35.0, 600.0)
+    dobs = e.forward_convolution(raw.reshape(-1, 400), 2e-3, 25.0).reshape(raw.shape)
+    for k in range(len(shots)):
+        dobs[k].tofile(os.path.join(d, f"mig_shot_{k + 1}.bin"))
+    run(exes["migration.exe"], p)
+    angle = migtype == 3
+    model, res = least_squares_mirror(e, tabs[0], tabs[1], xs, xr, dobs, 2e-3, 25.0, 35.0, 600.0, 3, angle=angle,
+                                      max_ang=60.0, da=2.0, smooth=0.5)
+    name = "ADLSKDM" if angle else "IDLSKDM"
+    dims = f"{nz}x{model.shape[0]}x{model.shape[1]}" if angle else f"{nz}x{nx}"
+    out = np.fromfile(os.path.join(d, f"{name}_result_{dims}_iteration_3.bin"), np.float32).reshape(model.shape)
+    conv = np.loadtxt(os.path.join(d, f"{name}_convergence_3_iterations.txt"))
+    print(name, "residual norms", conv)
+    assert len(conv) == 4 and conv[-1] < conv[0]
+    assert np.allclose(conv, res, rtol=1e-5)
+    assert np.abs(model).max() > 0
+    assert np.array_equal(out, model)

@@ -329,3 +329,76 @@ def test_kirchhoff_image_is_linear_in_the_traces(oracle):
     assert np.array_equal(b, 2 * a)
     c = oracle.kirchhoff_image(S, Ts, Tr, xs, xr, d, 0.001, 10.0, 10.0, 30.0, 50.0)  # offset cut
     assert not np.array_equal(a, c)
+
+
+def test_kirchhoff_forward_convolution_matches_fft_form(oracle):
+    """The direct FP64 convolution restates Migration::forward_convolution
+    (migration.cu:230-261): zero-padded FFT, product A B, unnormalised
+    inverse, output sample t read at t + nw/2 + nw/10."""
+    dt, fmax, nt = 0.002, 25.0, 300
+    w = oracle.kirchhoff_wavelet(fmax, dt)
+    nw = len(w)
+    tr = np.random.default_rng(6).standard_normal((3, nt)).astype(np.float32)
+    got = oracle.forward_convolution(tr, dt, fmax)
+    nfft = 1
+    while nfft < nt + nw - 1:
+        nfft *= 2
+    W = np.fft.rfft(np.concatenate([w.astype(np.float64), np.zeros(nfft - nw)]))
+    shift = nw // 2 + nw // 10
+    for q in range(3):
+        A = np.fft.rfft(np.concatenate([tr[q].astype(np.float64), np.zeros(nfft - nt)]))
+        c = np.fft.irfft(A * W, nfft) * nfft
+        ref = c[shift:shift + nt]
+        assert np.allclose(got[q], ref.astype(np.float32), rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+
+
+def _kirchhoff_case(oracle, seed=2, nx=24, nz=16):
+    rng = np.random.default_rng(seed)
+    S = oracle.expand_boundary((1.0 / rng.uniform(1800, 2500, (nx, nz))).astype(np.float32))
+    xs = np.array([60.0, 150.0], np.float32)
+    xr = np.array([30.0, 90.0, 170.0], np.float32)
+    Ts = np.stack([oracle.solve_f32(S, 10.0, 10.0, float(x), 0.0) for x in xs])
+    Tr = np.stack([oracle.solve_f32(S, 10.0, 10.0, float(x), 0.0) for x in xr])
+    return rng, S, xs, xr, Ts, Tr
+
+
+def test_kirchhoff_forward_is_the_adjoint_of_the_image(oracle):
+    """<F m, d> = <m, F^T d> for the image-domain forward operator (the
+    least-squares variant's demigration, migration.cu:485-570) and the
+    migration kernel (:398-483): the same weights and samples."""
+    rng, S, xs, xr, Ts, Tr = _kirchhoff_case(oracle)
+    nt, dt = 200, 0.001
+    m = rng.standard_normal((S.shape[0] - 6, S.shape[1] - 6)).astype(np.float32)
+    d = rng.standard_normal((2, 3, nt)).astype(np.float32)
+    Fm = oracle.kirchhoff_image_forward(S, Ts, Tr, xs, xr, m, nt, dt, 10.0, 10.0, 30.0, 1000.0)
+    Ftd = oracle.kirchhoff_image(S, Ts, Tr, xs, xr, d, dt, 10.0, 10.0, 30.0, 1000.0)
+    lhs = float(np.dot(Fm.ravel().astype(np.float64), d.ravel()))
+    rhs = float(np.dot(m.ravel().astype(np.float64), Ftd.ravel()))
+    assert abs(Fm).max() > 0
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+    # traces beyond max_offset stay zero
+    cut = oracle.kirchhoff_image_forward(S, Ts, Tr, xs, xr, m, nt, dt, 10.0, 10.0, 30.0, 50.0)
+    far = np.abs(xs[:, None] - xr[None, :]) >= 50.0
+    assert not cut[far].any() and cut[~far].any()
+
+
+def test_kirchhoff_angle_forward_bins(oracle):
+    """Angle-domain forward operator: a gather that is one in a single
+    (CMP, angle) bin and zero elsewhere feeds only the traces of that CMP;
+    the sum over all bins equals the image-domain operator on an image of
+    ones (every cell lands in exactly one angle bin below max_angle)."""
+    rng, S, xs, xr, Ts, Tr = _kirchhoff_case(oracle, seed=4)
+    nt, dt = 200, 0.001
+    na, nc, mn, dcmp = oracle.angle_bins(xs, xr, 90.0, 2.0)
+    nz = S.shape[1] - 6
+    ones = np.ones((nc, na, nz), np.float32)
+    a = oracle.kirchhoff_angle_forward(S, Ts, Tr, xs, xr, ones, nt, dt, 10.0, 10.0, 30.0, 1000.0, 90.0, 2.0)
+    img = oracle.kirchhoff_image_forward(S, Ts, Tr, xs, xr, np.ones((S.shape[0] - 6, nz), np.float32), nt, dt,
+                                         10.0, 10.0, 30.0, 1000.0)
+    assert np.abs(a).max() > 0
+    assert np.allclose(a, img, rtol=1e-5, atol=1e-6 * np.abs(img).max())
+    one = np.zeros_like(ones)
+    one[1, 3, :] = 1.0
+    b = oracle.kirchhoff_angle_forward(S, Ts, Tr, xs, xr, one, nt, dt, 10.0, 10.0, 30.0, 1000.0, 90.0, 2.0)
+    cmp_bin = ((0.5 * (xs[:, None] + xr[None, :]) - mn) / dcmp).astype(int)
+    assert not b[cmp_bin != 1].any()
