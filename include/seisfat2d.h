@@ -115,6 +115,21 @@ int sf_batch_table(sf_ctx* ctx, int shot, float* T, int mem, void* stream);
 int sf_batch_adjoint(sf_ctx* ctx, const float* pick_grad, int pg_mem, float* grad, int grad_mem,
                      void* stream);
 
+/* Anisotropic batches (sf_batch_forward with ani = 1 and SF_KEEP_TAPE) tape
+ * the second, qP solve. Their adjoint (sf_batch_adjoint or
+ * sf_batch_misfit_gradient) multiplies each shot's gradient with respect to
+ * its own qP slowness field by that field's derivatives, with the
+ * propagation direction of the first solve held fixed (the first solve sees
+ * S only, so the stiffness derivatives are exact): grad is then dJ/dS, and
+ * sf_batch_stiffness_gradient gives dJ/dC11 and dJ/dC13 (padded grid, nzz x
+ * nxx, z fastest) of the same adjoint. These are the three sensitivities
+ * Tomography_VTI::set_sensitivity_matrix builds from rays
+ * (src/inversion/tomography_vti.cpp:24-109) in the parameters the stiffness
+ * enters through (dC11/depsilon = 2 C33; dC13/ddelta = C33 (C33 - C55) /
+ * (C13 + C55) for VTI). SF_ERR_STATE unless the last adjoint was of an
+ * anisotropic batch. */
+int sf_batch_stiffness_gradient(sf_ctx* ctx, float* grad_c11, float* grad_c13, int mem, void* stream);
+
 /* Misfit J = 1/2 sum (pick - t_obs)^2 over valid picks (FP64) and its
  * gradient dJ/dS, from the last SF_KEEP_TAPE batch. Replaces
  * Inversion::check_convergence + optimization (inversion.cpp:179-345). */

@@ -598,6 +598,68 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
         }
 }
 
+/* Derivatives of one node's qP slowness with the direction p = grad T /
+ * |grad T| of the first solve held fixed: Sq = S sqrt(c33 / lambda), lambda the
+ * larger eigenvalue of the Christoffel matrix along p, v its unit eigenvector;
+ * dSq/dS = sqrt(c33/lambda), dSq/dC11 = -Sq px^2 vx^2 / (2 lambda),
+ * dSq/dC13 = -Sq px pz vx vz / lambda. FP64, each operation rounded once, in
+ * this order; (1, 0, 0) for a zero gradient or a non-positive eigenvalue. */
+static void qp_factors_f64(float tzp, float tzm, float txp, float txm, float s, float dx, float dz, float c11f,
+                           float c13f, float c15f, float c33f, float c35f, float c55f, float* fS, float* f11,
+                           float* f13)
+{
+    const double c11 = c11f, c13 = c13f, c15 = c15f, c33 = c33f, c35 = c35f, c55 = c55f;
+    double dTz = 0.5 * ((double)tzp - (double)tzm) / (double)dz;
+    double dTx = 0.5 * ((double)txp - (double)txm) / (double)dx;
+    double nrm = sqrt(dTx * dTx + dTz * dTz);
+    *fS = 1.0f;
+    *f11 = 0.0f;
+    *f13 = 0.0f;
+    if (!(nrm > 0.0)) return;
+    double px = dTx / nrm, pz = dTz / nrm;
+    double Gxx = c11 * px * px + c55 * pz * pz + 2.0 * c15 * px * pz;
+    double Gzz = c55 * px * px + c33 * pz * pz + 2.0 * c35 * px * pz;
+    double Gxz = c15 * px * px + c35 * pz * pz + (c13 + c55) * px * pz;
+    double h = 0.5 * (Gxx - Gzz);
+    double r = sqrt(h * h + Gxz * Gxz);
+    double lam = 0.5 * (Gxx + Gzz) + r;
+    if (!(lam > 0.0)) return;
+    double vx, vz;
+    if (h >= 0.0) { vx = h + r; vz = Gxz; }
+    else          { vx = Gxz; vz = r - h; }
+    double nv = sqrt(vx * vx + vz * vz);
+    if (nv > 0.0) { vx = vx / nv; vz = vz / nv; }
+    else          { vx = px; vz = pz; }
+    double fs = sqrt(c33 / lam);
+    double sq = (double)s * fs;
+    *fS = (float)fs;
+    *f11 = (float)((-0.5 * sq * (px * px) * (vx * vx)) / lam);
+    *f13 = (float)((-sq * (px * pz) * (vx * vz)) / lam);
+}
+
+/* The factors over a window, as the qP pass runs (interior nodes except the
+ * source; the others keep S: (1, 0, 0)). */
+void orc_qp_factors(int nzz, int ncols, int nb, const float* T, const float* Sin, int ldS, float dx, float dz,
+                    int sIdz, int sIdx_loc, const uint16_t* const codes[6], const float mm[12], float* fS,
+                    float* f11, float* f13)
+{
+    for (int j = 0; j < ncols; j++)
+        for (int i = 0; i < nzz; i++) {
+            size_t is = (size_t)i + (size_t)j * ldS;
+            size_t it = (size_t)i + (size_t)j * nzz;
+            fS[it] = 1.0f;
+            f11[it] = 0.0f;
+            f13[it] = 0.0f;
+            if (!((i >= nb) && (i < nzz - nb) && (j >= nb) && (j < ncols - nb))) continue;
+            if ((i == sIdz) && (j == sIdx_loc)) continue;
+            qp_factors_f64(T[it + 1], T[it - 1], T[it + nzz], T[it - nzz], Sin[is], dx, dz,
+                           decode_c(codes[0][is], mm[0], mm[1]), decode_c(codes[1][is], mm[2], mm[3]),
+                           decode_c(codes[2][is], mm[4], mm[5]), decode_c(codes[3][is], mm[6], mm[7]),
+                           decode_c(codes[4][is], mm[8], mm[9]), decode_c(codes[5][is], mm[10], mm[11]),
+                           &fS[it], &f11[it], &f13[it]);
+        }
+}
+
 /* ------------------------------------------------------------------ picks */
 
 /* admin.cpp:121-133 */
@@ -940,13 +1002,17 @@ void orc_adjoint_f64(int nzz, int ncols, int sIdz, int sIdx_loc, const uint8_t* 
 int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots,
                            const float* sx, const float* sz, const int* c0, const int* ncols,
                            const float* rx, const float* rz, int nrec, const float* tobs,
-                           float* picks, double* misfit, float* grad, int nthreads)
+                           float* picks, double* misfit, float* grad, int nthreads, int ani,
+                           const uint16_t* const codes[6], const float mm[12], float* grad_c11,
+                           float* grad_c13)
 {
     int used = 1;
     size_t* off = (size_t*)malloc(sizeof(size_t) * ((size_t)nshots + 1));
     off[0] = 0;
     for (int b = 0; b < nshots; b++) off[b + 1] = off[b] + (size_t)nzz * ncols[b];
     float* gw = (float*)calloc(off[nshots] ? off[nshots] : 1, sizeof(float));
+    /* anisotropic: each shot's dSq/dS, dSq/dC11, dSq/dC13 */
+    float* fq = ani ? (float*)malloc(3 * (off[nshots] ? off[nshots] : 1) * sizeof(float)) : NULL;
     int bad = 0;
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();
@@ -980,7 +1046,33 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
         float* c2 = (float*)malloc(4 * n * sizeof(float));
         float* lam = (float*)malloc(n * sizeof(float));
         float* pg = (float*)malloc(sizeof(float) * (nrec > 0 ? nrec : 1));
-        orc_solve_tape_f32(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, code, c1, c2);
+        if (ani) {
+            /* first solve untaped, qP pass and its derivative factors, then the
+             * second (qP) solve taped; its initial values read the qP field */
+            float* fS = fq + off[b];
+            float* Sq = (float*)malloc(n * sizeof(float));
+            const uint16_t* cw[6];
+            for (int q = 0; q < 6; q++) cw[q] = codes[q] + (size_t)c0[b] * nzz;
+            orc_solve_f32(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, 1, 1);
+            orc_qslowness_f32(nzz, nc, nb, T, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
+            orc_qp_factors(nzz, nc, nb, T, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, fS, fS + off[nshots],
+                           fS + 2 * off[nshots]);
+            for (int bb = 0; bb < 3; bb++)
+                for (int a = 0; a < 3; a++) {
+                    int zi = sIdz + a - 1, xl = sloc + bb - 1;
+                    if (g_arith == 1) {
+                        float X = fmaf((float)(xl + c0[b] - nb), dx, -sx[b]);
+                        float Z = fmaf((float)(zi - nb), dz, -sz[b]);
+                        init[a + 3 * bb] = Sq[zi + (size_t)xl * nzz] * sqrtf(X * X + Z * Z);
+                    } else {
+                        init[a + 3 * bb] = (float)((double)Sq[zi + (size_t)xl * nzz] * dist[a + 3 * bb]);
+                    }
+                }
+            orc_solve_tape_f32(nzz, nc, Sq, nzz, dx, dz, sIdz, sloc, init, T, code, c1, c2);
+            free(Sq);
+        } else {
+            orc_solve_tape_f32(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, code, c1, c2);
+        }
         float* pk = picks + (size_t)b * nrec;
         orc_picks_f32(T, nzz, nc, c0[b], dx, dz, nb, rx, rz, nrec, pk);
         for (int r = 0; r < nrec; r++) pg[r] = pk[r] - tobs[(size_t)b * nrec + r]; /* NaN: no pick */
@@ -992,11 +1084,22 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
     used = nthreads;
 #endif
     /* shot gradients summed in FP64 in caller order; misfit over (shot, receiver) */
-    double* acc = (double*)calloc((size_t)nzz * nxx, sizeof(double));
+    double* acc = (double*)calloc((size_t)nzz * nxx * (ani ? 3 : 1), sizeof(double));
     double J = 0.0;
     for (int b = 0; b < nshots; b++) {
         const size_t base = (size_t)c0[b] * nzz;
-        for (size_t q = 0; q < off[b + 1] - off[b]; q++) acc[base + q] += (double)gw[off[b] + q];
+        const size_t npad = (size_t)nzz * nxx;
+        for (size_t q = 0; q < off[b + 1] - off[b]; q++) {
+            if (ani) {
+                /* the shot's gradient with respect to its qP field times the factors */
+                const double gq = (double)gw[off[b] + q];
+                acc[base + q] += gq * (double)fq[off[b] + q];
+                acc[npad + base + q] += gq * (double)fq[off[nshots] + off[b] + q];
+                acc[2 * npad + base + q] += gq * (double)fq[2 * off[nshots] + off[b] + q];
+            } else {
+                acc[base + q] += (double)gw[off[b] + q];
+            }
+        }
         for (int r = 0; r < nrec; r++) {
             /* the residual is the FP32 pick gradient; its square is summed in FP64 */
             double d = (double)(picks[(size_t)b * nrec + r] - tobs[(size_t)b * nrec + r]);
@@ -1004,8 +1107,14 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
         }
     }
     for (size_t q = 0; q < (size_t)nzz * nxx; q++) grad[q] = (float)acc[q];
+    if (ani)
+        for (size_t q = 0; q < (size_t)nzz * nxx; q++) {
+            grad_c11[q] = (float)acc[(size_t)nzz * nxx + q];
+            grad_c13[q] = (float)acc[2 * (size_t)nzz * nxx + q];
+        }
     if (misfit) *misfit = J;
     free(acc);
+    free(fq);
     free(gw);
     free(off);
     return bad ? -1 : used;

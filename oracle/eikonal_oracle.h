@@ -147,7 +147,12 @@ void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb,
 int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots,
                            const float* sx, const float* sz, const int* c0, const int* ncols,
                            const float* rx, const float* rz, int nrec, const float* tobs,
-                           float* picks, double* misfit, float* grad, int nthreads);
+                           float* picks, double* misfit, float* grad, int nthreads, int ani,
+                           const uint16_t* const codes[6], const float mm[12], float* grad_c11,
+                           float* grad_c13);
+void orc_qp_factors(int nzz, int ncols, int nb, const float* T, const float* Sin, int ldS, float dx, float dz,
+                    int sIdz, int sIdx_loc, const uint16_t* const codes[6], const float mm[12], float* fS,
+                    float* f11, float* f13);
 
 /* Tomography update (inversion.cpp:347-447, tomography_iso.cpp:77-92):
  * the Gaussian kernel of smooth_matrix (n x n, x major), model_smoothing of a

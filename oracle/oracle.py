@@ -73,7 +73,10 @@ def lib():
                                           f32p, f32p, C.c_int, f64p, f64p]
         L.orc_batch_gradient_f32.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float,
                                              C.c_int, f32p, f32p, i32p, i32p, f32p, f32p, C.c_int,
-                                             f32p, f32p, C.POINTER(C.c_double), f32p, C.c_int]
+                                             f32p, f32p, C.POINTER(C.c_double), f32p, C.c_int, C.c_int,
+                                             C.c_void_p * 6, f32p, f32p, f32p]
+        L.orc_qp_factors.argtypes = [C.c_int, C.c_int, C.c_int, f32p, f32p, C.c_int, C.c_float, C.c_float,
+                                     C.c_int, C.c_int, C.c_void_p * 6, f32p, f32p, f32p, f32p]
         L.orc_batch_gradient_f32.restype = C.c_int
         L.orc_smooth_kernel.argtypes = [C.c_float, C.c_int, f32p]
         L.orc_model_smoothing.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_int, f32p]
@@ -267,10 +270,12 @@ def batch_picks(S, dx, dz, sx, sz, c0, ncols, rx, rz, nb=3, ani=None, nthreads=0
     return out, used
 
 
-def batch_misfit_gradient(S, dx, dz, shots, rx, rz, t_obs, nb=3, nthreads=0):
+def batch_misfit_gradient(S, dx, dz, shots, rx, rz, t_obs, nb=3, nthreads=0, ani=None):
     """FP32 oracle of sf_batch_misfit_gradient, one shot per thread.
     shots: (sx, sz) or (sx, sz, c0, ncols). Returns (misfit, grad (nxx, nzz),
-    picks (nshots, nrec), threads_used)."""
+    picks (nshots, nrec), threads_used). ani: (codes[6], mm[12]) for the
+    anisotropic two-pass scheme; then grad is dJ/dS and the return value has
+    two more entries, dJ/dC11 and dJ/dC13 (nxx, nzz)."""
     S = _f32(S)
     nxx, nzz = S.shape
     ns = len(shots)
@@ -282,11 +287,22 @@ def batch_misfit_gradient(S, dx, dz, shots, rx, rz, t_obs, nb=3, nthreads=0):
     picks = np.zeros((ns, len(rx)), np.float32)
     grad = np.zeros((nxx, nzz), np.float32)
     mis = C.c_double()
+    g11 = np.zeros((nxx, nzz), np.float32)
+    g13 = np.zeros((nxx, nzz), np.float32)
+    if ani is not None:
+        arr, keep = _codes_arg(ani[0])
+        mm = _f32(ani[1])
+    else:
+        arr, keep = (C.c_void_p * 6)(), []
+        mm = np.zeros(12, np.float32)
     used = lib().orc_batch_gradient_f32(nzz, nxx, nb, S, dx, dz, ns, sx, sz, c0, nc, _f32(rx), _f32(rz),
                                         len(rx), _f32(np.asarray(t_obs).reshape(ns, len(rx))), picks,
-                                        C.byref(mis), grad, nthreads)
+                                        C.byref(mis), grad, nthreads, 1 if ani is not None else 0, arr, mm,
+                                        g11, g13)
     if used < 0:
         raise ValueError("a source lies outside its window")
+    if ani is not None:
+        return mis.value, grad, picks, used, g11, g13
     return mis.value, grad, picks, used
 
 

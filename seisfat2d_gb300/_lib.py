@@ -52,6 +52,7 @@ SIGNATURES = {
     "sf_batch_table": (C.c_int, [VP, C.c_int, VP, C.c_int, VP]),
     "sf_batch_adjoint": (C.c_int, [VP, VP, C.c_int, VP, C.c_int, VP]),
     "sf_batch_misfit_gradient": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_double), VP, C.c_int, VP]),
+    "sf_batch_stiffness_gradient": (C.c_int, [VP, VP, VP, C.c_int, VP]),
     "sf_synchronize": (C.c_int, [VP, VP]),
     "sf_set_launch": (C.c_int, [VP, C.c_int, C.c_int]),
     "sf_set_arithmetic": (C.c_int, [VP, C.c_int]),

@@ -143,6 +143,7 @@ static int prepare_gather(sf_ctx* c, cudaStream_t st)
                 g.sx = d.sx;
                 g.sz = d.sz;
                 g.orig = o;
+                g.q_off = d.q_off;
                 ent.push_back(g);
             }
         }
@@ -227,8 +228,17 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     g.tcode = c->d_tcode;
     g.vrec = c->d_tc2;
     g.lam_init = c->d_lam_init;
+    if (c->batch_ani) {
+        const size_t npad = (size_t)c->nzz * c->nxx;
+        rc = sf_dev_reserve(c, (void**)&c->d_gcij, &c->cap_gcij, 2 * npad * sizeof(float));
+        if (rc) return rc;
+        g.vfac = c->d_vfac;
+        g.vfac_total = c->batch_q_cells;
+        g.grad_c11 = c->d_gcij;
+        g.grad_c13 = c->d_gcij + npad;
+    }
     A->kern = (const void*)k_adjoint;
-    A->gkern = (const void*)k_gather;
+    A->gkern = c->batch_ani ? (const void*)k_gather<true> : (const void*)k_gather<false>;
     A->grid = dim3(NG * G);
     A->block = dim3(c->warps * 32);
     A->smem = smem;
@@ -277,6 +287,7 @@ int sf_adjoint_device(sf_ctx* c, const float* d_pg, float* d_grad, cudaStream_t 
     if (!rc) rc = sf_adj_enqueue(c, A, d_pg, d_grad, sf_next_epoch(c), st);
     if (rc) return rc;
     c->tape_valid = false;  // the reverse sweeps overwrite the tape's c2 with their terms
+    c->gcij_valid = c->batch_ani != 0;
     return SF_OK;
 }
 
@@ -349,5 +360,20 @@ extern "C" int sf_batch_misfit_gradient(sf_ctx* c, const float* t_obs, int obs_m
     if (grad_mem == SF_MEM_HOST)
         CK(cudaMemcpyAsync(grad, dg, (size_t)c->nzz * c->nxx * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (misfit || grad_mem == SF_MEM_HOST) return sf_check_flags(c, st);
+    return SF_OK;
+}
+
+extern "C" int sf_batch_stiffness_gradient(sf_ctx* c, float* grad_c11, float* grad_c13, int mem, void* stream)
+{
+    if (!c) return SF_ERR_ARG;
+    if (!c->gcij_valid) return sf_fail(c, SF_ERR_STATE, "no adjoint of an anisotropic taped batch");
+    if (!grad_c11 || !grad_c13) return sf_fail(c, SF_ERR_ARG, "null argument");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t npad = (size_t)c->nzz * c->nxx;
+    const cudaMemcpyKind kind = (mem == SF_MEM_HOST) ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    CK(cudaMemcpyAsync(grad_c11, c->d_gcij, npad * sizeof(float), kind, st));
+    CK(cudaMemcpyAsync(grad_c13, c->d_gcij + npad, npad * sizeof(float), kind, st));
+    if (mem == SF_MEM_HOST) return sf_check_flags(c, st);
     return SF_OK;
 }

@@ -365,6 +365,11 @@ struct GatherSmem {
     GatherShot shots[kGChunk];
 };
 
+// VTI: the batch was anisotropic; each shot's summed terms (its gradient with
+// respect to its own qP slowness) are multiplied by the shot's derivative
+// factors of the qP slowness before the FP64 sum over shots, giving dJ/dS,
+// dJ/dC11 and dJ/dC13.
+template <bool VTI>
 __global__ void __launch_bounds__(256) k_gather(GatherParams p)
 {
     extern __shared__ __align__(16) unsigned char gsm_raw[];
@@ -410,6 +415,9 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
     };
 
     double total[4] = {0.0, 0.0, 0.0, 0.0};
+    double t11[VTI ? 4 : 1], t13[VTI ? 4 : 1];
+    if (VTI)
+        for (int q = 0; q < 4; q++) t11[q] = t13[q] = 0.0;
     float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const int e_end = p.blk_ptr[cb + 1];
 #pragma unroll 1
@@ -470,7 +478,14 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
                         const double d = src_dist(a, bc, p.nb, p.dx, p.dz, t.sx, t.sz);
                         g[q] = fadd(g[q], fmul(p.lam_init[(size_t)t.orig * 9 + da + 3 * db], __double2float_rn(d)));
                     }
-                    total[q] += (double)g[q];
+                    if (VTI) {
+                        const float* f = p.vfac + t.q_off + (size_t)a + (size_t)bl * p.nzz;
+                        total[q] += (double)g[q] * (double)f[0];
+                        t11[q] += (double)g[q] * (double)f[p.vfac_total];
+                        t13[q] += (double)g[q] * (double)f[2 * p.vfac_total];
+                    } else {
+                        total[q] += (double)g[q];
+                    }
                     g[q] = 0.0f;
                 }
             }
@@ -479,7 +494,13 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
     }
     for (int q = 0; q < 4; q++) {
         const int bc = c + cq + 8 * q;
-        if (a < p.nzz && bc < p.nxx) p.grad[(size_t)a + (size_t)bc * p.nzz] = __double2float_rn(total[q]);
+        if (a < p.nzz && bc < p.nxx) {
+            p.grad[(size_t)a + (size_t)bc * p.nzz] = __double2float_rn(total[q]);
+            if (VTI) {
+                p.grad_c11[(size_t)a + (size_t)bc * p.nzz] = __double2float_rn(t11[q]);
+                p.grad_c13[(size_t)a + (size_t)bc * p.nzz] = __double2float_rn(t13[q]);
+            }
+        }
     }
 }
 

@@ -46,6 +46,7 @@ struct GatherShot {
     int sIdx, sIdz;
     float sx, sz;
     int orig, pad_;
+    long long q_off;        // the shot's qP derivative factors (anisotropic batches)
 };
 
 struct GatherParams {
@@ -57,6 +58,12 @@ struct GatherParams {
     const float* vrec;       // v terms (tape c2 after the reverse sweeps)
     const float* lam_init;   // nshots x 9 (caller order)
     float* grad;             // nzz x nxx
+    // anisotropic batches: each shot's gradient with respect to its qP
+    // slowness, times the shot's dSq/dS, dSq/dC11, dSq/dC13 (3 x vfac_total)
+    const float* vfac;
+    long long vfac_total;
+    float* grad_c11;         // nzz x nxx
+    float* grad_c13;         // nzz x nxx
 };
 
 }  // namespace sf

@@ -277,4 +277,51 @@ __device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, fl
     return fdiv(1.0f, fsqrt(fmul(g0, Ro)));
 }
 
+// Derivatives of the qP slowness of one node (eikonal_ani.cu:59-108) with the
+// propagation direction p = grad T / |grad T| of the first solve held fixed
+// (the first solve sees S only, so for the stiffnesses this is exact):
+// Sq = S sqrt(c33 / lambda), lambda the larger eigenvalue of the Christoffel
+// matrix Gamma(C, p) and v its unit eigenvector, so
+//   dSq/dS   = sqrt(c33 / lambda)
+//   dSq/dC11 = -Sq / (2 lambda) * px^2 vx^2          (dGamma_xx/dC11 = px^2)
+//   dSq/dC13 = -Sq / lambda * px pz vx vz            (dGamma_xz/dC13 = px pz)
+// In FP64 with each operation rounded once (no contraction), then rounded to
+// FP32, so a C restatement gives the same bits. A zero gradient or a
+// non-positive eigenvalue gives (1, 0, 0).
+__device__ __forceinline__ void qp_factors(float tzp, float tzm, float txp, float txm, float s, float dx,
+                                           float dz, float c11, float c13, float c15, float c33, float c35,
+                                           float c55, float& fS, float& f11, float& f13)
+{
+    auto A = [](double a, double b) { return __dadd_rn(a, b); };
+    auto Sb = [](double a, double b) { return __dsub_rn(a, b); };
+    auto M = [](double a, double b) { return __dmul_rn(a, b); };
+    auto D = [](double a, double b) { return __ddiv_rn(a, b); };
+    const double dTz = D(M(0.5, Sb(tzp, tzm)), dz);
+    const double dTx = D(M(0.5, Sb(txp, txm)), dx);
+    const double nrm = __dsqrt_rn(A(M(dTx, dTx), M(dTz, dTz)));
+    fS = 1.0f;
+    f11 = 0.0f;
+    f13 = 0.0f;
+    if (!(nrm > 0.0)) return;
+    const double px = D(dTx, nrm), pz = D(dTz, nrm);
+    const double Gxx = A(A(M(M(c11, px), px), M(M(c55, pz), pz)), M(M(M(2.0, c15), px), pz));
+    const double Gzz = A(A(M(M(c55, px), px), M(M(c33, pz), pz)), M(M(M(2.0, c35), px), pz));
+    const double Gxz = A(A(M(M(c15, px), px), M(M(c35, pz), pz)), M(M(A(c13, c55), px), pz));
+    const double h = M(0.5, Sb(Gxx, Gzz));
+    const double r = __dsqrt_rn(A(M(h, h), M(Gxz, Gxz)));
+    const double lam = A(M(0.5, A(Gxx, Gzz)), r);
+    if (!(lam > 0.0)) return;
+    double vx, vz;
+    if (h >= 0.0) { vx = A(h, r); vz = Gxz; }
+    else          { vx = Gxz; vz = Sb(r, h); }
+    const double nv = __dsqrt_rn(A(M(vx, vx), M(vz, vz)));
+    if (nv > 0.0) { vx = D(vx, nv); vz = D(vz, nv); }
+    else          { vx = px; vz = pz; }
+    const double fs = __dsqrt_rn(D((double)c33, lam));
+    const double sq = M(s, fs);
+    fS = __double2float_rn(fs);
+    f11 = __double2float_rn(D(M(M(M(-0.5, sq), M(px, px)), M(vx, vx)), lam));
+    f13 = __double2float_rn(D(M(M(-sq, M(px, pz)), M(vx, vz)), lam));
+}
+
 }  // namespace sf

@@ -193,7 +193,8 @@ extern "C" int sf_ctx_destroy(sf_ctx* c)
     sf_adjoint_release(c);
     void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
                     c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand, c->d_ctr,
-                    c->d_skern, c->d_upd, c->d_wav, c->d_mig, c->d_kgeo, c->d_kint, c->d_kpart};
+                    c->d_skern, c->d_upd, c->d_wav, c->d_mig, c->d_kgeo, c->d_kint, c->d_kpart,
+                    c->d_vfac, c->d_gcij};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete c;
@@ -305,6 +306,8 @@ int sf_fwd_setup(sf_ctx* c)
     CK(cudaFuncSetAttribute(k_shots<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
     CK(cudaFuncSetAttribute(k_shots<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
     CK(cudaFuncSetAttribute(k_shots<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_shots<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_shots<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
     return sf_adj_setup(c);
 }
 
@@ -453,7 +456,7 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
     c->hshots.resize(nshots);
     std::vector<int> order(nshots);
     std::vector<std::pair<int, std::array<int, 8>>> skip_cache;
-    long long toff = 0, tape_off = 0;
+    long long toff = 0, tape_off = 0, q_off = 0;
     const int nstrips = (c->nzz + 31) / 32;
     int maxcols = 0;
     for (int b = 0; b < nshots; b++) {
@@ -494,6 +497,8 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
         if (keep_tables) toff += (long long)c->nzz * d.ncols;
         d.tape_off = tape_off;
         if (tape) tape_off += 4LL * nstrips * (d.ncols + 31) * 32;
+        d.q_off = q_off;
+        if (tape) q_off += (long long)c->nzz * d.ncols;
         maxcols = std::max(maxcols, d.ncols);
         c->hshots[b] = d;
     }
@@ -501,6 +506,7 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
                      [](const ShotDev& a, const ShotDev& b) { return a.ncols > b.ncols; });
     c->batch_T_floats = toff;
     c->batch_tape_entries = tape_off;
+    c->batch_q_cells = q_off;
     c->batch_maxcols = maxcols;
     c->tables_index.assign(nshots, 0);
     for (int q = 0; q < nshots; q++) c->tables_index[c->hshots[q].orig] = q;
@@ -515,7 +521,9 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     const int nstrips = (c->nzz + 31) / 32;
     const size_t smem = sf_fwd_smem_bytes(c->warps);
     const bool ref = c->arith == SF_ARITH_REFERENCE;
-    const void* kern = ref ? (tape ? (const void*)k_shots<true, true> : (const void*)k_shots<false, true>)
+    const bool vti = tape && ani;
+    const void* kern = vti ? (ref ? (const void*)k_shots<true, true, true> : (const void*)k_shots<true, false, true>)
+                     : ref ? (tape ? (const void*)k_shots<true, true> : (const void*)k_shots<false, true>)
                            : (tape ? (const void*)k_shots<true, false> : (const void*)k_shots<false, false>);
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
@@ -546,6 +554,7 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
         rc = sf_dev_reserve(c, (void**)&c->d_tcode, &c->cap_tcode, n);
         if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc1, &c->cap_tc1, n * sizeof(float));
         if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc2, &c->cap_tc2, n * sizeof(float));
+        if (!rc && ani) rc = sf_dev_reserve(c, (void**)&c->d_vfac, &c->cap_vfac, 3 * (size_t)c->batch_q_cells * sizeof(float));
         if (rc) return rc;
     }
     FwdParams& p = L->p;
@@ -577,6 +586,10 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
         p.tcode = c->d_tcode;
         p.tc1 = c->d_tc1;
         p.tc2 = c->d_tc2;
+        if (ani) {
+            p.vfac = c->d_vfac;
+            p.vfac_total = c->batch_q_cells;
+        }
     }
     p.rx = c->d_rx;
     p.rz = c->d_rz;
@@ -627,6 +640,8 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
     c->tables_valid = keep_tables;
     c->tape_valid = tape;
     c->batch_nrec = nrec;
+    c->batch_ani = ani;
+    c->gcij_valid = false;
     return SF_OK;
 }
 
@@ -673,7 +688,6 @@ extern "C" int sf_batch_forward(sf_ctx* c, int ani, const sf_shot* shots, int ns
         return sf_fail(c, SF_ERR_ARG, "bad batch arguments");
     if (ani && !c->have_cij) return sf_fail(c, SF_ERR_STATE, "anisotropic solve needs sf_set_stiffness");
     const bool tape = (flags & SF_KEEP_TAPE) != 0, tables = (flags & SF_KEEP_TABLES) != 0;
-    if (ani && tape) return sf_fail(c, SF_ERR_ARG, "the adjoint tape is isotropic only");
     CK(cudaSetDevice(c->dev));
     cudaStream_t st = (cudaStream_t)stream;
     c->tape_valid = false;

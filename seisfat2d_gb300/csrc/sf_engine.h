@@ -59,7 +59,9 @@ struct sf_ctx {
     std::vector<sf::ShotDev> hshots;  // sorted widest first
     std::vector<int> tables_index;    // caller index -> hshots index
     long long batch_T_floats = 0, batch_tape_entries = 0;
+    long long batch_q_cells = 0;      // window cells of all shots (qP derivative factors)
     int batch_maxcols = 0, batch_nshots = 0, batch_nrec = 0;
+    int batch_ani = 0;                // the last batch solved the anisotropic two-pass scheme
     float* batch_picks = nullptr;
     bool tables_valid = false, tape_valid = false;
     std::vector<float> h_rx, h_rz;
@@ -110,6 +112,12 @@ struct sf_ctx {
     float* d_kgeo = nullptr; size_t cap_kgeo = 0;
     int* d_kint = nullptr; size_t cap_kint = 0;
     float* d_kpart = nullptr; size_t cap_kpart = 0;  // forward operator chunk partials
+
+    // anisotropic adjoint: per-shot dSq/d{S, C11, C13} factors and the
+    // stiffness gradients of the last adjoint (sf_batch_stiffness_gradient)
+    float* d_vfac = nullptr; size_t cap_vfac = 0;
+    float* d_gcij = nullptr; size_t cap_gcij = 0;
+    bool gcij_valid = false;
     std::vector<int> h_kint;
     std::vector<double> h_wav;
     std::vector<float> h_kgeo;

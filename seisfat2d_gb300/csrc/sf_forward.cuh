@@ -18,6 +18,7 @@ struct ShotDev {
     int pad_;
     long long t_off;      // traveltime window offset (floats) when tables are kept
     long long tape_off;   // tape offset (entries)
+    long long q_off;      // qP derivative factors offset (window cells), anisotropic taped batches
 };
 
 struct FwdParams {
@@ -41,6 +42,8 @@ struct FwdParams {
     float mm[12];
     float* Sq;            // qP slowness, Sq + gang * sq_per_gang
     long long sq_per_gang;
+    float* vfac;          // taped: dSq/dS, dSq/dC11, dSq/dC13 per shot window cell (3 x vfac_total)
+    long long vfac_total;
     // tape
     uint8_t* tcode;
     float* tc1;
@@ -154,8 +157,10 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
 
 // Persistent gangs of G CTAs: gang k solves shots k, k+NG, ... (shots are
 // sorted widest window first). The grid never exceeds what the device can
-// hold at once, so every gang's CTAs are resident together.
-template <bool TAPE, bool REF>
+// hold at once, so every gang's CTAs are resident together. VTI (with TAPE):
+// anisotropic shots whose second (qP) solve is taped, with the qP pass
+// writing its derivative factors.
+template <bool TAPE, bool REF, bool VTI = false>
 // (kMaxWarps * 32, 1): with the block size alone as the bound ptxas caps the
 // kernel at 64 registers and spills the strip loop's state to local memory.
 __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
@@ -182,7 +187,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
         const unsigned tag = (p.epoch << 10) | (unsigned)((it * nsolves) & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE, REF>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
+        solve_window<TAPE && !VTI, REF>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
         if (p.ani) {
             // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
             // warp's strips, once the whole first solve is done
@@ -197,17 +202,28 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
                     const size_t g = (size_t)i + (size_t)(sh.c0 + j) * nzz;
                     float s = p.S[g];
                     float out = s;
+                    float fS = 1.0f, f11 = 0.0f, f13 = 0.0f;
                     if (i >= nb && i < nzz - nb && j >= nb && j < ncols - nb && !(i == sh.sIdz && j == sloc)) {
                         const float* Tc = T + idx;
-                        out = qp_slowness<REF>(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz,
-                                               decode_c(p.cij[0][g], p.mm[0], p.mm[1]),
-                                               decode_c(p.cij[1][g], p.mm[2], p.mm[3]),
-                                               decode_c(p.cij[2][g], p.mm[4], p.mm[5]),
-                                               decode_c(p.cij[3][g], p.mm[6], p.mm[7]),
-                                               decode_c(p.cij[4][g], p.mm[8], p.mm[9]),
-                                               decode_c(p.cij[5][g], p.mm[10], p.mm[11]));
+                        const float c11 = decode_c(p.cij[0][g], p.mm[0], p.mm[1]);
+                        const float c13 = decode_c(p.cij[1][g], p.mm[2], p.mm[3]);
+                        const float c15 = decode_c(p.cij[2][g], p.mm[4], p.mm[5]);
+                        const float c33 = decode_c(p.cij[3][g], p.mm[6], p.mm[7]);
+                        const float c35 = decode_c(p.cij[4][g], p.mm[8], p.mm[9]);
+                        const float c55 = decode_c(p.cij[5][g], p.mm[10], p.mm[11]);
+                        out = qp_slowness<REF>(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz, c11,
+                                               c13, c15, c33, c35, c55);
+                        if (VTI)
+                            qp_factors(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz, c11, c13, c15,
+                                       c33, c35, c55, fS, f11, f13);
                     }
                     Sq[idx] = out;
+                    if (VTI) {
+                        float* f = p.vfac + sh.q_off + idx;
+                        f[0] = fS;
+                        f[p.vfac_total] = f11;
+                        f[2 * p.vfac_total] = f13;
+                    }
                 }
             }
             gang_barrier(bar, (++nbar) * p.G, cs, p.err);
@@ -223,7 +239,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
                         __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
             }
             __syncthreads();
-            solve_window<false, REF>(p, sh, gp, Sq, nzz, T, tag + 1u, cs, rings);
+            solve_window<TAPE, REF>(p, sh, gp, Sq, nzz, T, tag + 1u, cs, rings);
         }
         // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {

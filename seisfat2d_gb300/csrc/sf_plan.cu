@@ -96,6 +96,7 @@ extern "C" int sf_plan_batch(sf_ctx* c, const sf_shot* shots, int nshots, const 
     cudaStream_t st = (cudaStream_t)stream;
     c->tape_valid = false;
     c->tables_valid = false;
+    c->batch_ani = 0;
     int rc = sf_prepare_shots(c, shots, nshots, false, true);
     if (!rc) rc = sf_upload_receivers(c, rx, rz, nrec, st);
     if (rc) return rc;
@@ -138,6 +139,8 @@ static void plan_done(sf_ctx* c, const float* t_obs, float* picks)
     c->batch_nshots = (int)c->hshots.size();
     c->batch_nrec = c->plan_nrec;
     c->tape_valid = (t_obs == nullptr);  // the reverse sweeps consume the tape
+    c->batch_ani = 0;
+    c->gcij_valid = false;
 }
 
 extern "C" int sf_plan_iteration(sf_ctx* c, const float* t_obs, float* picks, double* misfit, float* grad,

@@ -178,6 +178,16 @@ class Engine:
                     "sf_batch_adjoint")
         return out
 
+    def stiffness_gradient(self, stream=None):
+        """dJ/dC11 and dJ/dC13 (each (nxx, nzz)) of the last adjoint of an
+        anisotropic taped batch."""
+        g11 = np.zeros((self.nxx, self.nzz), np.float32)
+        g13 = np.zeros_like(g11)
+        self._check(self.L.sf_batch_stiffness_gradient(self._ctx, C.c_void_p(g11.ctypes.data),
+                                                       C.c_void_p(g13.ctypes.data), SF_MEM_HOST,
+                                                       _stream_ptr(stream)), "sf_batch_stiffness_gradient")
+        return g11, g13
+
     def misfit_gradient(self, t_obs, out=None, stream=None, want_misfit=True):
         """Misfit 1/2 sum (pick - t_obs)^2 of the taped batch and its slowness
         gradient (padded (nxx, nzz)). With want_misfit False and a device

@@ -1,7 +1,7 @@
 // inversion.exe parameters.txt — the reference's tomography driver
 // (src/inversion_main.cpp:4-41) on the GB300 engine. The reference reads
 // `inversion_type`, which run/parameters.txt spells `inv_type`; both are
-// accepted. Only the isotropic tomography (type 0) is built.
+// accepted: 0 isotropic (Tomography_ISO), 1 anisotropic VTI (Tomography_VTI).
 #include <chrono>
 #include <iostream>
 
@@ -18,8 +18,9 @@ int main(int argc, char** argv)
         auto file = std::string(argv[1]);
         std::string t = catch_parameter("inversion_type", file);
         if (t.empty()) t = catch_parameter("inv_type", file);
-        if (!t.empty() && std::stoi(t) != 0) throw std::invalid_argument("only inv_type = 0 (isotropic) is built");
-        Inversion* inv = new Tomography_ISO();
+        const int type = t.empty() ? 0 : std::stoi(t);
+        if (type != 0 && type != 1) throw std::invalid_argument("inv_type must be 0 (isotropic) or 1 (VTI)");
+        Inversion* inv = (type == 1) ? (Inversion*)new Tomography_VTI() : (Inversion*)new Tomography_ISO();
         inv->parameters = file;
         inv->set_parameters();
         inv->import_obsData();

@@ -224,16 +224,57 @@ void Eikonal_ANI::set_conditions()
     modeling_name = "Modeling type: Anisotropic eikonal solver";
     ani = 1;
     const char* names[6] = {"C11", "C13", "C15", "C33", "C35", "C55"};
-    std::vector<std::vector<float>> padded(6, std::vector<float>(matsize));
+    for (int q = 0; q < 6; q++) {
+        cij[q].assign(matsize, 0.0f);
+        set_stiffness_element(names[q], cij[q].data());
+    }
+    upload_stiffness();
+}
+
+// modeling.cu:264-279 on each padded field, then the codes to the engine
+void Eikonal_ANI::upload_stiffness()
+{
     std::vector<std::vector<uintc>> codes(6, std::vector<uintc>(matsize));
     float mm[12];
     const uint16_t* cp[6];
     for (int q = 0; q < 6; q++) {
-        set_stiffness_element(names[q], padded[q].data());
-        compression(padded[q].data(), codes[q].data(), matsize, mm[2 * q + 1], mm[2 * q]);
+        compression(cij[q].data(), codes[q].data(), matsize, mm[2 * q + 1], mm[2 * q]);
         cp[q] = codes[q].data();
     }
     sf_check(sf_set_stiffness_codes(ctx, cp, mm, SF_MEM_HOST), ctx, "sf_set_stiffness_codes");
+}
+
+// epsilon = (C11 - C33) / (2 C33), delta = ((C13 + C55)^2 - (C33 - C55)^2) /
+// (2 C33 (C33 - C55)): the inverse of the VTI relations of
+// src/functions.py:72-109
+void Eikonal_ANI::get_stiffness_VTI(float* E, float* D) const
+{
+    for (int index = 0; index < nPoints; index++) {
+        const int i = index % nz + nb, j = index / nz + nb;
+        const size_t k = (size_t)i + (size_t)j * nzz;
+        const double c11 = cij[0][k], c13 = cij[1][k], c33 = cij[3][k], c55 = cij[5][k];
+        E[index] = (float)((c11 - c33) / (2.0 * c33));
+        D[index] = (float)(((c13 + c55) * (c13 + c55) - (c33 - c55) * (c33 - c55)) / (2.0 * c33 * (c33 - c55)));
+    }
+}
+
+// C11 = C33 (1 + 2 epsilon), C13 = sqrt((C33 - C55)(2 delta C33 + C33 - C55))
+// - C55 on the model cells (delta held where the root stays real), padded by
+// edge replication, quantised and uploaded
+void Eikonal_ANI::set_stiffness_VTI(const float* E, const float* D)
+{
+    std::vector<float> m11(nPoints), m13(nPoints);
+    for (int index = 0; index < nPoints; index++) {
+        const int i = index % nz + nb, j = index / nz + nb;
+        const size_t k = (size_t)i + (size_t)j * nzz;
+        const double c33 = cij[3][k], c55 = cij[5][k];
+        const double arg = (c33 - c55) * (2.0 * (double)D[index] * c33 + c33 - c55);
+        m11[index] = (float)(c33 * (1.0 + 2.0 * (double)E[index]));
+        m13[index] = (float)(std::sqrt(std::max(arg, 0.0)) - c55);
+    }
+    expand_boundary(m11.data(), cij[0].data());
+    expand_boundary(m13.data(), cij[1].data());
+    upload_stiffness();
 }
 
 void Eikonal_ANI::time_propagation()

@@ -9,6 +9,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "geometry.hpp"
 #include "seisfat2d.h"
@@ -92,10 +93,22 @@ class Eikonal_ANI : public Modeling
 {
 private:
     void set_stiffness_element(std::string element, float* padded);
+    void upload_stiffness();
+
+    // padded C11, C13, C15, C33, C35, C55 (nzz x nxx), as last uploaded
+    std::vector<float> cij[6];
 
 public:
     void set_conditions() override;    // eikonal_ani.cu:18-31
     void time_propagation() override;  // eikonal_ani.cu:33-45
+
+    // Thomsen epsilon and delta (nz x nx) of the loaded stiffness, and the
+    // stiffness rebuilt from them with C33 and C55 kept: the two calls
+    // Tomography_VTI makes (tomography_vti.cpp:22, :128), which the
+    // reference never defines. VTI only (C15 and C35 are kept as loaded).
+    void get_stiffness_VTI(float* E, float* D) const;
+    void set_stiffness_VTI(const float* E, const float* D);
+    const std::vector<float>& stiffness(int q) const { return cij[q]; }
 };
 
 #endif

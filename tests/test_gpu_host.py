@@ -27,8 +27,8 @@ modeling_type = {mtype}
 modeling_output_folder = {d}/out_
 batch_shots = {batch}
 quiet = true
-inv_type = 0
-inv_max_it = 3
+inv_type = {invtype}
+inv_max_it = {maxit}
 smooth_per_iteration = true
 gaussian_filter_stdv = 2.0
 gaussian_filter_samples = 5
@@ -63,7 +63,8 @@ def exes(engine_lib):
                                               "migration.exe")}
 
 
-def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False, migtype=0):
+def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False, migtype=0, invtype=0,
+               maxit=3):
     m.astype(np.float32).tofile(os.path.join(d, "slowness.bin"))
     with open(os.path.join(d, "sps.txt"), "w") as f:
         f.write("".join(f"{x},{z}\n" for x, z in shots))
@@ -72,7 +73,8 @@ def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=Fa
     p = os.path.join(d, "parameters.txt")
     with open(p, "w") as f:
         f.write(PARAMS.format(nx=nx, nz=nz, dx=dx, dz=dz, d=d, mtype=mtype, batch="true" if batch else "false",
-                              aniso="true" if aniso else "false", migtype=migtype))
+                              aniso="true" if aniso else "false", migtype=migtype, invtype=invtype,
+                              maxit=maxit))
     return p
 
 
@@ -330,3 +332,71 @@ def test_migration_exe_least_squares(cuda, exes, tmp_path, migtype):
     assert np.allclose(conv, res, rtol=1e-5)
     assert np.abs(model).max() > 0
     assert np.array_equal(out, model)
+
+
+def _vti_files(oracle, d, nx, nz, m, eps, dlt):
+    from seisfat2d_gb300.synthetic import thomsen_stiffness
+    vp = 1.0 / m.astype(np.float64)
+    cij = thomsen_stiffness(vp, vp / np.sqrt(3.0), 1000.0, eps, dlt)
+    for name, c in zip(["C11", "C13", "C15", "C33", "C35", "C55"], cij):
+        c.astype(np.float32).tofile(os.path.join(d, f"model_{name}.bin"))
+    codes, mm = [], []
+    for c in cij:
+        cd, mn, mx = oracle.compress(oracle.expand_boundary(c.astype(np.float32)))
+        codes.append(cd)
+        mm += [mn, mx]
+    return codes, np.array(mm, np.float32)
+
+
+def test_inversion_exe_vti_stiffness_round_trip(oracle, cuda, exes, tmp_path):
+    """inv_type 1 with no iteration: the exported epsilon and delta are the
+    Thomsen parameters the stiffness files were built from (get_stiffness_VTI)."""
+    nx, nz = 40, 20
+    rng = np.random.default_rng(2)
+    m = smooth_model(nx, nz, 10.0, seed=3)
+    eps = rng.uniform(0.0, 0.25, (nx, nz))
+    dlt = rng.uniform(-0.05, 0.15, (nx, nz))
+    d = str(tmp_path)
+    _vti_files(oracle, d, nx, nz, m, eps, dlt)
+    shots = [(100.0, 0.0)]
+    recs = [(float(x), 0.0) for x in range(0, 390, 30)]
+    p = write_case(d, nx, nz, 10.0, 10.0, m, shots, recs, aniso=True, invtype=1, maxit=0)
+    np.zeros(len(recs), np.float32).tofile(os.path.join(d, "obs_shot_1.bin"))
+    run(exes["inversion.exe"], p)
+    ep = np.fromfile(os.path.join(d, f"tomography_vti_final_model_ep_{nz}x{nx}.bin"), np.float32).reshape(nx, nz)
+    dl = np.fromfile(os.path.join(d, f"tomography_vti_final_model_dl_{nz}x{nx}.bin"), np.float32).reshape(nx, nz)
+    assert np.allclose(ep, eps, atol=1e-5) and np.allclose(dl, dlt, atol=1e-4)
+
+
+def test_inversion_exe_vti_reduces_residual(oracle, cuda, exes, tmp_path):
+    """Anisotropic tomography (inv_type 1): observed picks from the oracle's
+    two-pass solve in the true (S, epsilon, delta); the start model has a
+    smoothed S and epsilon, delta off by a constant. The residual falls and the
+    three models are written."""
+    from seisfat2d_gb300.synthetic import gaussian_smooth
+    nx, nz = 70, 30
+    true = smooth_model(nx, nz, 10.0, seed=31, noise=0.0)
+    eps_t = np.full((nx, nz), 0.12)
+    dlt_t = np.full((nx, nz), 0.05)
+    d = str(tmp_path)
+    codes, mm = _vti_files(oracle, d, nx, nz, true, eps_t, dlt_t)
+    shots = [(float(x), 0.0) for x in range(50, 690, 80)]
+    recs = [(float(x), 0.0) for x in range(0, 690, 15)]
+    St = oracle.expand_boundary(true)
+    rx = np.array([r[0] for r in recs], np.float32)
+    for k, (sx, sz) in enumerate(shots):
+        _, po = oracle.shot(St, 10.0, 10.0, sx, sz, rx, np.zeros(len(recs), np.float32), ani=(codes, mm))
+        po.astype(np.float32).tofile(os.path.join(d, f"obs_shot_{k + 1}.bin"))
+    start = (1.0 / gaussian_smooth(1.0 / true.astype(np.float64), 4.0)).astype(np.float32)
+    _vti_files(oracle, d, nx, nz, start, eps_t - 0.08, dlt_t + 0.04)
+    p = write_case(d, nx, nz, 10.0, 10.0, start, shots, recs, aniso=True, invtype=1, maxit=3)
+    run(exes["inversion.exe"], p)
+    res = np.loadtxt(os.path.join(d, "tomography_vti_convergence_3_iterations.txt"))
+    print("VTI residuo per iteration:", res)
+    assert len(res) == 4 and res[-1] < 0.9 * res[0]
+    ep = np.fromfile(os.path.join(d, f"tomography_vti_final_model_ep_{nz}x{nx}.bin"), np.float32)
+    dl = np.fromfile(os.path.join(d, f"tomography_vti_final_model_dl_{nz}x{nx}.bin"), np.float32)
+    vp = np.fromfile(os.path.join(d, f"tomography_vti_final_model_vp_{nz}x{nx}.bin"), np.float32)
+    assert ep.size == dl.size == vp.size == nx * nz
+    assert np.isfinite(ep).all() and np.isfinite(dl).all() and np.isfinite(vp).all()
+    print("mean epsilon", ep.mean(), "mean delta", dl.mean())
