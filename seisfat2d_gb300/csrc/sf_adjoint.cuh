@@ -33,6 +33,10 @@ constexpr int kLookA = 4;
 constexpr int kAheadA = kLookA + 2 * kU;  // a consumer's fall-back distance after a stall
 constexpr int kTR = 12;    // tape ring slots (a multiple of kU, > kLookA + kU)
 constexpr int kTPitch = 72;  // c1[32], c2[32], code bytes (8 words)
+// the prefetch slots b0 + kLookA + u and tb0 + kLookA + u are wrapped once:
+// blocks must tile the lead and both rings
+static_assert(kLookA % kU == 0 && kRing % kU == 0 && kTR % kU == 0, "ring slots of a block would wrap twice");
+static_assert(kTR >= kLookA + kU && kRing >= 32 + kLookA + kU, "ring too small for the lead");
 
 struct AdjRing {
     float L[kRing * kLP];
