@@ -77,8 +77,9 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     const bool consumer = (lane == 0) && (a.h_in != nullptr);
     const int nsteps = ncols + 31;
     auto col_of = [&](int m) { return (SX < 0) ? m : ncols - 1 - m; };
-    // running source addresses of march q (q advances by one per call): the
-    // lambda column, the handoff pairs, and forward tape step ncols+30-q
+    // march q reads lambda column col_of(q), the pairs of march q and forward
+    // tape step ncols+30-q; the pointers below stand at the block's first
+    // march and move once per block, the steps inside a block are offsets
     const long long dL = (SX < 0) ? (long long)nzz : -(long long)nzz;
     const float* pL = lamg + (size_t)(rb + lane) + (long long)col_of(0) * (long long)nzz;
     const unsigned long long* pH = a.h_in;
@@ -86,29 +87,36 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     const float* pT1 = a.tc1 + fs0 + lane;
     const float* pT2 = a.tc2 + fs0 + lane;
     const uint8_t* pTc = a.tcode + fs0 + 4 * lane;
-    auto prefetch = [&](int q, int lslot, int tslot) {
-        if (q < ncols) {
-            if (lt_ok) cp_async4(&Lr[lslot * kLP + lane], pL);
-            if (consumer) cp_async16(&Lr[lslot * kLP + 32], pH);
+    // FAST: every march of the call is inside the window (no bounds tests)
+    auto prefetch = [&](int q, int u, int lslot, int tslot, auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        if (FAST || q < ncols) {
+            if (lt_ok) cp_async4(&Lr[lslot * kLP + lane], pL + u * dL);
+            if (consumer) cp_async16(&Lr[lslot * kLP + 32], pH + 2 * u);
         }
-        if (q < nsteps) {
-            cp_async4(&TPr[tslot * kTPitch + lane], pT1);
-            cp_async4(&TPr[tslot * kTPitch + 32 + lane], pT2);
-            if (lane < 8) cp_async4(&TPr[tslot * kTPitch + 64 + lane], pTc);
+        if (FAST || q < nsteps) {
+            cp_async4(&TPr[tslot * kTPitch + lane], pT1 - 32 * u);
+            cp_async4(&TPr[tslot * kTPitch + 32 + lane], pT2 - 32 * u);
+            if (lane < 8) cp_async4(&TPr[tslot * kTPitch + 64 + lane], pTc - 32 * u);
         }
         cp_commit();
-        pL += dL;
-        pH += 2;
-        pT1 -= 32;
-        pT2 -= 32;
-        pTc -= 32;
+    };
+    auto advance = [&](int n) {
+        pL += n * dL;
+        pH += 2 * n;
+        pT1 -= 32 * n;
+        pT2 -= 32 * n;
+        pTc -= 32 * n;
     };
 
     // let the previous strip get kAheadA columns ahead before the first prefetches
     if (consumer) wait_pair(a.h_in + 2 * (size_t)min(kAheadA, ncols - 1) + 1, a.tag, sh, a.err);
     __syncwarp();
 #pragma unroll 1
-    for (int q = 0; q < kLookA; q++) prefetch(q, q, q % kTR);
+    for (int q = 0; q < kLookA; q++) {
+        prefetch(q, 0, q, q % kTR, std::false_type{});
+        advance(1);
+    }
 
     // running destinations: the term v of forward tape step ncols+30-s, and
     // the write-back of march column s-31 (row r)
@@ -120,15 +128,16 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
 
     // Blocks of kU steps, as in the forward: one wait per block, the block's
     // ring reads, its kU linear updates (the only serial chain), its stores.
-#pragma unroll 1
-    for (int s0 = 0; s0 < nsteps; s0 += kU) {
+    auto block = [&](int s0, auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
         {
             int pf0 = b0 + kLookA;
             if (pf0 >= kRing) pf0 -= kRing;
             int tf0 = tb0 + kLookA;
             if (tf0 >= kTR) tf0 -= kTR;
 #pragma unroll
-            for (int u = 0; u < kU; u++) prefetch(s0 + kLookA + u, pf0 + u, tf0 + u);
+            for (int u = 0; u < kU; u++) prefetch(s0 + kLookA + u, u, pf0 + u, tf0 + u, fast_tag);
+            advance(kU);
         }
         cp_wait<kLookA>();
         __syncwarp();
@@ -162,7 +171,7 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
 #pragma unroll
             for (int u = 0; u < kU; u++) {
                 const int s = s0 + u;
-                if (s < ncols && (tag_of(e0[u]) != a.tag || tag_of(e1[u]) != a.tag)) {
+                if ((FAST || s < ncols) && (tag_of(e0[u]) != a.tag || tag_of(e1[u]) != a.tag)) {
                     e0[u] = pack_tag(wait_pair(a.h_in + 2 * (size_t)s, a.tag, sh, a.err), a.tag);
                     e1[u] = pack_tag(wait_pair(a.h_in + 2 * (size_t)s + 1, a.tag, sh, a.err), a.tag);
                     wait_pair(a.h_in + 2 * (size_t)min(s + kAheadA, ncols - 1) + 1, a.tag, sh, a.err);
@@ -176,12 +185,12 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         for (int u = 0; u < kU; u++) {
             const int s = s0 + u;
             const int m = s - lane;
-            const bool act = vrow && (m >= 0) && (m < ncols);
+            const bool act = FAST ? vrow : (vrow && (m >= 0) && (m < ncols));
             // pv of the upwind row's node in this column plus pev of its node in
             // the previous column, summed by the lane above
             float x_in = __shfl_up_sync(0xffffffffu, my_x, 1);
             if (lane == 0) {  // upwind row of the strip: the previous strip, or outside the grid
-                const bool have = consumer && s < ncols;
+                const bool have = consumer && (FAST || s < ncols);
                 x_in = fadd(have ? val_of(e0[u]) : 0.0f, pev_hold);
                 pev_hold = have ? val_of(e1[u]) : 0.0f;
             }
@@ -215,21 +224,21 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
             const int s = s0 + u;
             if (actv[u]) {
                 Lr[msl[u] * kLP + tix] = lo[u];
-                *pV = vv[u];
+                pV[-32 * u] = vv[u];
                 if (lane == 31 && a.h_out != nullptr) {
                     const int m = s - 31;
                     st_u64(a.h_out + 2 * (size_t)m, pack_tag(opv[u], a.tag));
                     st_u64(a.h_out + 2 * (size_t)m + 1, pack_tag(opev[u], a.tag));
                 }
             }
-            pV -= 32;
         }
+        pV -= 32 * kU;
         int wb = b0 + (kRing - 31);  // slot of march s0 - 31
         if (wb >= kRing) wb -= kRing;
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             const int s = s0 + u;
-            if (s >= 31 && s < nsteps) {
+            if (FAST || (s >= 31 && s < nsteps)) {
                 int ws = wb + u;
                 if (ws >= kRing) ws -= kRing;
                 if (vrow) *pW = Lr[ws * kLP + tix];
@@ -240,6 +249,13 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         if (b0 >= kRing) b0 -= kRing;
         tb0 += kU;
         if (tb0 >= kTR) tb0 -= kTR;
+    };
+#pragma unroll 1
+    for (int s0 = 0; s0 < nsteps; s0 += kU) {
+        if (s0 >= 31 && s0 + kLookA + kU <= ncols)
+            block(s0, std::true_type{});
+        else
+            block(s0, std::false_type{});
     }
     cp_wait<0>();
     __syncwarp();

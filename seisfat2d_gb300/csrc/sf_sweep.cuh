@@ -230,8 +230,10 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     const float* pX = Sg + (size_t)(rb + 31) + (long long)col_of(0) * (long long)ldS;
     const float* pT = Tg + (size_t)(rb + lane) + (long long)col_of(0) * (long long)nzz;
     const long long dS = dcol * (long long)ldS, dT = dcol * (long long)nzz;
-    auto prefetch = [&](int q, int slot) {
-        if (q < ncols) {
+    // FAST: every march the call touches lies inside the window (no bounds tests)
+    auto prefetch = [&](int q, int slot, auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        if (FAST || q < ncols) {
             if (ls_ok) cp_async4(&Sring[slot * kSP + lane], pS);
             if (lx_ok) cp_async4(&Sring[slot * kSP + 32], pX);
             if (!SW0 && lt_ok) cp_async4(&Tring[slot * kTP + lane], pT);
@@ -250,7 +252,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
     // prologue: march columns 0 .. kLook-1
 #pragma unroll 1
-    for (int q = 0; q < kLook; q++) prefetch(q, q);
+    for (int q = 0; q < kLook; q++) prefetch(q, q, std::false_type{});
 
     // running destinations: write-back of march column s-31 (row r), tape entry s*32+lane
     float* pW = Tg + (size_t)r + (long long)col_of(0) * (long long)nzz;
@@ -267,13 +269,13 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     // block's ring reads, its kU node updates, and its stores. Within a block
     // the node updates are the only serial chain; the loads before and the
     // stores after it are independent of it.
-#pragma unroll 1
-    for (int s0 = 0; s0 < nsteps; s0 += kU) {
+    auto block = [&](int s0, auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
         {
             int pf0 = b0 + kLook;
             if (pf0 >= kRing) pf0 -= kRing;
 #pragma unroll
-            for (int u = 0; u < kU; u++) prefetch(s0 + kLook + u, pf0 + u);
+            for (int u = 0; u < kU; u++) prefetch(s0 + kLook + u, pf0 + u, fast_tag);
         }
         // march columns <= s0+kU are staged (SX < 0 reads one column ahead)
         cp_wait<kLook - 1>();
@@ -302,7 +304,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 #pragma unroll
             for (int u = 0; u < kU; u++) {
                 const int s = s0 + u;
-                if (s < ncols && tag_of(pr[u]) != a.tag) {
+                if ((FAST || s < ncols) && tag_of(pr[u]) != a.tag) {
                     pr[u] = pack_tag(wait_pair(a.h_in + s, a.tag, sh, a.err), a.tag);
                     wait_pair(a.h_in + min(s + kAhead, ncols - 1), a.tag, sh, a.err);
                 }
@@ -320,11 +322,11 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         for (int u = 0; u < kU; u++) {
             const int s = s0 + u;
             const int m = s - lane;
-            const bool act = vrow && (m >= 0) && (m < ncols);
+            const bool act = FAST ? vrow : (vrow && (m >= 0) && (m < ncols));
             const int j = col_of(m);
             // upwind value from the lane above (or the previous strip)
             float tv = __shfl_up_sync(0xffffffffu, tn, 1);
-            if (consumer && s < ncols) tv = val_of(pr[u]);
+            if (consumer && (FAST || s < ncols)) tv = val_of(pr[u]);
             const float te = tn, tev = tvp;
 
             float to = told[u];
@@ -338,7 +340,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
             float tnew = to;
             rec[u].code = 0; rec[u].c1 = 0.0f; rec[u].c2 = 0.0f;
-            const bool inner = act && irow && (j >= 1) && (j <= ncols - 2) &&
+            const bool inner = act && irow && (FAST || ((j >= 1) && (j <= ncols - 2))) &&
                                !(r == a.skip_i && j == a.skip_j);
             // rows: i1 (SZ>0: r-1, else r); columns: j-1 (clamped to 1), j
             const float Si1_j = (SZ > 0) ? U_j : I_j;
@@ -382,18 +384,18 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         for (int u = 0; u < kU; u++) {
             const int s = s0 + u;
             if (actv[u]) Tring[msl[u] * kTP + tix] = tnw[u];
-            if (TAPE) {
-                if (s < nsteps) {
-                    *pcode = actv[u] ? rec[u].code : (uint8_t)0;
-                    *pc1 = rec[u].c1;
-                    *pc2 = rec[u].c2;
-                }
-                pcode += 32;
-                pc1 += 32;
-                pc2 += 32;
+            if (TAPE && (FAST || s < nsteps)) {
+                pcode[32 * u] = actv[u] ? rec[u].code : (uint8_t)0;
+                pc1[32 * u] = rec[u].c1;
+                pc2[32 * u] = rec[u].c2;
             }
             // feed the next strip: lane 31 just finished march s-31
             if (lane == 31 && a.h_out != nullptr && actv[u]) st_u64(a.h_out + (s - 31), pack_tag(tnw[u], a.tag));
+        }
+        if (TAPE) {
+            pcode += 32 * kU;
+            pc1 += 32 * kU;
+            pc2 += 32 * kU;
         }
         // write back the columns every lane has finished (march s-31)
         int wb = b0 + (kRing - 31);
@@ -401,7 +403,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             const int s = s0 + u;
-            if (s >= 31 && s < nsteps) {
+            if (FAST || (s >= 31 && s < nsteps)) {
                 int ws = wb + u;
                 if (ws >= kRing) ws -= kRing;
                 if (vrow) *pW = Tring[ws * kTP + tix];
@@ -410,6 +412,13 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         }
         b0 += kU;
         if (b0 >= kRing) b0 -= kRing;
+    };
+#pragma unroll 1
+    for (int s0 = 0; s0 < nsteps; s0 += kU) {
+        if (s0 >= 32 && s0 + kLook + kU <= ncols - 1)
+            block(s0, std::true_type{});
+        else
+            block(s0, std::false_type{});
     }
     cp_wait<0>();
     __syncwarp();
