@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0: engine default)")
     ap.add_argument("--gang", type=int, default=0, help="warps per shot (0: automatic)")
+    ap.add_argument("--strip-loop", default="auto", choices=["auto", "general", "interior"],
+                    help="strip-loop form (fixing it, or --warps/--gang, skips the autotuner)")
     ap.add_argument("--arith", default="reference", choices=["reference", "ieee"])
     ap.add_argument("--nplain", type=int, default=8, help="shots timed one at a time for the plain solver")
     return ap.parse_args()
@@ -274,6 +276,7 @@ def run_ours(a):
     eng.set_arithmetic(a.arith)
     if a.warps or a.gang:
         eng.set_launch(a.warps, a.gang)
+    eng.set_strip_loop(a.strip_loop)
     if ani:
         eng.set_stiffness(w.cij)
     dev = torch.device("cuda", local)
@@ -302,7 +305,7 @@ def run_ours(a):
         # planned batch: shots and receivers stay on the device, the iteration
         # replays from the engine's CUDA graph; the autotuner picks the launch shape
         eng.plan_batch(tab, w.rx, w.rz, stream=stream)
-        if not (a.warps or a.gang):
+        if not (a.warps or a.gang or a.strip_loop != "auto"):
             tuned = eng.plan_autotune(picks, t_obs=obs, grad=grad, misfit=misfit, reps=2, stream=stream)
 
     def step():
@@ -394,7 +397,9 @@ def run_ours(a):
     # --- plain: one shot at a time, spread over the batch, with the engine's
     # default launch shape (the autotuned one belongs to the batch)
     launch_used = eng.get_launch()
+    loop_used = eng.strip_loop()
     eng.set_launch(1, 0)
+    eng.set_strip_loop("auto")
     nplain = max(1, min(a.nplain, len(shots)))
     sel = [shots[q * len(shots) // nplain] for q in range(nplain)]
     Tdev = torch.empty((eng.nxx, eng.nzz), dtype=torch.float32, device=dev)
@@ -467,8 +472,10 @@ def run_ours(a):
                    "parallelism": f"shots sharded over {world} GPU(s)",
                    "l2": "flushed between timed steps (512 MB write)",
                    "launch": {"warps_per_cta": launch_used[0], "warps_per_shot": launch_used[1] or "auto",
-                              "chosen_by": "sf_plan_autotune" if tuned else ("flags" if (a.warps or a.gang) else
-                                                                             "default")},
+                              "strip_loop": {"mode": loop_used[0],
+                                             "form": "interior-block" if loop_used[1] else "general"},
+                              "chosen_by": "sf_plan_autotune" if tuned else (
+                                  "flags" if (a.warps or a.gang or a.strip_loop != "auto") else "default")},
                    "timed_path": ("sf_plan_graph_launch (CUDA graph of the planned iteration)" if fa
                                   else "sf_batch_forward"),
                    "eager_ms_per_step": statistics.mean(eager_ms),

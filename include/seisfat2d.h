@@ -45,6 +45,11 @@ extern "C" {
 #define SF_ARITH_REFERENCE 0 /* the reference build's: FP32 init, nvcc's FMAs (default) */
 #define SF_ARITH_IEEE 1      /* every operation rounded once, FP64 3x3 initialisation */
 
+/* strip-loop forms (sf_set_strip_loop) */
+#define SF_LOOP_AUTO -1    /* interior-block body when all shots run at once, one window width, a warp per strip */
+#define SF_LOOP_GENERAL 0  /* one loop body with bounds tests in every block            */
+#define SF_LOOP_INTERIOR 1 /* blocks inside the window run a body without bounds tests   */
+
 /* sf_batch_forward flags */
 #define SF_KEEP_TAPE 1   /* record the update tape for sf_batch_adjoint      */
 #define SF_KEEP_TABLES 2 /* keep every shot's traveltime window on device   */
@@ -173,6 +178,17 @@ int sf_time_propagation_noalloc(const float* S, int nx, int nz, float dx, float 
 int sf_set_launch(sf_ctx* ctx, int warps, int gang_warps);
 int sf_get_launch(const sf_ctx* ctx, int* warps, int* gang_warps);
 
+/* Form of the strip loops of the forward and reverse sweeps (no counterpart
+ * in the reference). Both forms compute the same bits; the interior-block
+ * form runs fewer instructions per step but is larger code, which measured
+ * faster for a batch whose shots all run at once with one window width and
+ * one warp per strip, slower for uneven windows or several strips per warp.
+ * SF_LOOP_AUTO (default) chooses per batch;
+ * sf_plan_autotune times both. last_interior: whether the last batch's
+ * forward used the interior-block form (the reverse sweeps follow it). */
+int sf_set_strip_loop(sf_ctx* ctx, int mode);
+int sf_get_strip_loop(const sf_ctx* ctx, int* mode, int* last_interior);
+
 /* ---- planned batches, CUDA graphs, autotuner (no counterpart in the
  * reference, which solves one shot per call: inversion.cpp:52-67 and
  * migration.cu:116-171 loop over time_propagation) ----
@@ -205,8 +221,9 @@ int sf_plan_graph_launch(sf_ctx* ctx, const float* t_obs, float* picks, double* 
                          void* stream);
 /* Autotuner: times `reps` iterations of the plan for each candidate launch
  * shape (1, 2, 4 warps per CTA x automatic, all, 1/2, 1/3, 1/4 of the strips
- * per gang), keeps the fastest (as sf_set_launch would) and reports it.
- * Every shape computes the same bits. Synchronises `stream`. */
+ * per gang; under SF_LOOP_AUTO also both strip-loop forms), keeps the fastest
+ * (as sf_set_launch and sf_set_strip_loop would) and reports its launch
+ * shape. Every shape computes the same bits. Synchronises `stream`. */
 int sf_plan_autotune(sf_ctx* ctx, const float* t_obs, float* picks, double* misfit, float* grad, int reps,
                      void* stream, int* best_warps, int* best_gang_warps, float* best_ms);
 

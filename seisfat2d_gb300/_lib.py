@@ -58,6 +58,8 @@ SIGNATURES = {
     "sf_set_arithmetic": (C.c_int, [VP, C.c_int]),
     "sf_get_arithmetic": (C.c_int, [VP, IP]),
     "sf_get_launch": (C.c_int, [VP, IP, IP]),
+    "sf_set_strip_loop": (C.c_int, [VP, C.c_int]),
+    "sf_get_strip_loop": (C.c_int, [VP, IP, IP]),
     "sf_time_propagation_noalloc": (C.c_int, [VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                                               C.c_float, VP, VP]),
     "sf_plan_batch": (C.c_int, [VP, C.POINTER(sf_shot), C.c_int, VP, VP, C.c_int, VP]),

@@ -21,6 +21,20 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-O2",
 ]
 UNITS = ["sf_engine.cu", "sf_adjoint.cu", "sf_plan.cu", "sf_update.cu", "sf_migration.cu"]
+# k_shots instantiations, one object each from sf_shots_inst.cu:
+# (tape, reference arithmetic, anisotropic taped, interior-block strip loops)
+KSHOTS = [(0, 0, 0, 0), (0, 0, 0, 1), (0, 1, 0, 0), (0, 1, 0, 1), (1, 0, 0, 0), (1, 0, 0, 1),
+          (1, 1, 0, 0), (1, 1, 0, 1), (1, 0, 1, 0), (1, 1, 1, 0)]
+
+
+def _jobs():
+    """(source, extra nvcc flags, object name) of every translation unit."""
+    jobs = [(u, [], u.replace(".cu", ".o")) for u in UNITS]
+    for v in KSHOTS:
+        tag = "".join(str(b) for b in v)
+        defs = [f"-DSF_{k}={'true' if b else 'false'}" for k, b in zip(("TAPE", "REF", "VTI", "INTERIOR"), v)]
+        jobs.append(("sf_shots_inst.cu", defs + [f"-DSF_KSHOTS_NAME=sf_kshots_{tag}"], f"sf_shots_{tag}.o"))
+    return jobs
 
 
 def _nvcc():
@@ -49,18 +63,20 @@ def build(force=False, verbose=False, ptxas_info=False):
     nvcc = _nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
 
-    def compile_unit(u):
-        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
-        cmd = [nvcc] + NVCC_FLAGS + extra + ["-I", INC, "-c", os.path.join(CSRC, u), "-o", obj]
+    def compile_unit(job):
+        u, defs, oname = job
+        obj = os.path.join(BUILD, oname)
+        cmd = [nvcc] + NVCC_FLAGS + extra + defs + ["-I", INC, "-c", os.path.join(CSRC, u), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0 or verbose or ptxas_info:
             print(r.stdout + r.stderr)
         if r.returncode != 0:
-            raise RuntimeError("nvcc failed on " + u)
+            raise RuntimeError("nvcc failed on " + oname)
         return obj
 
-    with cf.ThreadPoolExecutor(len(UNITS)) as ex:
-        objs = list(ex.map(compile_unit, UNITS))
+    jobs = _jobs()
+    with cf.ThreadPoolExecutor(min(len(jobs), max(4, os.cpu_count() or 4))) as ex:
+        objs = list(ex.map(compile_unit, jobs))
     tmp = LIB + ".tmp"
     subprocess.run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"], check=True)
     os.replace(tmp, LIB)

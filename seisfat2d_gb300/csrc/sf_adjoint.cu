@@ -32,7 +32,9 @@ size_t sf_adj_smem_bytes(int warps)
 
 int sf_adj_setup(sf_ctx* c)
 {
-    CK(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CK(cudaFuncSetAttribute(k_adjoint<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sf_adj_smem_bytes(kMaxWarps)));
+    CK(cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sf_adj_smem_bytes(kMaxWarps)));
     return SF_OK;
 }
@@ -167,7 +169,9 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     const int nstrips = (c->nzz + 31) / 32;
     const size_t smem = sf_adj_smem_bytes(c->warps);
     int G, NG;
-    int rc = sf_gang_shape(c, (const void*)k_adjoint, smem, ns, nstrips, c->gang_warps, &G, &NG);
+    // the reverse sweeps take the loop form of the taped forward they reverse
+    const void* akern = c->batch_interior ? (const void*)k_adjoint<true> : (const void*)k_adjoint<false>;
+    int rc = sf_gang_shape(c, akern, smem, ns, nstrips, c->gang_warps, &G, &NG);
     if (rc) return rc;
     rc = sf_dev_reserve(c, (void**)&c->d_lam, &c->cap_lam, (size_t)NG * c->nzz * c->batch_maxcols * sizeof(float));
     if (!rc) rc = sf_dev_reserve_zero(c, (void**)&c->d_hand2, &c->cap_hand2,
@@ -237,7 +241,7 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
         g.grad_c11 = c->d_gcij;
         g.grad_c13 = c->d_gcij + npad;
     }
-    A->kern = (const void*)k_adjoint;
+    A->kern = akern;
     A->gkern = c->batch_ani ? (const void*)k_gather<true> : (const void*)k_gather<false>;
     A->grid = dim3(NG * G);
     A->block = dim3(c->warps * 32);

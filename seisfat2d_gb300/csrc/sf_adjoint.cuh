@@ -57,8 +57,9 @@ struct AdjStripArgs {
     int* err;
 };
 
-// SZ, SX: signs of the forward sweep being reversed.
-template <int SZ, int SX>
+// SZ, SX: signs of the forward sweep being reversed. INTERIOR: blocks whose
+// marches all lie inside the window run a body without bounds tests.
+template <int SZ, int SX, bool INTERIOR>
 __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
 {
     const int lane = threadIdx.x & 31;
@@ -252,10 +253,14 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
     };
 #pragma unroll 1
     for (int s0 = 0; s0 < nsteps; s0 += kU) {
-        if (s0 >= 31 && s0 + kLookA + kU <= ncols)
-            block(s0, std::true_type{});
-        else
+        if constexpr (INTERIOR) {
+            if (s0 >= 31 && s0 + kLookA + kU <= ncols)
+                block(s0, std::true_type{});
+            else
+                block(s0, std::false_type{});
+        } else {
             block(s0, std::false_type{});
+        }
     }
     cp_wait<0>();
     __syncwarp();
@@ -263,12 +268,13 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
 
 // (kMaxWarps * 32, 1): the block size alone as the bound caps the kernel at
 // 64 registers and spills the strip loop's state.
+template <bool INTERIOR>
 __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
     AdjRing* rings = reinterpret_cast<AdjRing*>(smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15)));
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x;
     const GangPos gp = gang_pos(p.G);
     const int nzz = p.nzz, nstrips = p.nstrips;
     float* lam = p.lam + (size_t)gp.gang * p.lam_per_gang;
@@ -338,10 +344,10 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
                 a.tc1 = p.tc1 + tb;
                 a.tc2 = p.tc2 + tb;
                 switch (sw) {
-                case 0: adj_strip<1, 1>(a); break;
-                case 1: adj_strip<-1, 1>(a); break;
-                case 2: adj_strip<1, -1>(a); break;
-                default: adj_strip<-1, -1>(a); break;
+                case 0: adj_strip<1, 1, INTERIOR>(a); break;
+                case 1: adj_strip<-1, 1, INTERIOR>(a); break;
+                case 2: adj_strip<1, -1, INTERIOR>(a); break;
+                default: adj_strip<-1, -1, INTERIOR>(a); break;
                 }
             }
         }

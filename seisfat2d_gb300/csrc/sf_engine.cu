@@ -237,6 +237,24 @@ extern "C" int sf_get_arithmetic(const sf_ctx* c, int* mode)
     return SF_OK;
 }
 
+extern "C" int sf_set_strip_loop(sf_ctx* c, int mode)
+{
+    if (!c) return SF_ERR_ARG;
+    if (mode != SF_LOOP_AUTO && mode != SF_LOOP_GENERAL && mode != SF_LOOP_INTERIOR)
+        return sf_fail(c, SF_ERR_ARG, "unknown strip-loop mode");
+    c->strip_loop = mode;
+    c->plan_dirty = true;
+    return SF_OK;
+}
+
+extern "C" int sf_get_strip_loop(const sf_ctx* c, int* mode, int* last_interior)
+{
+    if (!c) return SF_ERR_ARG;
+    if (mode) *mode = c->strip_loop;
+    if (last_interior) *last_interior = c->batch_interior ? 1 : 0;
+    return SF_OK;
+}
+
 extern "C" int sf_get_launch(const sf_ctx* c, int* warps, int* gang_warps)
 {
     if (!c) return SF_ERR_ARG;
@@ -299,15 +317,69 @@ int sf_verify_divisors(sf_ctx* c)
     return SF_OK;
 }
 
+namespace sf {
+// accessors of the k_shots instantiations: tape, reference arithmetic,
+// anisotropic taped (VTI), interior-block body
+const void* sf_kshots_0000();
+const void* sf_kshots_0001();
+const void* sf_kshots_0100();
+const void* sf_kshots_0101();
+const void* sf_kshots_1000();
+const void* sf_kshots_1001();
+const void* sf_kshots_1100();
+const void* sf_kshots_1101();
+const void* sf_kshots_1010();
+const void* sf_kshots_1110();
+}  // namespace sf
+
+// Anisotropic taped batches run the general loops only.
+const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior)
+{
+    vti = vti && tape;
+    if (vti) interior = false;
+    switch (((int)tape << 3) | ((int)ref << 2) | ((int)vti << 1) | (int)interior) {
+    case 0x0: return sf::sf_kshots_0000();
+    case 0x1: return sf::sf_kshots_0001();
+    case 0x4: return sf::sf_kshots_0100();
+    case 0x5: return sf::sf_kshots_0101();
+    case 0x8: return sf::sf_kshots_1000();
+    case 0x9: return sf::sf_kshots_1001();
+    case 0xc: return sf::sf_kshots_1100();
+    case 0xd: return sf::sf_kshots_1101();
+    case 0xa: return sf::sf_kshots_1010();
+    case 0xe: return sf::sf_kshots_1110();
+    default: return nullptr;
+    }
+}
+
+// The interior-block body saves instructions per step but adds code. It
+// measured faster for 100 equal windows of 1707 x 357 with every shot at once
+// and one warp per strip (forward 3.93 -> 3.58 ms, reverse sweeps 6.66 ->
+// 5.46 ms), and slower for 1000 windows of 2-8 km with four strips per warp
+// (forward 46 -> 55 ms, reverse 46 -> 67 ms) and for 200 equal windows with
+// two strips per warp (9.39 -> 9.67 ms). SF_LOOP_AUTO takes it only when all
+// three conditions of the first case hold.
+bool sf_interior_loops(sf_ctx* c, const void* kernel, size_t smem, int G)
+{
+    if (c->strip_loop == SF_LOOP_GENERAL) return false;
+    if (c->strip_loop == SF_LOOP_INTERIOR) return true;
+    const int ns = (int)c->hshots.size();
+    if (ns == 0) return false;
+    if (c->hshots.front().ncols != c->hshots.back().ncols) return false;  // sorted widest first
+    if ((long long)G * c->warps < (c->nzz + 31) / 32) return false;       // a warp per strip
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, c->warps * 32, smem) != cudaSuccess)
+        return false;
+    return (long long)ns * G <= (long long)per_sm * c->sms;
+}
+
 int sf_fwd_setup(sf_ctx* c)
 {
     size_t mx = sf_fwd_smem_bytes(kMaxWarps);
-    CK(cudaFuncSetAttribute(k_shots<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_shots<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_shots<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_shots<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_shots<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_shots<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    for (int k = 0; k < 16; k++) {
+        const void* f = sf_kshots_kernel(k & 8, k & 4, k & 2, k & 1);
+        if (f) CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    }
     return sf_adj_setup(c);
 }
 
@@ -522,12 +594,12 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     const size_t smem = sf_fwd_smem_bytes(c->warps);
     const bool ref = c->arith == SF_ARITH_REFERENCE;
     const bool vti = tape && ani;
-    const void* kern = vti ? (ref ? (const void*)k_shots<true, true, true> : (const void*)k_shots<true, false, true>)
-                     : ref ? (tape ? (const void*)k_shots<true, true> : (const void*)k_shots<false, true>)
-                           : (tape ? (const void*)k_shots<true, false> : (const void*)k_shots<false, false>);
+    const void* kern = sf_kshots_kernel(tape, ref, vti, false);
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
     if (rc) return rc;
+    c->batch_interior = !vti && sf_interior_loops(c, kern, smem, G);
+    if (c->batch_interior) kern = sf_kshots_kernel(tape, ref, vti, true);
     if ((long long)(nshots + NG - 1) / NG * (ani ? 2 : 1) > 1023)
         return sf_fail(c, SF_ERR_ARG, "too many shots per gang for one launch; split the batch");
     c->last_G = G;

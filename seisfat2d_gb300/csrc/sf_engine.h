@@ -43,6 +43,8 @@ struct sf_ctx {
     int sms = 1;
     int warps = 1;        // warps per CTA
     int gang_warps = 0;   // warps solving one shot (0: chosen per batch)
+    int strip_loop = -1;  // strip loops: SF_LOOP_* (sf_set_strip_loop)
+    bool batch_interior = false;  // the last batch's forward ran the interior-block body
     int arith = SF_ARITH_REFERENCE;
     std::string err;
 
@@ -152,6 +154,10 @@ int sf_check_flags(sf_ctx* c, cudaStream_t st);
 int sf_fwd_setup(sf_ctx* c);
 int sf_verify_divisors(sf_ctx* c);
 size_t sf_fwd_smem_bytes(int warps);
+// k_shots instantiation (one object file each, sf_shots_inst.cu)
+const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior);
+// whether the batch of hshots, G CTAs per shot, runs the interior-block body
+bool sf_interior_loops(sf_ctx* c, const void* kernel, size_t smem, int G);
 void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4]);
 int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape);
 int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,

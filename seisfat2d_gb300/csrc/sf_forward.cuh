@@ -102,7 +102,7 @@ __device__ __forceinline__ GangPos gang_pos(int G)
 // runs the strips of its slot. No barrier between sweeps: consecutive sweeps
 // run the rows in opposite directions, a warp rereads only rows it wrote
 // itself, and the handoff chain orders everything else.
-template <bool TAPE, bool REF>
+template <bool TAPE, bool REF, bool INTERIOR>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPos& gp, const float* Sw,
                              int ldS, float* T, unsigned tag, CtaShared* cs, WarpRing* rings)
 {
@@ -146,10 +146,10 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
                 a.tc2 = p.tc2 + base;
             }
             switch (sw) {
-            case 0: run_strip<1, 1, true, TAPE, REF>(a); break;
-            case 1: run_strip<-1, 1, false, TAPE, REF>(a); break;
-            case 2: run_strip<1, -1, false, TAPE, REF>(a); break;
-            default: run_strip<-1, -1, false, TAPE, REF>(a); break;
+            case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR>(a); break;
+            case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR>(a); break;
+            case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR>(a); break;
+            default: run_strip<-1, -1, false, TAPE, REF, INTERIOR>(a); break;
             }
         }
     }
@@ -159,8 +159,9 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
 // sorted widest window first). The grid never exceeds what the device can
 // hold at once, so every gang's CTAs are resident together. VTI (with TAPE):
 // anisotropic shots whose second (qP) solve is taped, with the qP pass
-// writing its derivative factors.
-template <bool TAPE, bool REF, bool VTI = false>
+// writing its derivative factors. INTERIOR: the strip loops' bounds-test-free
+// body for interior blocks (see run_strip).
+template <bool TAPE, bool REF, bool VTI, bool INTERIOR>
 // (kMaxWarps * 32, 1): with the block size alone as the bound ptxas caps the
 // kernel at 64 registers and spills the strip loop's state to local memory.
 __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
         const unsigned tag = (p.epoch << 10) | (unsigned)((it * nsolves) & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE && !VTI, REF>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
+        solve_window<TAPE && !VTI, REF, INTERIOR>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
         if (p.ani) {
             // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
             // warp's strips, once the whole first solve is done
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
                         __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
             }
             __syncthreads();
-            solve_window<TAPE, REF>(p, sh, gp, Sq, nzz, T, tag + 1u, cs, rings);
+            solve_window<TAPE, REF, INTERIOR>(p, sh, gp, Sq, nzz, T, tag + 1u, cs, rings);
         }
         // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {

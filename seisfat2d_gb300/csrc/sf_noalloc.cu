@@ -53,7 +53,7 @@ int noalloc_setup(int dev, unsigned char** addr)
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SF_ERR_CUDA;
-        if (cudaFuncSetAttribute(k_shots<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(sf_kshots_kernel(false, true, false, true), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sf_fwd_smem_bytes(kMaxWarps)) != cudaSuccess)
             return SF_ERR_CUDA;
         // the tagged pairs must not start with a valid-looking tag
@@ -135,8 +135,10 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     p.bar = &dh->bar;
     p.epoch = epoch;
     const int warps = 8;
-    k_shots<false, true><<<1, warps * 32, sf_fwd_smem_bytes(warps), st>>>(p);
-    if (cudaGetLastError() != cudaSuccess) return SF_ERR_CUDA;
+    void* args[] = {&p};
+    if (cudaLaunchKernel(sf_kshots_kernel(false, true, false, true), dim3(1), dim3(warps * 32), args,
+                         sf_fwd_smem_bytes(warps), st) != cudaSuccess)
+        return SF_ERR_CUDA;
     int err = 0;
     if (cudaMemcpyAsync(&err, &dh->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return SF_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return SF_ERR_CUDA;

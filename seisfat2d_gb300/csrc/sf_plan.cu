@@ -229,16 +229,22 @@ extern "C" int sf_plan_autotune(sf_ctx* c, const float* t_obs, float* picks, dou
     std::sort(gangs.begin(), gangs.end());
     gangs.erase(std::unique(gangs.begin(), gangs.end()), gangs.end());
     const int warps_c[] = {1, 2, 4};
-    const int w0 = c->warps, g0 = c->gang_warps;
-    int bw = w0, bg = g0;
+    const int w0 = c->warps, g0 = c->gang_warps, l0 = c->strip_loop;
+    // both strip-loop forms unless the caller fixed one
+    std::vector<int> loops;
+    if (l0 == SF_LOOP_AUTO) loops = {SF_LOOP_GENERAL, SF_LOOP_INTERIOR};
+    else loops = {l0};
+    int bw = w0, bg = g0, bl = l0;
     float bms = -1.0f;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
+    for (int lp : loops)
     for (int w : warps_c) {
         for (int g : gangs) {
             c->warps = w;
             c->gang_warps = g;
+            c->strip_loop = lp;
             rc = plan_configure(c, st);
             if (!rc) rc = plan_enqueue(c, t_obs, picks, misfit, grad, sf_next_epoch(c), sf_next_epoch(c), st);
             if (!rc) rc = sf_cuda_check(c, cudaEventRecord(e0, st), "cudaEventRecord");
@@ -255,6 +261,7 @@ extern "C" int sf_plan_autotune(sf_ctx* c, const float* t_obs, float* picks, dou
                 bms = ms;
                 bw = w;
                 bg = g;
+                bl = lp;
             }
         }
         if (rc) break;
@@ -263,6 +270,7 @@ extern "C" int sf_plan_autotune(sf_ctx* c, const float* t_obs, float* picks, dou
     cudaEventDestroy(e1);
     c->warps = rc ? w0 : bw;
     c->gang_warps = rc ? g0 : bg;
+    c->strip_loop = rc ? l0 : bl;
     int rc2 = plan_configure(c, st);
     if (rc) return rc;
     if (rc2) return rc2;

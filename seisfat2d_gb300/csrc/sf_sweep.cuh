@@ -193,7 +193,10 @@ __device__ __forceinline__ unsigned wait_counter(const unsigned* p, unsigned tar
     return v;
 }
 
-template <int SZ, int SX, bool SW0, bool TAPE, bool REF>
+// INTERIOR: blocks whose marches all lie inside the window run a body without
+// bounds tests (fewer instructions per step, more code); otherwise every block
+// runs the general body. Both give the same bits.
+template <int SZ, int SX, bool SW0, bool TAPE, bool REF, bool INTERIOR>
 __device__ __forceinline__ void run_strip(const StripArgs& a)
 {
     constexpr int kU = FwdBlock<TAPE>::U, kLook = FwdBlock<TAPE>::LOOK, kAhead = FwdBlock<TAPE>::AHEAD;
@@ -415,10 +418,14 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     };
 #pragma unroll 1
     for (int s0 = 0; s0 < nsteps; s0 += kU) {
-        if (s0 >= 32 && s0 + kLook + kU <= ncols - 1)
-            block(s0, std::true_type{});
-        else
+        if constexpr (INTERIOR) {
+            if (s0 >= 32 && s0 + kLook + kU <= ncols - 1)
+                block(s0, std::true_type{});
+            else
+                block(s0, std::false_type{});
+        } else {
             block(s0, std::false_type{});
+        }
     }
     cp_wait<0>();
     __syncwarp();

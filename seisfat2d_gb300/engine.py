@@ -396,6 +396,17 @@ class Engine:
         """warps per CTA (0 keeps it) and warps per shot (0: automatic)."""
         self._check(self.L.sf_set_launch(self._ctx, int(warps), int(gang_warps)), "sf_set_launch")
 
+    def set_strip_loop(self, mode):
+        """'auto', 'general' or 'interior' (sf_set_strip_loop)."""
+        m = {"auto": -1, "general": 0, "interior": 1}[mode]
+        self._check(self.L.sf_set_strip_loop(self._ctx, m), "sf_set_strip_loop")
+
+    def strip_loop(self):
+        """(mode, whether the last batch ran the interior-block form)."""
+        m, last = C.c_int(), C.c_int()
+        self._check(self.L.sf_get_strip_loop(self._ctx, C.byref(m), C.byref(last)), "sf_get_strip_loop")
+        return {-1: "auto", 0: "general", 1: "interior"}[m.value], bool(last.value)
+
     def get_launch(self):
         a, b = C.c_int(), C.c_int()
         self.L.sf_get_launch(self._ctx, C.byref(a), C.byref(b))
