@@ -391,6 +391,43 @@ struct GatherSmem {
     GatherShot shots[kGChunk];
 };
 
+// One stage's node terms for the thread's four cells when the tile lies inside
+// the shot's window and is not the last strip: the same terms and order as the
+// general loop of k_gather (cells q, corners (0,0),(0,1),(1,0),(1,1)), with the
+// 16 node slots one base plus offsets fixed by the sweep's directions.
+template <bool SZPOS, bool SXPOS>
+__device__ __forceinline__ void gather_interior(const GatherStage& S, float g[4], int a, int rb, int bl0, int ncols,
+                                                int fmlo, bool last_row)
+{
+    const unsigned char* cbytes = reinterpret_cast<const unsigned char*>(S.code);
+    // node (ni, nj) = (a + 1 - dr, bl + 1 - dc) of cell (a, bl), bl = bl0 + 8q
+    const int fl0 = SZPOS ? a + 1 - rb : rb + 31 - (a + 1);
+    const int fm0 = SXPOS ? bl0 + 1 : ncols - 1 - (bl0 + 1);
+    const int base = (fm0 + fl0 - fmlo) * 32 + fl0;
+    constexpr int DR = SZPOS ? -33 : 33;    // ni - 1: fl -/+ 1
+    constexpr int DC = SXPOS ? -32 : 32;    // nj - 1: fm -/+ 1
+    constexpr int DQ = SXPOS ? 256 : -256;  // nj + 8: fm +/- 8
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int dr = 0; dr < 2; dr++)
+#pragma unroll
+            for (int dc = 0; dc < 2; dc++) {
+                int cd;
+                float v;
+                if (dr == 0 && last_row) {  // node row a + 1: the next strip's first row
+                    const int q2 = (SXPOS ? bl0 + 8 * q + 1 - dc : ncols - 1 - (bl0 + 8 * q + 1 - dc)) - fmlo;
+                    cd = (S.code2[q2] >> (SZPOS ? 0 : 24)) & 0xff;
+                    v = S.v2[q2];
+                } else {
+                    const int idx = base + q * DQ + dr * DR + dc * DC;
+                    cd = cbytes[idx];
+                    v = S.v[idx];
+                }
+                if ((cd & 7) && (cd & 0x18) == ((dr << 3) | (dc << 4))) g[q] = fadd(g[q], v);
+            }
+}
+
 // VTI: the batch was anisotropic; each shot's summed terms (its gradient with
 // respect to its own qP slowness) are multiplied by the shot's derivative
 // factors of the qP slowness before the FP64 sum over shots, giving dJ/dS,
@@ -474,11 +511,24 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
             fm_range(t, sw, fmlo, fmhi);
             const GatherStage& S = sm.stg[i % kGStages];
             const unsigned char* cbytes = reinterpret_cast<const unsigned char*>(S.code);
+            // the tile's cells and their nodes all inside the window, rows below the last strip
+            const bool interior = (c >= t.c0) && (c + kGT - t.c0 <= t.ncols - 1) && (rb + 33 <= p.nzz);
+            if (interior) {
+                const int bl0 = c + cq - t.c0;
+                const bool last_row = a == rb + 31;
+                switch (sw) {
+                case 0: gather_interior<true, true>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                case 1: gather_interior<false, true>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                case 2: gather_interior<true, false>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                default: gather_interior<false, false>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                }
+            }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int bc = c + cq + 8 * q;
                 const int bl = bc - t.c0;
                 if (a >= p.nzz || bc >= p.nxx || bl < 0 || bl >= t.ncols) continue;
+                if (!interior)
                 for (int dr = 0; dr < 2; dr++)
                     for (int dc = 0; dc < 2; dc++) {
                         const int ni = a + 1 - dr, nj = bl + 1 - dc;
