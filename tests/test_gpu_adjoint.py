@@ -137,3 +137,27 @@ def test_strip_loop_forms_same_bits(oracle, engine_lib, cuda, arith):
     assert e.strip_loop() == ("auto", True)
     e.batch_forward([(150.0, 0.0, 0, 90), (700.0, 0.0, 40, 110)], rx, rz)
     assert e.strip_loop() == ("auto", False)
+
+
+@pytest.mark.parametrize("arith", ["ieee", "reference"])
+def test_strip_loop_forms_same_bits_windows(engine_lib, cuda, arith):
+    """Forced interior-block loops on windowed shots (offsets, widths from too
+    narrow for any interior block to wide, sources near window edges) give
+    the general loops' bits: picks, tables, misfit, gradient."""
+    e, m = setup(nx=160, nz=80, seed=12, arith=arith)
+    rx, rz = surface_receivers(e.nx, 10.0, step=2)
+    shots = [(200.0, 0.0, 10, 30), (500.0, 60.0, 30, 44), (900.0, 20.0, 50, 90), (1300.0, 150.0, 100, 66),
+             (1500.0, 0.0, 0, 166)]
+    res = {}
+    for mode in ("general", "interior"):
+        e.set_strip_loop(mode)
+        pk = e.batch_forward(shots, rx, rz, keep_tables=True)
+        tabs = [e.batch_table(k, s[3]) for k, s in enumerate(shots)]
+        pk2 = e.batch_forward(shots, rx, rz, keep_tape=True)
+        J, g = e.misfit_gradient(np.nan_to_num(pk2) + np.float32(0.02))
+        res[mode] = (pk, tabs, pk2, J, g)
+    a, b = res["general"], res["interior"]
+    assert np.array_equal(a[0], b[0], equal_nan=True) and np.array_equal(a[2], b[2], equal_nan=True)
+    for ta, tb in zip(a[1], b[1]):
+        assert np.array_equal(ta, tb)
+    assert a[3] == b[3] and np.array_equal(a[4], b[4]) and np.abs(a[4]).max() > 0
