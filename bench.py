@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0: engine default)")
     ap.add_argument("--gang", type=int, default=0, help="warps per shot (0: automatic)")
+    ap.add_argument("--no-fused-gather", action="store_true", help="gather in its own launch")
     ap.add_argument("--strip-loop", default="auto", choices=["auto", "general", "interior"],
                     help="strip-loop form (fixing it, or --warps/--gang, skips the autotuner)")
     ap.add_argument("--arith", default="reference", choices=["reference", "ieee"])
@@ -277,6 +278,7 @@ def run_ours(a):
     if a.warps or a.gang:
         eng.set_launch(a.warps, a.gang)
     eng.set_strip_loop(a.strip_loop)
+    eng.set_fused_gather(not a.no_fused_gather)
     if ani:
         eng.set_stiffness(w.cij)
     dev = torch.device("cuda", local)
@@ -405,6 +407,7 @@ def run_ours(a):
     # default launch shape (the autotuned one belongs to the batch)
     launch_used = eng.get_launch()
     loop_used = eng.strip_loop()
+    fused_used = eng.fused_gather()[1]
     eng.set_launch(1, 0)
     eng.set_strip_loop("auto")
     nplain = max(1, min(a.nplain, len(shots)))
@@ -451,12 +454,18 @@ def run_ours(a):
     kname = "k_shots_tape" if fa else ("k_shots_ani" if ani else "k_shots")
     stages = {"forward": {"kernel": "sf::k_shots<tape>" if fa else "sf::k_shots", "ms": kt["forward"],
                           "algorithmic_bytes": fwd_bpc * cells, "traffic_file": f"{kname}_cfg{a.config}.txt"}}
-    if fa:
+    if fa and "gather" in kt:
         stages["adjoint"] = {"kernel": "sf::k_adjoint", "ms": kt["adjoint"],
                              "algorithmic_bytes": (BYTES_PER_CELL_ADJ - 8) * cells,
                              "traffic_file": f"k_adjoint_cfg{a.config}.txt"}
         stages["gather"] = {"kernel": "sf::k_gather", "ms": kt["gather"], "algorithmic_bytes": 8 * cells,
                             "traffic_file": f"k_gather_cfg{a.config}.txt"}
+    elif fa:
+        # reverse sweeps and gather in one launch (sf_set_fused_gather)
+        stages["adjoint"] = {"kernel": "sf::k_adjoint_gather (reverse sweeps + gather)", "ms": kt["adjoint"],
+                             "algorithmic_bytes": BYTES_PER_CELL_ADJ * cells,
+                             "traffic_file": f"k_adjoint_gather_cfg{a.config}.txt"}
+    if fa:
         stages["residual"] = {"kernel": "sf::k_residual", "ms": kt["residual"],
                               "algorithmic_bytes": 3 * 4 * len(shots) * nrec, "traffic_file": None}
     for st in stages.values():
@@ -481,6 +490,7 @@ def run_ours(a):
                    "launch": {"warps_per_cta": launch_used[0], "warps_per_shot": launch_used[1] or "auto",
                               "strip_loop": {"mode": loop_used[0],
                                              "form": "interior-block" if loop_used[1] else "general"},
+                              "gather": "inside the reverse-sweep launch" if fused_used else "own launch",
                               "chosen_by": "sf_plan_autotune" if tuned else (
                                   "flags" if (a.warps or a.gang or a.strip_loop != "auto") else "default")},
                    "timed_path": ("sf_plan_graph_launch (CUDA graph of the planned iteration)" if fa
@@ -501,7 +511,7 @@ def run_ours(a):
         "plain": {"forward_ms_per_shot": plain_ms, "forward_shots_per_s": 1e3 / plain_ms,
                   "path": "sf_time_propagation + sf_compute_seismogram, one shot per call",
                   "batched_vs_plain_forward": value / world / (1e3 / plain_ms)},
-        "gpu_launches": a.steps * (4 if fa else 1),
+        "gpu_launches": a.steps * ((4 if "gather" in kt else 3) if fa else 1),
         "clocks": clk.summary(),
         "wall_s_timed": wall,
     }

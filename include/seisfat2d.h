@@ -189,6 +189,16 @@ int sf_get_launch(const sf_ctx* ctx, int* warps, int* gang_warps);
 int sf_set_strip_loop(sf_ctx* ctx, int mode);
 int sf_get_strip_loop(const sf_ctx* ctx, int* mode, int* last_interior);
 
+/* Gradient gather inside the reverse-sweep launch (no counterpart in the
+ * reference; default on). With 2 or 4 warps per CTA and an isotropic batch,
+ * and when the device holds every reverse-sweep CTA plus gather CTAs at
+ * once, one launch runs both: each gather tile starts as soon as every shot's
+ * last reverse sweep has finished its columns in the tile's strip and the
+ * next, instead of after the whole reverse pass. Same bits either way.
+ * last_fused: whether the last adjoint ran fused. */
+int sf_set_fused_gather(sf_ctx* ctx, int enable);
+int sf_get_fused_gather(const sf_ctx* ctx, int* enable, int* last_fused);
+
 /* ---- planned batches, CUDA graphs, autotuner (no counterpart in the
  * reference, which solves one shot per call: inversion.cpp:52-67 and
  * migration.cu:116-171 loop over time_propagation) ----

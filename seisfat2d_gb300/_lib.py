@@ -59,6 +59,8 @@ SIGNATURES = {
     "sf_get_arithmetic": (C.c_int, [VP, IP]),
     "sf_get_launch": (C.c_int, [VP, IP, IP]),
     "sf_set_strip_loop": (C.c_int, [VP, C.c_int]),
+    "sf_set_fused_gather": (C.c_int, [VP, C.c_int]),
+    "sf_get_fused_gather": (C.c_int, [VP, IP, IP]),
     "sf_get_strip_loop": (C.c_int, [VP, IP, IP]),
     "sf_time_propagation_noalloc": (C.c_int, [VP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                                               C.c_float, VP, VP]),

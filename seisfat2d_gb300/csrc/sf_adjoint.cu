@@ -36,6 +36,10 @@ int sf_adj_setup(sf_ctx* c)
                             (int)sf_adj_smem_bytes(kMaxWarps)));
     CK(cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sf_adj_smem_bytes(kMaxWarps)));
+    const int fs = (int)std::max(sf_adj_smem_bytes(kMaxWarps), sizeof(GatherSmem));
+    for (const void* f : {(const void*)k_adjoint_gather<false, 2>, (const void*)k_adjoint_gather<true, 2>,
+                          (const void*)k_adjoint_gather<false, 4>, (const void*)k_adjoint_gather<true, 4>})
+        CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, fs));
     return SF_OK;
 }
 
@@ -250,6 +254,40 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     A->hand_bytes = (size_t)NG * 4 * nstrips * c->batch_maxcols * 2 * sizeof(unsigned long long);
     A->ggrid = dim3((unsigned)(nstrips * ((c->nxx + kGT - 1) / kGT)));
     A->gblock = dim3(256);
+    // The gather inside the reverse-sweep launch (isotropic batches, 2 or 4
+    // warps per CTA) when the device holds every reverse-sweep CTA and at
+    // least one gather CTA at once.
+    A->fused = false;
+    if (c->fuse_gather && !c->batch_ani && (c->warps == 2 || c->warps == 4)) {
+        const bool in = c->batch_interior;
+        const void* fk = (c->warps == 2) ? (in ? (const void*)k_adjoint_gather<true, 2> : (const void*)k_adjoint_gather<false, 2>)
+                                         : (in ? (const void*)k_adjoint_gather<true, 4> : (const void*)k_adjoint_gather<false, 4>);
+        const size_t fsmem = std::max(smem, sizeof(GatherSmem));
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fk, c->warps * 32, fsmem));
+        const long long cap = (long long)per_sm * c->sms, nadj = (long long)NG * G;
+        const int nblk = (c->nxx + kGT - 1) / kGT, ntiles = nstrips * nblk;
+        const long long nga = std::min<long long>(cap - nadj, ntiles);
+        if (nga >= 1) {
+            const size_t nz = (size_t)ntiles + 1 + (size_t)ns;  // ready counters, tile counter, shot flags
+            rc = sf_dev_reserve(c, (void**)&c->d_fuse, &c->cap_fuse, nz * sizeof(unsigned));
+            if (rc) return rc;
+            A->fused = true;
+            A->fkern = fk;
+            A->fsmem = fsmem;
+            A->fgrid = dim3((unsigned)(nadj + nga));
+            A->fzero_bytes = nz * sizeof(unsigned);
+            A->f.nadj = (int)nadj;
+            A->f.nblk = nblk;
+            A->f.ready = c->d_fuse;
+            A->f.tile_ctr = c->d_fuse + ntiles;
+            A->f.shot_done = c->d_fuse + ntiles + 1;
+            A->f.done_tag = 1u;
+            g.shot_done = A->f.shot_done;
+            g.done_tag = 1u;
+            g.err = c->d_flags + 1;
+        }
+    }
     return SF_OK;
 }
 
@@ -259,6 +297,16 @@ int sf_adj_enqueue(sf_ctx* c, AdjLaunch& A, const float* d_pg, float* d_grad, un
     A.p.epoch = epoch;
     A.g.grad = d_grad;
     CK(cudaMemsetAsync(A.p.bar, 0, A.nctr * sizeof(unsigned), st));
+    c->last_fused = A.fused;
+    if (A.fused) {
+        // one launch: the gather's tiles start as the last reverse sweep finishes them
+        CK(cudaMemsetAsync(A.f.ready, 0, A.fzero_bytes, st));
+        int rc = sf_kt_begin(c, SF_KT_ADJOINT, st);
+        if (rc) return rc;
+        void* fargs[] = {&A.p, &A.g, &A.f};
+        CK(cudaLaunchKernel(A.fkern, A.fgrid, A.block, fargs, A.fsmem, st));
+        return sf_kt_end(c, SF_KT_ADJOINT, st);
+    }
     int rc = sf_kt_begin(c, SF_KT_ADJOINT, st);
     if (rc) return rc;
     void* args[] = {&A.p};
@@ -379,5 +427,21 @@ extern "C" int sf_batch_stiffness_gradient(sf_ctx* c, float* grad_c11, float* gr
     CK(cudaMemcpyAsync(grad_c11, c->d_gcij, npad * sizeof(float), kind, st));
     CK(cudaMemcpyAsync(grad_c13, c->d_gcij + npad, npad * sizeof(float), kind, st));
     if (mem == SF_MEM_HOST) return sf_check_flags(c, st);
+    return SF_OK;
+}
+
+extern "C" int sf_set_fused_gather(sf_ctx* c, int enable)
+{
+    if (!c) return SF_ERR_ARG;
+    c->fuse_gather = enable != 0;
+    c->plan_dirty = true;
+    return SF_OK;
+}
+
+extern "C" int sf_get_fused_gather(const sf_ctx* c, int* enable, int* last_fused)
+{
+    if (!c) return SF_ERR_ARG;
+    if (enable) *enable = c->fuse_gather ? 1 : 0;
+    if (last_fused) *last_fused = c->last_fused ? 1 : 0;
     return SF_OK;
 }

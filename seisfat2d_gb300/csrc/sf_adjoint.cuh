@@ -25,6 +25,7 @@
 
 namespace sf {
 
+constexpr int kGT = 32;    // gather tile columns (the column blocks of the gradient gather)
 constexpr int kLP = 36;    // lambda slot pitch: 32 rows, then the {pv,tag},{pev,tag} handoff pairs
 // The reverse sweeps stage 4 columns ahead (one block): their tape rows come
 // from DRAM, but a shorter lead keeps consecutive strips closer together,
@@ -55,6 +56,10 @@ struct AdjStripArgs {
     unsigned long long* h_out;       // pairs this strip feeds to the next one (nullptr: last strip)
     unsigned tag;
     int* err;
+    // last reverse sweep inside a fused launch: count each column block of
+    // kGT padded columns once all lanes have finished its columns
+    unsigned* ready;   // this strip's row of counters (nullptr: no counting)
+    int c0;            // the window's first padded column
 };
 
 // SZ, SX: signs of the forward sweep being reversed. INTERIOR: blocks whose
@@ -251,6 +256,23 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         tb0 += kU;
         if (tb0 >= kTR) tb0 -= kTR;
     };
+    // column blocks in the order the march finishes them: the counted sweep
+    // is the reverse of sweep 0 (SX > 0), which marches down the columns, so
+    // block b is done once lane 31 has passed its first window column (the
+    // tile's extra node column, the next block's first, came earlier)
+    const int blo = a.c0 / kGT, bhi = (a.c0 + ncols - 1) / kGT;
+    int next_b = bhi;
+    auto count_done = [&](int s_end) {
+        while (SX > 0 && next_b >= blo) {
+            const int wcol = max(next_b * kGT, a.c0) - a.c0;
+            const int m = ncols - 1 - wcol;  // march of that column
+            if (m + 31 > s_end) break;
+            __threadfence();  // this lane's terms before the count
+            __syncwarp();
+            if (lane == 0) atomicAdd(a.ready + next_b, 1u);
+            next_b--;
+        }
+    };
 #pragma unroll 1
     for (int s0 = 0; s0 < nsteps; s0 += kU) {
         if constexpr (INTERIOR) {
@@ -261,6 +283,7 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
         } else {
             block(s0, std::false_type{});
         }
+        if (a.ready) count_done(s0 + kU - 1);
     }
     cp_wait<0>();
     __syncwarp();
@@ -268,8 +291,11 @@ __device__ __forceinline__ void adj_strip(const AdjStripArgs& a)
 
 // (kMaxWarps * 32, 1): the block size alone as the bound caps the kernel at
 // 64 registers and spills the strip loop's state.
+// The reverse sweeps of every shot (persistent gangs, as the forward). f:
+// inside a fused launch, count finished column blocks in the last reverse
+// sweep and flag each shot's initialisation term.
 template <bool INTERIOR>
-__global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
+__device__ void adjoint_body(const AdjParams& p, const FuseParams* f)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
@@ -343,6 +369,8 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
                 a.tcode = p.tcode + tb;
                 a.tc1 = p.tc1 + tb;
                 a.tc2 = p.tc2 + tb;
+                a.ready = (f && sw == 0) ? f->ready + (size_t)a.k * f->nblk : nullptr;
+                a.c0 = sh.c0;
                 switch (sw) {
                 case 0: adj_strip<1, 1, INTERIOR>(a); break;
                 case 1: adj_strip<-1, 1, INTERIOR>(a); break;
@@ -357,8 +385,19 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
             const int zi = sh.sIdz + aa - 1, xl = sh.sIdx - sh.c0 + bb - 1;
             p.lam_init[(size_t)sh.orig * 9 + tid] = lam[(size_t)zi + (size_t)xl * nzz];
         }
+        if (f && gp.g == 0) {
+            __threadfence();
+            __syncthreads();
+            if (tid == 0) st_release_gpu(f->shot_done + sh.orig, f->done_tag);
+        }
         gang_barrier(bar, (++nbar) * p.G, cs, p.err);
     }
+}
+
+template <bool INTERIOR>
+__global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
+{
+    adjoint_body<INTERIOR>(p, nullptr);
 }
 
 // g(a, b) = sum over shots (caller order, FP64) of the shot's FP32 sum over
@@ -374,7 +413,6 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint(AdjParams p)
 // the threads sum their cells' terms in the order above. The shots covering
 // the tile's columns come from a per-column-block list built on the host,
 // staged in shared memory kGChunk at a time.
-constexpr int kGT = 32;             // tile columns
 constexpr int kGSteps = kGT + 32;   // tape steps a tile's strip spans per sweep
 constexpr int kGStages = 3;
 constexpr int kGChunk = 128;
@@ -391,24 +429,26 @@ struct GatherSmem {
     GatherShot shots[kGChunk];
 };
 
-// One stage's node terms for the thread's four cells when the tile lies inside
-// the shot's window and is not the last strip: the same terms and order as the
-// general loop of k_gather (cells q, corners (0,0),(0,1),(1,0),(1,1)), with the
-// 16 node slots one base plus offsets fixed by the sweep's directions.
-template <bool SZPOS, bool SXPOS>
-__device__ __forceinline__ void gather_interior(const GatherStage& S, float g[4], int a, int rb, int bl0, int ncols,
+// One stage's node terms for the thread's NQ = 32 / W cells (columns W
+// apart) when the tile lies inside the shot's window and is not the last
+// strip: the same terms and order as the general loop of gather_tile (cells q,
+// corners (0,0),(0,1),(1,0),(1,1)), with the node slots one base plus offsets
+// fixed by the sweep's directions.
+template <int W, bool SZPOS, bool SXPOS>
+__device__ __forceinline__ void gather_interior(const GatherStage& S, float* g, int a, int rb, int bl0, int ncols,
                                                 int fmlo, bool last_row)
 {
+    constexpr int NQ = 32 / W;
     const unsigned char* cbytes = reinterpret_cast<const unsigned char*>(S.code);
-    // node (ni, nj) = (a + 1 - dr, bl + 1 - dc) of cell (a, bl), bl = bl0 + 8q
+    // node (ni, nj) = (a + 1 - dr, bl + 1 - dc) of cell (a, bl), bl = bl0 + W q
     const int fl0 = SZPOS ? a + 1 - rb : rb + 31 - (a + 1);
     const int fm0 = SXPOS ? bl0 + 1 : ncols - 1 - (bl0 + 1);
     const int base = (fm0 + fl0 - fmlo) * 32 + fl0;
-    constexpr int DR = SZPOS ? -33 : 33;    // ni - 1: fl -/+ 1
-    constexpr int DC = SXPOS ? -32 : 32;    // nj - 1: fm -/+ 1
-    constexpr int DQ = SXPOS ? 256 : -256;  // nj + 8: fm +/- 8
+    constexpr int DR = SZPOS ? -33 : 33;            // ni - 1: fl -/+ 1
+    constexpr int DC = SXPOS ? -32 : 32;            // nj - 1: fm -/+ 1
+    constexpr int DQ = SXPOS ? 32 * W : -32 * W;    // nj + W: fm +/- W
 #pragma unroll
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < NQ; q++)
 #pragma unroll
         for (int dr = 0; dr < 2; dr++)
 #pragma unroll
@@ -416,7 +456,7 @@ __device__ __forceinline__ void gather_interior(const GatherStage& S, float g[4]
                 int cd;
                 float v;
                 if (dr == 0 && last_row) {  // node row a + 1: the next strip's first row
-                    const int q2 = (SXPOS ? bl0 + 8 * q + 1 - dc : ncols - 1 - (bl0 + 8 * q + 1 - dc)) - fmlo;
+                    const int q2 = (SXPOS ? bl0 + W * q + 1 - dc : ncols - 1 - (bl0 + W * q + 1 - dc)) - fmlo;
                     cd = (S.code2[q2] >> (SZPOS ? 0 : 24)) & 0xff;
                     v = S.v2[q2];
                 } else {
@@ -428,21 +468,48 @@ __device__ __forceinline__ void gather_interior(const GatherStage& S, float g[4]
             }
 }
 
+__device__ __forceinline__ void cp_async16_cg(void* smem, const void* gmem)
+{
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// Bounded wait of one thread until *p >= target (acquire); false after the
+// limit, with the error flag set.
+__device__ __forceinline__ bool wait_count(const unsigned* p, unsigned target, int* err)
+{
+    if (ld_acquire_gpu(p) >= target) return true;
+    const unsigned long long t0 = global_ns();
+    long long n = 0;
+    while (ld_acquire_gpu(p) < target) {
+        if (*(volatile int*)err) return false;
+        __nanosleep(256);
+        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > kSpinNs)) {
+            atomicExch(err, 2);
+            return false;
+        }
+    }
+    return true;
+}
+
+// g(a, b) of one tile (strip k, column block cb) by 32 W threads: thread
+// (warp w, lane l) owns cells (32 k + l, 32 cb + w + W q), q < 32 / W.
 // VTI: the batch was anisotropic; each shot's summed terms (its gradient with
 // respect to its own qP slowness) are multiplied by the shot's derivative
 // factors of the qP slowness before the FP64 sum over shots, giving dJ/dS,
-// dJ/dC11 and dJ/dC13.
-template <bool VTI>
-__global__ void __launch_bounds__(256) k_gather(GatherParams p)
+// dJ/dC11 and dJ/dC13. FUSED: the tile runs inside the reverse-sweep launch
+// while other shots may still be writing terms; it reads the tape through L2
+// only (cp.async.cg, ld.global.cg) and waits for a shot's flag before using
+// its initialisation term. Returns false when a wait gave up.
+template <int W, bool VTI, bool FUSED>
+__device__ bool gather_tile(const GatherParams& p, GatherSmem& sm, int k, int cb)
 {
-    extern __shared__ __align__(16) unsigned char gsm_raw[];
-    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(gsm_raw);
+    constexpr int NQ = 32 / W;
     const int tid = threadIdx.x;
-    const int ntx = (p.nxx + kGT - 1) / kGT;
-    const int k = blockIdx.x / ntx, cb = blockIdx.x % ntx, c = cb * kGT;
+    const int c = cb * kGT;
     const int rb = 32 * k;
     const bool next_strip = k + 1 < p.nstrips;
-    const int a = rb + (tid & 31);   // the thread's cells: row a, columns c + (tid>>5) + 8q
+    const int a = rb + (tid & 31);   // the thread's cells: row a, columns c + (tid>>5) + W q
     const int cq = tid >> 5;
 
     // node-column range of stage (shot entry e, sweep sw) in march order
@@ -459,7 +526,10 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
         const size_t base = tape_strip_base(t.tape_off, sw, k, p.nstrips, t.ncols);
         for (int q = tid; q < kGSteps * 8; q += blockDim.x) {
             const int st = fmlo + (q >> 3);
-            if (st < nst) cp_async16(&S.v[q * 4], p.vrec + base + (size_t)st * 32 + (q & 7) * 4);
+            if (st < nst) {
+                if (FUSED) cp_async16_cg(&S.v[q * 4], p.vrec + base + (size_t)st * 32 + (q & 7) * 4);
+                else cp_async16(&S.v[q * 4], p.vrec + base + (size_t)st * 32 + (q & 7) * 4);
+            }
         }
         for (int q = tid; q < kGSteps * 2; q += blockDim.x) {
             const int st = fmlo + (q >> 1);
@@ -470,18 +540,26 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
             const int fl2 = (sw == 1 || sw == 3) ? 31 : 0;
             for (int q = tid; q <= fmhi - fmlo; q += blockDim.x) {
                 const size_t e = base2 + (size_t)(fmlo + q + fl2) * 32 + fl2;
-                cp_async4(&S.v2[q], p.vrec + e);
+                if (FUSED) {
+                    S.v2[q] = __ldcg(p.vrec + e);
+                } else {
+                    cp_async4(&S.v2[q], p.vrec + e);
+                }
                 cp_async4(&S.code2[q], p.tcode + (e & ~(size_t)3));
             }
         }
         cp_commit();
     };
 
-    double total[4] = {0.0, 0.0, 0.0, 0.0};
-    double t11[VTI ? 4 : 1], t13[VTI ? 4 : 1];
-    if (VTI)
-        for (int q = 0; q < 4; q++) t11[q] = t13[q] = 0.0;
-    float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    double total[NQ], t11[VTI ? NQ : 1], t13[VTI ? NQ : 1];
+    float g[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        total[q] = 0.0;
+        g[q] = 0.0f;
+        if (VTI) t11[q] = t13[q] = 0.0;
+    }
+    bool ok = true;
     const int e_end = p.blk_ptr[cb + 1];
 #pragma unroll 1
     for (int e0 = p.blk_ptr[cb]; e0 < e_end; e0 += kGChunk) {
@@ -503,9 +581,14 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
             } else {
                 cp_wait<0>();
             }
-            __syncthreads();
             const GatherShot& t = sm.shots[i >> 2];
             const int sw = i & 3;
+            if (FUSED && sw == 3 && tid == 0) {
+                // the shot's initialisation term is written when its reverse sweeps end
+                const bool src = t.sIdz + 1 >= rb && t.sIdz - 1 < rb + 32 && t.sIdx + 1 >= c && t.sIdx - 1 < c + kGT;
+                if (src && !wait_count(p.shot_done + t.orig, p.done_tag, p.err)) ok = false;
+            }
+            __syncthreads();
             const bool szpos = !(sw == 1 || sw == 3), sxpos = sw < 2;
             int fmlo, fmhi;
             fm_range(t, sw, fmlo, fmhi);
@@ -517,15 +600,15 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
                 const int bl0 = c + cq - t.c0;
                 const bool last_row = a == rb + 31;
                 switch (sw) {
-                case 0: gather_interior<true, true>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
-                case 1: gather_interior<false, true>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
-                case 2: gather_interior<true, false>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
-                default: gather_interior<false, false>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                case 0: gather_interior<W, true, true>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                case 1: gather_interior<W, false, true>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                case 2: gather_interior<W, true, false>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
+                default: gather_interior<W, false, false>(S, g, a, rb, bl0, t.ncols, fmlo, last_row); break;
                 }
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int bc = c + cq + 8 * q;
+            for (int q = 0; q < NQ; q++) {
+                const int bc = c + cq + W * q;
                 const int bl = bc - t.c0;
                 if (a >= p.nzz || bc >= p.nxx || bl < 0 || bl >= t.ncols) continue;
                 if (!interior)
@@ -552,7 +635,9 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
                     const int da = a - t.sIdz + 1, db = bc - t.sIdx + 1;
                     if (da >= 0 && da < 3 && db >= 0 && db < 3) {
                         const double d = src_dist(a, bc, p.nb, p.dx, p.dz, t.sx, t.sz);
-                        g[q] = fadd(g[q], fmul(p.lam_init[(size_t)t.orig * 9 + da + 3 * db], __double2float_rn(d)));
+                        const float li = FUSED ? __ldcg(p.lam_init + (size_t)t.orig * 9 + da + 3 * db)
+                                               : p.lam_init[(size_t)t.orig * 9 + da + 3 * db];
+                        g[q] = fadd(g[q], fmul(li, __double2float_rn(d)));
                     }
                     if (VTI) {
                         const float* f = p.vfac + t.q_off + (size_t)a + (size_t)bl * p.nzz;
@@ -568,8 +653,9 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
             __syncthreads();  // stage i's buffer is refilled by stage i + kGStages
         }
     }
-    for (int q = 0; q < 4; q++) {
-        const int bc = c + cq + 8 * q;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        const int bc = c + cq + W * q;
         if (a < p.nzz && bc < p.nxx) {
             p.grad[(size_t)a + (size_t)bc * p.nzz] = __double2float_rn(total[q]);
             if (VTI) {
@@ -578,6 +664,17 @@ __global__ void __launch_bounds__(256) k_gather(GatherParams p)
             }
         }
     }
+    return ok;
+}
+
+// The gather as its own launch: one CTA of 8 warps per tile.
+template <bool VTI>
+__global__ void __launch_bounds__(256) k_gather(GatherParams p)
+{
+    extern __shared__ __align__(16) unsigned char gsm_raw[];
+    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(gsm_raw);
+    const int ntx = (p.nxx + kGT - 1) / kGT;
+    gather_tile<8, VTI, false>(p, sm, blockIdx.x / ntx, blockIdx.x % ntx);
 }
 
 // Residuals r = pick - t_obs (NaN picks or observations contribute nothing)
@@ -600,6 +697,49 @@ __global__ void k_residual(const float* picks, const float* tobs, size_t n, floa
         __syncthreads();
     }
     if (threadIdx.x == 0) *misfit = part[0];
+}
+
+}  // namespace sf
+
+namespace sf {
+
+// Reverse sweeps and gather in one launch of 32 W-thread CTAs (see
+// FuseParams). Every CTA of the launch is resident at once (the host sizes
+// the grid to the device), the reverse sweeps never wait on the gather, and
+// every gather wait is bounded.
+template <bool INTERIOR, int W>
+__global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint_gather(AdjParams p, GatherParams g, FuseParams f)
+{
+    if ((int)blockIdx.x < f.nadj) {
+        adjoint_body<INTERIOR>(p, &f);
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char fsm_raw[];
+    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(fsm_raw);
+    __shared__ int tile_s, ok_s;
+    const int ntiles = p.nstrips * f.nblk;
+#pragma unroll 1
+    while (true) {
+        if (threadIdx.x == 0) {
+            const int t = (int)atomicAdd(f.tile_ctr, 1u);
+            int ok = 1;
+            if (t < ntiles) {
+                // bottom strips first, columns right to left: the order the last
+                // reverse sweep finishes them
+                const int k = p.nstrips - 1 - t / f.nblk, cb = f.nblk - 1 - t % f.nblk;
+                const unsigned cover = (unsigned)(g.blk_ptr[cb + 1] - g.blk_ptr[cb]);
+                ok = wait_count(f.ready + (size_t)k * f.nblk + cb, cover, g.err);
+                if (ok && k + 1 < p.nstrips) ok = wait_count(f.ready + (size_t)(k + 1) * f.nblk + cb, cover, g.err);
+            }
+            tile_s = t;
+            ok_s = ok;
+        }
+        __syncthreads();
+        const int t = tile_s, ok = ok_s;
+        __syncthreads();
+        if (t >= ntiles || !ok) break;
+        if (!gather_tile<W, false, true>(g, sm, p.nstrips - 1 - t / f.nblk, f.nblk - 1 - t % f.nblk)) break;
+    }
 }
 
 }  // namespace sf

@@ -64,6 +64,25 @@ struct GatherParams {
     long long vfac_total;
     float* grad_c11;         // nzz x nxx
     float* grad_c13;         // nzz x nxx
+    // gather inside the reverse-sweep launch: a shot's initialisation term is
+    // final when shot_done[orig] == done_tag; waits give up with *err set
+    const unsigned* shot_done;
+    unsigned done_tag;
+    int* err;
+};
+
+// The reverse sweeps and the gather in one launch: CTAs [0, nadj) run the
+// reverse sweeps and count, per (strip, column block), the shots whose last
+// reverse sweep has finished the block (ready); the other CTAs take tiles in
+// that order (tile_ctr) and start a tile when every shot covering it has
+// finished it in the tile's strip and the next one.
+struct FuseParams {
+    int nadj;            // reverse-sweep CTAs
+    int nblk;            // column blocks of kGT columns
+    unsigned* ready;     // nstrips x nblk counters (zeroed per launch)
+    unsigned* tile_ctr;  // next tile (zeroed per launch)
+    unsigned* shot_done; // per shot: done_tag once its initialisation term is written
+    unsigned done_tag;
 };
 
 }  // namespace sf

@@ -194,7 +194,7 @@ extern "C" int sf_ctx_destroy(sf_ctx* c)
     void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
                     c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand, c->d_ctr,
                     c->d_skern, c->d_upd, c->d_wav, c->d_mig, c->d_kgeo, c->d_kint, c->d_kpart,
-                    c->d_vfac, c->d_gcij};
+                    c->d_vfac, c->d_gcij, c->d_fuse};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete c;

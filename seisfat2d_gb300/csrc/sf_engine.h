@@ -30,6 +30,13 @@ struct AdjLaunch {
     size_t smem = 0;
     size_t nctr = 0;
     size_t hand_bytes = 0;
+    // reverse sweeps and gather in one launch (k_adjoint_gather)
+    bool fused = false;
+    const void* fkern = nullptr;
+    sf::FuseParams f{};
+    dim3 fgrid;
+    size_t fsmem = 0;
+    size_t fzero_bytes = 0;  // counters zeroed before each launch (f.ready ...)
 };
 
 // Kernels timed by sf_kernel_times (events around each launch when enabled).
@@ -44,6 +51,9 @@ struct sf_ctx {
     int warps = 1;        // warps per CTA
     int gang_warps = 0;   // warps solving one shot (0: chosen per batch)
     int strip_loop = -1;  // strip loops: SF_LOOP_* (sf_set_strip_loop)
+    bool fuse_gather = true;  // gather inside the reverse-sweep launch when it fits (sf_set_fused_gather)
+    bool last_fused = false;  // the last adjoint ran fused
+    unsigned* d_fuse = nullptr; size_t cap_fuse = 0;
     bool batch_interior = false;  // the last batch's forward ran the interior-block body
     int arith = SF_ARITH_REFERENCE;
     std::string err;

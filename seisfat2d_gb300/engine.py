@@ -401,6 +401,15 @@ class Engine:
         m = {"auto": -1, "general": 0, "interior": 1}[mode]
         self._check(self.L.sf_set_strip_loop(self._ctx, m), "sf_set_strip_loop")
 
+    def set_fused_gather(self, enable):
+        self._check(self.L.sf_set_fused_gather(self._ctx, 1 if enable else 0), "sf_set_fused_gather")
+
+    def fused_gather(self):
+        """(enabled, whether the last adjoint ran the gather inside its launch)."""
+        e, last = C.c_int(), C.c_int()
+        self._check(self.L.sf_get_fused_gather(self._ctx, C.byref(e), C.byref(last)), "sf_get_fused_gather")
+        return bool(e.value), bool(last.value)
+
     def strip_loop(self):
         """(mode, whether the last batch ran the interior-block form)."""
         m, last = C.c_int(), C.c_int()

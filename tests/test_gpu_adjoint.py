@@ -161,3 +161,35 @@ def test_strip_loop_forms_same_bits_windows(engine_lib, cuda, arith):
     for ta, tb in zip(a[1], b[1]):
         assert np.array_equal(ta, tb)
     assert a[3] == b[3] and np.array_equal(a[4], b[4]) and np.abs(a[4]).max() > 0
+
+
+@pytest.mark.parametrize("warps", [2, 4])
+def test_fused_gather_same_bits(engine_lib, cuda, warps):
+    """The gather inside the reverse-sweep launch (tiles started as the last
+    reverse sweep finishes them) gives the separate gather's bits, eagerly
+    and from a replayed CUDA graph of the planned iteration."""
+    e, m = setup(nx=150, nz=90, seed=21)
+    e.set_launch(warps, 0)
+    rx, rz = surface_receivers(e.nx, 10.0, step=3)
+    shots = [(150.0, 0.0), (700.0, 40.0, 20, 100), (1200.0, 10.0), (400.0, 300.0, 0, 80), (1000.0, 0.0, 60, 96)]
+    res = {}
+    for fused in (False, True):
+        e.set_fused_gather(fused)
+        pk = e.batch_forward(shots, rx, rz, keep_tape=True)
+        J, g = e.misfit_gradient(np.nan_to_num(pk) + np.float32(0.01))
+        assert e.fused_gather() == (fused, fused)
+        res[fused] = (pk, J, g)
+    assert res[False][1] == res[True][1] and np.array_equal(res[False][2], res[True][2])
+    assert np.abs(res[True][2]).max() > 0
+    # planned iteration replayed from a graph, fused
+    dev = cuda.device("cuda", 0)
+    tobs = cuda.from_numpy(np.nan_to_num(res[True][0]) + np.float32(0.01)).to(dev)
+    picks = cuda.empty(tobs.shape, dtype=cuda.float32, device=dev)
+    grad = cuda.empty((e.nxx, e.nzz), dtype=cuda.float32, device=dev)
+    e.set_fused_gather(True)
+    e.plan_batch(shots, rx, rz)
+    for _ in range(3):
+        e.plan_graph_launch(picks, t_obs=tobs, grad=grad)
+        e.synchronize()
+        assert e.fused_gather() == (True, True)
+        assert np.array_equal(grad.cpu().numpy(), res[False][2])
