@@ -31,7 +31,7 @@ constexpr int kLP = 36;    // lambda slot pitch: 32 rows, then the {pv,tag},{pev
 // from DRAM, but a shorter lead keeps consecutive strips closer together,
 // which measured faster than 8 or 12.
 constexpr int kLookA = 4;
-constexpr int kAheadA = kLookA + 2 * kU;  // a consumer's fall-back distance after a stall
+constexpr int kAheadA = kLookA + kU;  // a consumer's fall-back distance after a stall
 constexpr int kTR = 12;    // tape ring slots (a multiple of kU, > kLookA + kU)
 constexpr int kTPitch = 72;  // c1[32], c2[32], code bytes (8 words)
 // the prefetch slots b0 + kLookA + u and tb0 + kLookA + u are wrapped once:
