@@ -490,7 +490,8 @@ def run_ours(a):
                    "launch": {"warps_per_cta": launch_used[0], "warps_per_shot": launch_used[1] or "auto",
                               "strip_loop": {"mode": loop_used[0],
                                              "form": "interior-block" if loop_used[1] else "general"},
-                              "gather": "inside the reverse-sweep launch" if fused_used else "own launch",
+                              **({"gather": "inside the reverse-sweep launch" if fused_used else "own launch"}
+                                 if fa else {}),
                               "chosen_by": "sf_plan_autotune" if tuned else (
                                   "flags" if (a.warps or a.gang or a.strip_loop != "auto") else "default")},
                    "timed_path": ("sf_plan_graph_launch (CUDA graph of the planned iteration)" if fa
