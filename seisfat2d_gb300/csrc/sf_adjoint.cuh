@@ -15,10 +15,15 @@
 // march reversed, so the same strip-systolic schedule runs it: lane l owns a
 // row, the lane above supplies the sum of its pv of the previous step and its
 // pev of the step before by one shfl (the two pushes of the upwind row are
-// summed by their sender), the lane's own previous pe is kept in a register. The tape was written in the forward
-// strip's skewed step order, which makes the reverse read of one step 32
-// consecutive entries (lane l of the reverse march is lane 31-l of the
-// forward one).
+// summed by their sender), the lane's own previous pe is kept in a register.
+// The tape was written in the forward strip's skewed step order, which makes
+// the reverse read of one step 32 consecutive entries (lane l of the reverse
+// march is lane 31-l of the forward one).
+//
+// The node terms v overwrite the tape's c2; the gradient gather (gather_tile)
+// sums them per slowness cell, either in its own launch (k_gather) or inside
+// the reverse-sweep launch (k_adjoint_gather), where each tile starts as soon
+// as the last reverse sweep of every shot has finished it.
 #pragma once
 #include "sf_adjoint_params.cuh"
 #include "sf_forward.cuh"

@@ -25,7 +25,7 @@ struct AdjLaunch {
     sf::AdjParams p{};
     sf::GatherParams g{};
     const void* kern = nullptr;   // k_adjoint
-    const void* gkern = nullptr;  // k_gather
+    const void* gkern = nullptr;  // k_gather (when not fused)
     dim3 grid, block, ggrid, gblock;
     size_t smem = 0;
     size_t nctr = 0;
