@@ -183,7 +183,8 @@ int sf_get_launch(const sf_ctx* ctx, int* warps, int* gang_warps);
  * form runs fewer instructions per step but is larger code, which measured
  * faster for a batch whose shots all run at once with one window width and
  * one warp per strip, slower for uneven windows or several strips per warp.
- * SF_LOOP_AUTO (default) chooses per batch;
+ * SF_LOOP_AUTO (default) chooses per batch (taped batches with more than 8
+ * warps per CTA always run the general form);
  * sf_plan_autotune times both. last_interior: whether the last batch's
  * forward used the interior-block form (the reverse sweeps follow it). */
 int sf_set_strip_loop(sf_ctx* ctx, int mode);

@@ -598,8 +598,23 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
     if (rc) return rc;
-    c->batch_interior = !vti && sf_interior_loops(c, kern, smem, G);
-    if (c->batch_interior) kern = sf_kshots_kernel(tape, ref, vti, true);
+    // the interior-block kernels of taped batches are built for at most
+    // kMaxWarpsTapedInterior warps per CTA; the gang shape must come from the
+    // kernel that runs (every CTA of a gang resident at once)
+    c->batch_interior = !vti && !(tape && c->warps > kMaxWarpsTapedInterior) && sf_interior_loops(c, kern, smem, G);
+    if (c->batch_interior) {
+        const void* ik = sf_kshots_kernel(tape, ref, vti, true);
+        int Gi, NGi;
+        rc = sf_gang_shape(c, ik, smem, nshots, nstrips, gang_warps, &Gi, &NGi);
+        if (rc) return rc;
+        if (c->strip_loop == SF_LOOP_INTERIOR || sf_interior_loops(c, ik, smem, Gi)) {
+            kern = ik;
+            G = Gi;
+            NG = NGi;
+        } else {
+            c->batch_interior = false;
+        }
+    }
     if ((long long)(nshots + NG - 1) / NG * (ani ? 2 : 1) > 1023)
         return sf_fail(c, SF_ERR_ARG, "too many shots per gang for one launch; split the batch");
     c->last_G = G;

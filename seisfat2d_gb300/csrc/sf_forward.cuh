@@ -164,7 +164,7 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
 template <bool TAPE, bool REF, bool VTI, bool INTERIOR>
 // (kMaxWarps * 32, 1): with the block size alone as the bound ptxas caps the
 // kernel at 64 registers and spills the strip loop's state to local memory.
-__global__ void __launch_bounds__(kMaxWarps * 32, 1) k_shots(FwdParams p)
+__global__ void __launch_bounds__(((TAPE && INTERIOR) ? kMaxWarpsTapedInterior : kMaxWarps) * 32, 1) k_shots(FwdParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);

@@ -55,6 +55,10 @@ struct FwdBlock {
 constexpr int kSP = 36;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff pair at 34..35
 constexpr int kTP = 32;     // T slot pitch
 constexpr int kMaxWarps = 16;
+// the taped interior-block forward kernels bound their CTAs to 8 warps, which
+// lets them keep more of the block's state in registers (measured 2.6%
+// faster on the headline batch; the other kernels measured slower that way)
+constexpr int kMaxWarpsTapedInterior = 8;
 constexpr long long kSpinLimit = 1ll << 30;          // iterations
 constexpr unsigned long long kSpinNs = 2000000000ull;  // and at most ~2 s
 
