@@ -73,7 +73,10 @@ struct Rec {
 // columns max(j-1,1) and j); s2a/s2b: cells of the horizontal edge (rows
 // max(i-1,1) and i, column j1); sref = S[i1][j1]. dr1/dc2 locate i1/j1 in the
 // 2x2 block around the node, dc1a/dr2a locate the clamped first cells.
-template <bool TAPE, bool REF, bool EXACT = false>
+// SQ: square cells (dx and dz equal as floats). Then the two edge
+// thresholds are one quotient and the step constants need no per-node
+// selection; every value is the one the general form computes.
+template <bool TAPE, bool REF, bool EXACT = false, bool SQ = false>
 __device__ __forceinline__ float node_update(float told, float tv, float te, float tev, float s1a,
                                              float s1b, float s2a, float s2b, float sref,
                                              const Consts& k, int dr1, int dc1a, int dc2, int dr2a,
@@ -93,17 +96,18 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
     // reference's branches would take (same operations, same bits); the
     // operations of the other candidate get operands that keep them on their
     // fast paths.
-    const bool c2d = (tv <= fadd(te, fmul(k.dx, sref))) && (te <= fadd(tv, fmul(k.dz, sref))) &&
-                     (dte >= 0.0f) && (dtv >= 0.0f);
+    const float dxs = fmul(k.dx, sref);
+    const float dzs = SQ ? dxs : fmul(k.dz, sref);
+    const bool c2d = (tv <= fadd(te, dxs)) && (te <= fadd(tv, dzs)) && (dte >= 0.0f) && (dtv >= 0.0f);
     const float thz = fdiv_k<EXACT>(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4, bad);
-    const float thx = fdiv_k<EXACT>(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4, bad);
+    const float thx = SQ ? thz : fdiv_k<EXACT>(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4, bad);
     const bool c2 = !c2d && (dte <= thz) && (dte > 0.0f);        // t2: from te, step dz
     const bool c3 = !c2d && !c2 && (dtv <= thx) && (dtv > 0.0f);  // t3: from tv, step dx
     const bool ce = c2 || c3;
-    const float hq = c2 ? k.dz : k.dx;  // step the difference is divided by
-    const float rq = c2 ? k.rdz : k.rdx;
-    const bool vq = c2 ? (k.mflags & 2) : (k.mflags & 1);
-    const float hx = c2 ? k.dx : k.dz;  // step that multiplies the root
+    const float hq = SQ ? k.dz : (c2 ? k.dz : k.dx);  // step the difference is divided by
+    const float rq = SQ ? k.rdz : (c2 ? k.rdz : k.rdx);
+    const bool vq = SQ ? (k.mflags & 2) : (c2 ? (k.mflags & 2) : (k.mflags & 1));
+    const float hx = SQ ? k.dz : (c2 ? k.dx : k.dz);  // step that multiplies the root
     const float bs = c2 ? te : tv;
     const float qe = fdiv_k<EXACT>(ce ? (c2 ? dte : dtv) : hq, hq, rq, vq, bad);
     const float ta = fsub(fadd(tev, te), tv);
@@ -156,8 +160,8 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
                         rec.c1 = fdiv_k<EXACT>(k.kA, k.D, k.rD, k.mflags & 8, bad);
                     }
                 } else {
-                    float hx = (br == 4) ? k.dx : k.dz;
-                    float hq = (br == 4) ? k.dz : k.dx;
+                    float hx = SQ ? k.dz : ((br == 4) ? k.dx : k.dz);
+                    float hq = SQ ? k.dz : ((br == 4) ? k.dz : k.dx);
                     if (qq > 0.0f) {
                         rec.c1 = fdiv(fmul(hx, q), fmul(hq, qq));
                         rec.c2 = fdiv(fmul(hx, sref), qq);

@@ -101,7 +101,8 @@ __device__ __forceinline__ GangPos gang_pos(int G)
 // The four sweeps of one solve of the current shot; every warp of the gang
 // runs the strips of its slot. No barrier between sweeps: consecutive sweeps
 // run the rows in opposite directions, a warp rereads only rows it wrote
-// itself, and the handoff chain orders everything else.
+// itself, and the handoff chain orders everything else. Square cells (dx and
+// dz equal) run the strip loops' square-cell form.
 template <bool TAPE, bool REF, bool INTERIOR>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPos& gp, const float* Sw,
                              int ldS, float* T, unsigned tag, CtaShared* cs, WarpRing* rings)
@@ -145,11 +146,20 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
                 a.tc1 = p.tc1 + base;
                 a.tc2 = p.tc2 + base;
             }
-            switch (sw) {
-            case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR>(a); break;
-            case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR>(a); break;
-            case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR>(a); break;
-            default: run_strip<-1, -1, false, TAPE, REF, INTERIOR>(a); break;
+            if (p.kc.dx == p.kc.dz) {
+                switch (sw) {
+                case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR, true>(a); break;
+                case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR, true>(a); break;
+                case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR, true>(a); break;
+                default: run_strip<-1, -1, false, TAPE, REF, INTERIOR, true>(a); break;
+                }
+            } else {
+                switch (sw) {
+                case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR, false>(a); break;
+                case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR, false>(a); break;
+                case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR, false>(a); break;
+                default: run_strip<-1, -1, false, TAPE, REF, INTERIOR, false>(a); break;
+                }
             }
         }
     }

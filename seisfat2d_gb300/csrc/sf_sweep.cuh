@@ -199,8 +199,9 @@ __device__ __forceinline__ unsigned wait_counter(const unsigned* p, unsigned tar
 
 // INTERIOR: blocks whose marches all lie inside the window run a body without
 // bounds tests (fewer instructions per step, more code); otherwise every block
-// runs the general body. Both give the same bits.
-template <int SZ, int SX, bool SW0, bool TAPE, bool REF, bool INTERIOR>
+// runs the general body. SQ: square cells (node_update). All forms give the
+// same bits.
+template <int SZ, int SX, bool SW0, bool TAPE, bool REF, bool INTERIOR, bool SQ>
 __device__ __forceinline__ void run_strip(const StripArgs& a)
 {
     constexpr int kU = FwdBlock<TAPE>::U, kLook = FwdBlock<TAPE>::LOOK, kAhead = FwdBlock<TAPE>::AHEAD;
@@ -230,6 +231,8 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
     CtaShared* sh = a.sh;
     const bool consumer = (lane == 0) && (a.h_in != nullptr);
+    // the strip holds rows of the source's 3x3 block (first sweep only)
+    const bool src_rows = SW0 && (a.sIdz + 1 >= rb) && (a.sIdz - 1 <= rb + 31);
     auto col_of = [&](int m) { return (SX > 0) ? m : ncols - 1 - m; };
     // running source addresses of march column q (q advances by one per call)
     const long long dcol = (SX > 0) ? 1 : -1;
@@ -337,7 +340,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             const float te = tn, tev = tvp;
 
             float to = told[u];
-            if (SW0) {
+            if (SW0 && src_rows) {
                 const int da = r - a.sIdz + 1, db = j - a.sIdx + 1;
                 if (da >= 0 && da < 3 && db >= 0 && db < 3) to = a.init[da + 3 * db];
             }
@@ -361,8 +364,8 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             const int dc1a = (j - 1 >= 1) ? 0 : 1;
             bool bad_u = false;
             if (inner)
-                tnew = node_update<TAPE, REF, EXACT>(to, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc, dr1,
-                                                     dc1a, dc2, dr2a, rec[u], bad_u);
+                tnew = node_update<TAPE, REF, EXACT, SQ>(to, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc,
+                                                         dr1, dc1a, dc2, dr2a, rec[u], bad_u);
             bad |= bad_u;
             tnw[u] = tnew;
             actv[u] = act;
