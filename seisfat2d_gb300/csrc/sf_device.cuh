@@ -273,10 +273,17 @@ __device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, fl
     }
     float coeff1 = fadd(Gxx, Gzz);
     float coeff2 = fsub(Gxx, Gzz);
-    float det = fsqrt(fadd(fdiv(fmul(coeff2, coeff2), 4.0f), fmul(Gxz, Gxz)));
-    // coeff1 / 2.0 is a double expression in the reference
-    float g0 = __double2float_rn(__dadd_rn(__ddiv_rn((double)coeff1, 2.0), (double)det));
-    float g1 = __double2float_rn(__dsub_rn(__ddiv_rn((double)coeff1, 2.0), (double)det));
+    // x / 4 and x * 0.25 have the same exact value, hence the same rounding
+    float det = fsqrt(fadd(fmul(fmul(coeff2, coeff2), 0.25f), fmul(Gxz, Gxz)));
+    // The reference evaluates coeff1 / 2.0 +- det in double and rounds to
+    // float. The halving is exact, and rounding a sum of two 24-bit values
+    // first to binary64 and then to binary32 gives the binary32 rounding of
+    // the exact sum (double rounding is innocuous for addition when the
+    // wider format has at least 2p + 1 bits, 53 >= 49; S. A. Figueroa, "When
+    // is double rounding innocuous?", ACM SIGNUM Newsletter 30(3), 1995). So
+    // one FP32 FMA gives the same bits, without the GPU's slow FP64 pipe.
+    float g0 = __fmaf_rn(coeff1, 0.5f, det);
+    float g1 = __fmaf_rn(coeff1, 0.5f, -det);
     if (g0 < g1) g0 = g1;
     return fdiv(1.0f, fsqrt(fmul(g0, Ro)));
 }
