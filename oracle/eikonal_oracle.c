@@ -602,39 +602,39 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
  * |grad T| of the first solve held fixed: Sq = S sqrt(c33 / lambda), lambda the
  * larger eigenvalue of the Christoffel matrix along p, v its unit eigenvector;
  * dSq/dS = sqrt(c33/lambda), dSq/dC11 = -Sq px^2 vx^2 / (2 lambda),
- * dSq/dC13 = -Sq px pz vx vz / lambda. FP64, each operation rounded once, in
- * this order; (1, 0, 0) for a zero gradient or a non-positive eigenvalue. */
-static void qp_factors_f64(float tzp, float tzm, float txp, float txm, float s, float dx, float dz, float c11f,
-                           float c13f, float c15f, float c33f, float c35f, float c55f, float* fS, float* f11,
+ * dSq/dC13 = -Sq px pz vx vz / lambda. FP32, each operation rounded once, in
+ * this order (the engine's qp_factors in sf_device.cuh); (1, 0, 0) for a zero
+ * gradient or a non-positive eigenvalue. */
+static void qp_factors_f32(float tzp, float tzm, float txp, float txm, float s, float dx, float dz, float c11,
+                           float c13, float c15, float c33, float c35, float c55, float* fS, float* f11,
                            float* f13)
 {
-    const double c11 = c11f, c13 = c13f, c15 = c15f, c33 = c33f, c35 = c35f, c55 = c55f;
-    double dTz = 0.5 * ((double)tzp - (double)tzm) / (double)dz;
-    double dTx = 0.5 * ((double)txp - (double)txm) / (double)dx;
-    double nrm = sqrt(dTx * dTx + dTz * dTz);
+    float dTz = (0.5f * (tzp - tzm)) / dz;
+    float dTx = (0.5f * (txp - txm)) / dx;
+    float nrm = sqrtf(dTx * dTx + dTz * dTz);
     *fS = 1.0f;
     *f11 = 0.0f;
     *f13 = 0.0f;
-    if (!(nrm > 0.0)) return;
-    double px = dTx / nrm, pz = dTz / nrm;
-    double Gxx = c11 * px * px + c55 * pz * pz + 2.0 * c15 * px * pz;
-    double Gzz = c55 * px * px + c33 * pz * pz + 2.0 * c35 * px * pz;
-    double Gxz = c15 * px * px + c35 * pz * pz + (c13 + c55) * px * pz;
-    double h = 0.5 * (Gxx - Gzz);
-    double r = sqrt(h * h + Gxz * Gxz);
-    double lam = 0.5 * (Gxx + Gzz) + r;
-    if (!(lam > 0.0)) return;
-    double vx, vz;
-    if (h >= 0.0) { vx = h + r; vz = Gxz; }
-    else          { vx = Gxz; vz = r - h; }
-    double nv = sqrt(vx * vx + vz * vz);
-    if (nv > 0.0) { vx = vx / nv; vz = vz / nv; }
-    else          { vx = px; vz = pz; }
-    double fs = sqrt(c33 / lam);
-    double sq = (double)s * fs;
-    *fS = (float)fs;
-    *f11 = (float)((-0.5 * sq * (px * px) * (vx * vx)) / lam);
-    *f13 = (float)((-sq * (px * pz) * (vx * vz)) / lam);
+    if (!(nrm > 0.0f)) return;
+    float px = dTx / nrm, pz = dTz / nrm;
+    float Gxx = c11 * px * px + c55 * pz * pz + 2.0f * c15 * px * pz;
+    float Gzz = c55 * px * px + c33 * pz * pz + 2.0f * c35 * px * pz;
+    float Gxz = c15 * px * px + c35 * pz * pz + (c13 + c55) * px * pz;
+    float h = 0.5f * (Gxx - Gzz);
+    float r = sqrtf(h * h + Gxz * Gxz);
+    float lam = 0.5f * (Gxx + Gzz) + r;
+    if (!(lam > 0.0f)) return;
+    float vx, vz;
+    if (h >= 0.0f) { vx = h + r; vz = Gxz; }
+    else           { vx = Gxz; vz = r - h; }
+    float nv = sqrtf(vx * vx + vz * vz);
+    if (nv > 0.0f) { vx = vx / nv; vz = vz / nv; }
+    else           { vx = px; vz = pz; }
+    float fs = sqrtf(c33 / lam);
+    float sq = s * fs;
+    *fS = fs;
+    *f11 = (-0.5f * sq * (px * px) * (vx * vx)) / lam;
+    *f13 = (-sq * (px * pz) * (vx * vz)) / lam;
 }
 
 /* The factors over a window, as the qP pass runs (interior nodes except the
@@ -652,7 +652,7 @@ void orc_qp_factors(int nzz, int ncols, int nb, const float* T, const float* Sin
             f13[it] = 0.0f;
             if (!((i >= nb) && (i < nzz - nb) && (j >= nb) && (j < ncols - nb))) continue;
             if ((i == sIdz) && (j == sIdx_loc)) continue;
-            qp_factors_f64(T[it + 1], T[it - 1], T[it + nzz], T[it - nzz], Sin[is], dx, dz,
+            qp_factors_f32(T[it + 1], T[it - 1], T[it + nzz], T[it - nzz], Sin[is], dx, dz,
                            decode_c(codes[0][is], mm[0], mm[1]), decode_c(codes[1][is], mm[2], mm[3]),
                            decode_c(codes[2][is], mm[4], mm[5]), decode_c(codes[3][is], mm[6], mm[7]),
                            decode_c(codes[4][is], mm[8], mm[9]), decode_c(codes[5][is], mm[10], mm[11]),

@@ -296,43 +296,39 @@ __device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, fl
 //   dSq/dS   = sqrt(c33 / lambda)
 //   dSq/dC11 = -Sq / (2 lambda) * px^2 vx^2          (dGamma_xx/dC11 = px^2)
 //   dSq/dC13 = -Sq / lambda * px pz vx vz            (dGamma_xz/dC13 = px pz)
-// In FP64 with each operation rounded once (no contraction), then rounded to
-// FP32, so a C restatement gives the same bits. A zero gradient or a
-// non-positive eigenvalue gives (1, 0, 0).
+// In FP32 with each operation rounded once (no contraction), so a C
+// restatement gives the same bits; FP32 keeps the pass off the GPU's slow
+// FP64 pipe. A zero gradient or a non-positive eigenvalue gives (1, 0, 0).
 __device__ __forceinline__ void qp_factors(float tzp, float tzm, float txp, float txm, float s, float dx,
                                            float dz, float c11, float c13, float c15, float c33, float c35,
                                            float c55, float& fS, float& f11, float& f13)
 {
-    auto A = [](double a, double b) { return __dadd_rn(a, b); };
-    auto Sb = [](double a, double b) { return __dsub_rn(a, b); };
-    auto M = [](double a, double b) { return __dmul_rn(a, b); };
-    auto D = [](double a, double b) { return __ddiv_rn(a, b); };
-    const double dTz = D(M(0.5, Sb(tzp, tzm)), dz);
-    const double dTx = D(M(0.5, Sb(txp, txm)), dx);
-    const double nrm = __dsqrt_rn(A(M(dTx, dTx), M(dTz, dTz)));
+    const float dTz = fdiv(fmul(0.5f, fsub(tzp, tzm)), dz);
+    const float dTx = fdiv(fmul(0.5f, fsub(txp, txm)), dx);
+    const float nrm = fsqrt(fadd(fmul(dTx, dTx), fmul(dTz, dTz)));
     fS = 1.0f;
     f11 = 0.0f;
     f13 = 0.0f;
-    if (!(nrm > 0.0)) return;
-    const double px = D(dTx, nrm), pz = D(dTz, nrm);
-    const double Gxx = A(A(M(M(c11, px), px), M(M(c55, pz), pz)), M(M(M(2.0, c15), px), pz));
-    const double Gzz = A(A(M(M(c55, px), px), M(M(c33, pz), pz)), M(M(M(2.0, c35), px), pz));
-    const double Gxz = A(A(M(M(c15, px), px), M(M(c35, pz), pz)), M(M(A(c13, c55), px), pz));
-    const double h = M(0.5, Sb(Gxx, Gzz));
-    const double r = __dsqrt_rn(A(M(h, h), M(Gxz, Gxz)));
-    const double lam = A(M(0.5, A(Gxx, Gzz)), r);
-    if (!(lam > 0.0)) return;
-    double vx, vz;
-    if (h >= 0.0) { vx = A(h, r); vz = Gxz; }
-    else          { vx = Gxz; vz = Sb(r, h); }
-    const double nv = __dsqrt_rn(A(M(vx, vx), M(vz, vz)));
-    if (nv > 0.0) { vx = D(vx, nv); vz = D(vz, nv); }
-    else          { vx = px; vz = pz; }
-    const double fs = __dsqrt_rn(D((double)c33, lam));
-    const double sq = M(s, fs);
-    fS = __double2float_rn(fs);
-    f11 = __double2float_rn(D(M(M(M(-0.5, sq), M(px, px)), M(vx, vx)), lam));
-    f13 = __double2float_rn(D(M(M(-sq, M(px, pz)), M(vx, vz)), lam));
+    if (!(nrm > 0.0f)) return;
+    const float px = fdiv(dTx, nrm), pz = fdiv(dTz, nrm);
+    const float Gxx = fadd(fadd(fmul(fmul(c11, px), px), fmul(fmul(c55, pz), pz)), fmul(fmul(fmul(2.0f, c15), px), pz));
+    const float Gzz = fadd(fadd(fmul(fmul(c55, px), px), fmul(fmul(c33, pz), pz)), fmul(fmul(fmul(2.0f, c35), px), pz));
+    const float Gxz = fadd(fadd(fmul(fmul(c15, px), px), fmul(fmul(c35, pz), pz)), fmul(fmul(fadd(c13, c55), px), pz));
+    const float h = fmul(0.5f, fsub(Gxx, Gzz));
+    const float r = fsqrt(fadd(fmul(h, h), fmul(Gxz, Gxz)));
+    const float lam = fadd(fmul(0.5f, fadd(Gxx, Gzz)), r);
+    if (!(lam > 0.0f)) return;
+    float vx, vz;
+    if (h >= 0.0f) { vx = fadd(h, r); vz = Gxz; }
+    else           { vx = Gxz; vz = fsub(r, h); }
+    const float nv = fsqrt(fadd(fmul(vx, vx), fmul(vz, vz)));
+    if (nv > 0.0f) { vx = fdiv(vx, nv); vz = fdiv(vz, nv); }
+    else           { vx = px; vz = pz; }
+    const float fs = fsqrt(fdiv(c33, lam));
+    const float sq = fmul(s, fs);
+    fS = fs;
+    f11 = fdiv(fmul(fmul(fmul(-0.5f, sq), fmul(px, px)), fmul(vx, vx)), lam);
+    f13 = fdiv(fmul(fmul(-sq, fmul(px, pz)), fmul(vx, vz)), lam);
 }
 
 }  // namespace sf

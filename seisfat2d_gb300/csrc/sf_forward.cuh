@@ -199,7 +199,8 @@ __global__ void __launch_bounds__(((TAPE && INTERIOR) ? kMaxWarpsTapedInterior :
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
         solve_window<TAPE && !VTI, REF, INTERIOR>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
-        if (p.ani) {
+        // taped isotropic batches never set ani: their kernels carry no qP pass
+        if ((!TAPE || VTI) && p.ani) {
             // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
             // warp's strips, once the whole first solve is done
             gang_barrier(bar, (++nbar) * p.G, cs, p.err);

@@ -2,7 +2,7 @@
 and SF_KEEP_TAPE tapes the second (qP) solve; sf_batch_misfit_gradient gives
 dJ/dS and sf_batch_stiffness_gradient dJ/dC11, dJ/dC13. All three equal the
 oracle's FP32 restatement bit for bit (same tapes, the qP derivative factors
-in FP64 rounded once, shot sums in FP64 in caller order); the oracle's
+in FP32, each operation rounded once, shot sums in FP64 in caller order); the oracle's
 stiffness gradients match central differences of the misfit
 (tests/test_oracle.py)."""
 import numpy as np
