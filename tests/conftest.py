@@ -34,3 +34,12 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return torch
+
+
+@pytest.fixture(scope="session")
+def exes(engine_lib):
+    """The C++ drivers (seisfat2d_gb300/host), built against the engine library."""
+    from seisfat2d_gb300.host import build as hb
+    out = hb.build()
+    return {k: os.path.join(out, k) for k in ("modeling.exe", "inversion.exe", "traveltime_tables.exe",
+                                              "migration.exe")}

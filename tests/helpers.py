@@ -1,4 +1,6 @@
 """Small seeded models and geometries shared by the tests."""
+import os
+
 import numpy as np
 
 
@@ -33,3 +35,63 @@ def rel_err(a, b, floor=1e-6):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+# parameters.txt of the C++ drivers, with the keys of the reference's run/parameters.txt
+PARAMS = """#--------------------------------------------------------------
+# Model paramenters
+x_samples = {nx}                       # <int>
+z_samples = {nz}                       # <int>
+
+x_spacing = {dx}                       # [m] <float>
+z_spacing = {dz}                       # [m] <float>
+
+slowness_file = {d}/slowness.bin
+Cijkl_folder = {d}/model_
+SPS = {d}/sps.txt
+RPS = {d}/rps.txt
+modeling_type = {mtype}
+modeling_output_folder = {d}/out_
+batch_shots = {batch}
+quiet = true
+inv_type = {invtype}
+inv_max_it = {maxit}
+smooth_per_iteration = true
+gaussian_filter_stdv = 2.0
+gaussian_filter_samples = 5
+inv_residuo_folder = {d}/
+inv_output_folder = {d}/
+inv_data_folder = {d}/
+inv_data_prefix = obs_shot_
+anisotropy = {aniso}
+mig_tables_folder = {d}/tab_
+mig_type = {migtype}
+mig_max_angle = 60
+mig_angle_spacing = 2.0
+time_samples = 400
+time_spacing = 2e-3
+max_frequency = 25.0
+mig_aperture = 35
+mig_max_offset = 600
+mig_data_folder = {d}/
+mig_data_prefix = mig_shot_
+mig_seismic_folder = {d}/
+mig_max_iteration = 3
+mig_residuo_folder = {d}/
+mig_smooth_lambda = 0.5
+"""
+
+
+def write_case(d, nx, nz, dx, dz, m, shots, recs, mtype=0, batch=False, aniso=False, migtype=0, invtype=0,
+               maxit=3):
+    m.astype(np.float32).tofile(os.path.join(d, "slowness.bin"))
+    with open(os.path.join(d, "sps.txt"), "w") as f:
+        f.write("".join(f"{x},{z}\n" for x, z in shots))
+    with open(os.path.join(d, "rps.txt"), "w") as f:
+        f.write("".join(f"{x},{z}\n" for x, z in recs))
+    p = os.path.join(d, "parameters.txt")
+    with open(p, "w") as f:
+        f.write(PARAMS.format(nx=nx, nz=nz, dx=dx, dz=dz, d=d, mtype=mtype, batch="true" if batch else "false",
+                              aniso="true" if aniso else "false", migtype=migtype, invtype=invtype,
+                              maxit=maxit))
+    return p
