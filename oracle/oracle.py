@@ -217,6 +217,18 @@ def qslowness(T, S, dx, dz, sIdz, sIdx, codes, mm, nb=3):
     return out
 
 
+def qp_factors(T, S, dx, dz, sIdz, sIdx, codes, mm, nb=3):
+    """Derivative factors of the qP pass (dSq/dS, dSq/dC11, dSq/dC13) over a
+    window, as the taped anisotropic forward writes them."""
+    T = _f32(T)
+    S = _f32(S)
+    ncols, nzz = T.shape
+    arr, keep = _codes_arg(codes)
+    f = [np.zeros_like(T) for _ in range(3)]
+    lib().orc_qp_factors(nzz, ncols, nb, T, S, nzz, dx, dz, sIdz, sIdx, arr, _f32(mm), f[0], f[1], f[2])
+    return f
+
+
 def picks(T, dx, dz, rx, rz, nb=3, c0=0):
     T = _f32(T)
     ncols, nzz = T.shape

@@ -492,3 +492,62 @@ def test_vti_gradient_isotropic_limit(oracle):
         return out
     fa, fi = fold(ga), fold(gi)
     assert np.abs(fa - fi).max() <= 2e-3 * np.abs(fi).max()
+
+
+def test_vti_factors_fp32_vs_fp64(oracle):
+    """The qP pass's derivative factors are computed in FP32 (each operation
+    rounded once). On a solved VTI field they agree with the same formulas
+    evaluated in FP64 from the same inputs to a few FP32 ulps."""
+    from helpers import smooth_model
+    from seisfat2d_gb300.synthetic import thomsen_stiffness
+    rng = np.random.default_rng(21)
+    m = smooth_model(48, 30, 10.0, seed=21)
+    vp = 1.0 / m.astype(np.float64)
+    cij = thomsen_stiffness(vp, vp / np.sqrt(3.0), 1000.0, rng.uniform(0.0, 0.25, vp.shape),
+                            rng.uniform(-0.05, 0.15, vp.shape))
+    codes, mm = [], []
+    for c in cij:
+        cd, mn, mx = oracle.compress(oracle.expand_boundary(c.astype(np.float32)))
+        codes.append(cd)
+        mm += [mn, mx]
+    mm = np.array(mm, np.float32)
+    S = oracle.expand_boundary(m)
+    T = oracle.solve_f32(S, 10.0, 10.0, 230.0, 40.0)
+    init, sIdx, sIdz = oracle.init_block_f32(S, 230.0, 40.0, 10.0, 10.0, 3)
+    fS, f11, f13 = oracle.qp_factors(T, S, 10.0, 10.0, sIdz, sIdx, codes, mm)
+
+    # FP64 restatement from the same FP32 inputs (decoded stiffness as the oracle decodes it)
+    nb = 3
+    ncols, nzz = T.shape
+    dec = [(mm[2 * q] + (codes[q].astype(np.float32) - np.float32(1.0)) * (mm[2 * q + 1] - mm[2 * q])
+            / np.float32(65534.0)).astype(np.float32).astype(np.float64) for q in range(6)]
+    c11, c13, c15, c33, c35, c55 = dec
+    Td = T.astype(np.float64)
+    sl = (slice(nb, ncols - nb), slice(nb, nzz - nb))
+    dTz = 0.5 * (Td[nb:ncols - nb, nb + 1:nzz - nb + 1] - Td[nb:ncols - nb, nb - 1:nzz - nb - 1]) / 10.0
+    dTx = 0.5 * (Td[nb + 1:ncols - nb + 1, nb:nzz - nb] - Td[nb - 1:ncols - nb - 1, nb:nzz - nb]) / 10.0
+    nrm = np.sqrt(dTx * dTx + dTz * dTz)
+    px, pz = dTx / nrm, dTz / nrm
+    c11, c13, c15, c33, c35, c55 = (c[sl] for c in (c11, c13, c15, c33, c35, c55))
+    Gxx = c11 * px * px + c55 * pz * pz + 2.0 * c15 * px * pz
+    Gzz = c55 * px * px + c33 * pz * pz + 2.0 * c35 * px * pz
+    Gxz = c15 * px * px + c35 * pz * pz + (c13 + c55) * px * pz
+    h = 0.5 * (Gxx - Gzz)
+    r = np.sqrt(h * h + Gxz * Gxz)
+    lam = 0.5 * (Gxx + Gzz) + r
+    vx = np.where(h >= 0.0, h + r, Gxz)
+    vz = np.where(h >= 0.0, Gxz, r - h)
+    nv = np.sqrt(vx * vx + vz * vz)
+    vx, vz = vx / nv, vz / nv
+    fs = np.sqrt(c33 / lam)
+    sq = S.astype(np.float64)[sl] * fs
+    e11 = -0.5 * sq * px * px * vx * vx / lam
+    e13 = -sq * px * pz * vx * vz / lam
+    keep = np.ones(fs.shape, bool)
+    keep[sIdx - nb, sIdz - nb] = False  # the source node keeps (1, 0, 0)
+    for got, want in ((fS, fs), (f11, e11), (f13, e13)):
+        g = got[sl].astype(np.float64)[keep]
+        w = want[keep]
+        err = np.abs(g - w).max() / np.abs(w).max()
+        print(f"max |FP32 - FP64| / max |FP64| = {err:.2e}")
+        assert err <= 2e-6
