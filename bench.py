@@ -214,12 +214,13 @@ class CpuPort:
 
 def cpu_baseline(w, seconds, fa):
     port = CpuPort(w, fa)
-    n, _ = port.calibrate(seconds)
+    n, one = port.calibrate(seconds)
     sel = port.sample(n)
     t0 = time.perf_counter()
     used = port.run(sel, port.nthreads)
     dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": UNIT, "cores": used, "kind": "port", "sample": port.describe(n, dt)}
+    return {"value": n / dt, "unit": UNIT, "cores": used, "kind": "port", "sample": port.describe(n, dt),
+            "single_thread_ms_per_shot": 1e3 * one}
 
 
 def run_reference(a):
@@ -233,7 +234,7 @@ def run_reference(a):
     w = workload(a.config)
     fa = a.config in FA_CONFIGS
     port = CpuPort(w, fa)
-    n, _ = port.calibrate(a.cpu_seconds / max(1, a.steps))
+    n, one = port.calibrate(a.cpu_seconds / max(1, a.steps))
     for k in range(a.warmup):
         port.run(port.sample(n, k), port.nthreads)
     done, tot, used = 0, 0.0, 1
@@ -251,7 +252,7 @@ def run_reference(a):
             "config": {"workload": w.name, "nshots": len(w.shots), "nrec": len(w.rx), "grid": [w.nx, w.nz],
                        "dh": w.dx, "step": "forward+adjoint" if fa else "forward"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": used, "kind": "port",
-                             "sample": port.describe(n, tot)},
+                             "sample": port.describe(n, tot), "single_thread_ms_per_shot": 1e3 * one},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference has no CPU eikonal path and no adjoint; this arm times the oracle's "
                     "FP32 restatement of its schedule on the host cores"}

@@ -34,6 +34,7 @@ def test_reference_arm_prints_one_contract_line(oracle):
     assert d["config"]["workload"].startswith("cfg4_adjoint_1701x351_100shots_400rec")
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["single_thread_ms_per_shot"] > 0
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
 
