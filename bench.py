@@ -507,6 +507,9 @@ def run_ours(a):
                      "kernel": dom["kernel"], "algorithmic_bytes": dom["algorithmic_bytes"],
                      "stages": stages, "timing": "CUDA events recorded by the engine around each launch "
                                                  "(sf_set_kernel_timing), mean over the eager steps",
+                     "limiter": "latency of the sweep recurrence: a shot's critical path is 4 sweeps x "
+                                "(columns + 31) dependent warp-steps, and the batch fills about 12% of the "
+                                "warp slots; HBM is the bound the fraction is quoted against",
                      "step": {"algorithmic_bytes": step_bytes,
                               "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
                               "frac": step_bytes / (ms / 1e3) / 1e9 / peak}},
