@@ -507,7 +507,7 @@ def run_ours(a):
                      "kernel": dom["kernel"], "algorithmic_bytes": dom["algorithmic_bytes"],
                      "stages": stages, "timing": "CUDA events recorded by the engine around each launch "
                                                  "(sf_set_kernel_timing), mean over the eager steps",
-                     "limiter": "latency of the sweep recurrence: a shot's critical path is 4 sweeps x "
+                     "limiter": "latency of the sweep recurrence: each solve of a shot is 4 sweeps x "
                                 "(columns + 31) dependent warp-steps, and the batch fills about 12% of the "
                                 "warp slots; HBM is the bound the fraction is quoted against",
                      "step": {"algorithmic_bytes": step_bytes,
