@@ -551,3 +551,27 @@ def test_vti_factors_fp32_vs_fp64(oracle):
         err = np.abs(g - w).max() / np.abs(w).max()
         print(f"max |FP32 - FP64| / max |FP64| = {err:.2e}")
         assert err <= 2e-6
+
+
+@pytest.mark.parametrize("stdv,samples", [(5.0, 11), (2.0, 5), (3.0, 3), (0.0, 7), (1.5, 1), (4.0, 15)])
+def test_smoothing_matches_reference_code(oracle, stdv, samples):
+    """The oracle's model_smoothing restatement equals the reference's own
+    Inversion::model_smoothing / smooth_matrix (src/inversion/inversion.cpp:
+    347-447, compiled from the reference source by oracle/build_ref.py) bit
+    for bit. Needs the reference sources (present where the fixtures are
+    made, not on the GPU machines)."""
+    import ctypes as C
+    from oracle import build_ref
+    lib = build_ref.build_inversion_host()
+    if lib is None:
+        pytest.skip("reference sources not present")
+    L = C.CDLL(lib)
+    L.ref_model_smoothing.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float]
+    rng = np.random.default_rng(samples)
+    for nx, nz in ((37, 23), (64, 9)):
+        m = rng.standard_normal((nx, nz)).astype(np.float32) * np.float32(1e-5)
+        ref = np.ascontiguousarray(m.copy())
+        L.ref_model_smoothing(ref.ctypes.data, nx, nz, samples, stdv)
+        ours = oracle.model_smoothing(m, stdv, samples)
+        assert np.array_equal(ours, ref), np.abs(ours - ref).max()
+        assert np.array_equal(ref, m) == (stdv == 0.0 or samples == 1)
