@@ -189,10 +189,39 @@ def build_inversion_host():
     return INV_LIB
 
 
+MOD_HARNESS_SRC = os.path.join(HERE, "ref_modeling_harness.cu")
+MOD_LIB = os.path.join(OUT, "libref_modeling_host.so")
+MOD_SRCS = ["src/modeling/modeling.cu", "src/admin/admin.cpp", "src/geometry/geometry.cpp"]
+
+
+def build_modeling_host():
+    """The reference's Modeling host methods (with admin.cpp and geometry.cpp,
+    which they call) and the setup harness, into
+    ``oracle/_ref/libref_modeling_host.so``; None without the reference
+    sources. Built without OpenMP."""
+    srcs = [os.path.join(REF, r) for r in MOD_SRCS]
+    if not all(os.path.exists(x) for x in srcs):
+        return None
+    stub = os.path.join(OUT, "stub")
+    os.makedirs(stub, exist_ok=True)
+    with open(os.path.join(stub, "fftw3.h"), "w") as f:
+        f.write(FFTW_STUB)
+    newest = max(os.path.getmtime(x) for x in srcs + [MOD_HARNESS_SRC])
+    if os.path.exists(MOD_LIB) and os.path.getmtime(MOD_LIB) >= newest:
+        return MOD_LIB
+    cmd = ["nvcc", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-O2", "--std=c++17",
+           "-gencode", "arch=compute_103a,code=sm_103a", "-I", stub, "-I", os.path.join(REF, "src", "modeling"),
+           *srcs, MOD_HARNESS_SRC, "-o", MOD_LIB + ".tmp"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    os.replace(MOD_LIB + ".tmp", MOD_LIB)
+    return MOD_LIB
+
+
 def build():
     build_cubins()
     build_harness()
     build_inversion_host()
+    build_modeling_host()
 
 
 def available():

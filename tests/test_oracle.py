@@ -575,3 +575,55 @@ def test_smoothing_matches_reference_code(oracle, stdv, samples):
         ours = oracle.model_smoothing(m, stdv, samples)
         assert np.array_equal(ours, ref), np.abs(ours - ref).max()
         assert np.array_equal(ref, m) == (stdv == 0.0 or samples == 1)
+
+
+def _ref_modeling_host():
+    import ctypes as C
+    from oracle import build_ref
+    lib = build_ref.build_modeling_host()
+    if lib is None:
+        pytest.skip("reference sources not present")
+    L = C.CDLL(lib)
+    L.ref_expand_boundary.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+    L.ref_compression.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    return L
+
+
+@pytest.mark.parametrize("nx,nz", [(40, 20), (17, 33), (1, 5)])
+def test_padding_matches_reference_code(oracle, nx, nz):
+    """The oracle's expand_boundary (the padding behind every golden vector and
+    the engine's sf_set_slowness) equals the reference's own
+    Modeling::expand_boundary (src/modeling/modeling.cu:204-232, compiled from
+    the reference sources) bit for bit."""
+    L = _ref_modeling_host()
+    nb = 3
+    m = np.random.default_rng(nx * nz).uniform(2e-4, 7e-4, (nx, nz)).astype(np.float32)
+    ref = np.zeros((nx + 2 * nb, nz + 2 * nb), np.float32)
+    L.ref_expand_boundary(np.ascontiguousarray(m).ctypes.data, ref.ctypes.data, nx, nz, nb)
+    assert np.array_equal(oracle.expand_boundary(m), ref)
+
+
+def test_quantisation_matches_reference_code(oracle):
+    """The oracle's Cij quantisation equals the reference's own
+    Modeling::compression (modeling.cu:264-279, compiled single-threaded)
+    for varying fields: same range and same codes. A constant field makes the
+    reference divide 0 by 0; both decode to the constant, so only the range is
+    compared there."""
+    import ctypes as C
+    from seisfat2d_gb300.synthetic import thomsen_stiffness
+    L = _ref_modeling_host()
+    rng = np.random.default_rng(7)
+    vp = rng.uniform(1500.0, 4500.0, (50, 30))
+    cij = thomsen_stiffness(vp, vp / np.sqrt(3.0), 1000.0, rng.uniform(0.0, 0.25, vp.shape),
+                            rng.uniform(-0.05, 0.15, vp.shape), tilt_deg=20.0)
+    cij.append(np.full(vp.shape, 3.5e9))
+    for k, c in enumerate(cij):
+        f = oracle.expand_boundary(c.astype(np.float32))
+        codes, mn, mx = oracle.compress(f)
+        ref = np.zeros(f.size, np.uint16)
+        rmx, rmn = C.c_float(), C.c_float()
+        L.ref_compression(np.ascontiguousarray(f).ctypes.data, ref.ctypes.data, f.size, C.byref(rmx),
+                          C.byref(rmn))
+        assert (mn, mx) == (rmn.value, rmx.value)
+        if mx > mn:
+            assert np.array_equal(codes.ravel(), ref), k
