@@ -627,3 +627,36 @@ def test_quantisation_matches_reference_code(oracle):
         assert (mn, mx) == (rmn.value, rmx.value)
         if mx > mn:
             assert np.array_equal(codes.ravel(), ref), k
+
+
+def test_picks_match_reference_code(oracle):
+    """The oracle's picks (receiver stencil + Catmull-Rom rule) equal the
+    reference's own compute_seismogram host loop and cubic2d
+    (modeling.cu:161-194, admin.cpp:121-133, compiled from the reference
+    sources) bit for bit, for receivers whose 4x4 stencil lies inside the
+    field (the reference reads outside it otherwise; the oracle and the engine
+    return NaN there). Runs without a GPU only: the reference's copy of the
+    device field must fail to leave the given field in place."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("needs a machine without a GPU")
+    L = _ref_modeling_host()
+    L.ref_compute_seismogram.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p,
+                                         C.c_void_p, C.c_int, C.c_void_p]
+    nx, nz, nb = 60, 30, 3
+    for dx, dz in ((10.0, 10.0), (12.5, 7.5)):
+        S = oracle.expand_boundary(np.full((nx, nz), 1.0 / 2000.0, np.float32))
+        T = oracle.solve_f32(S, dx, dz, 0.37 * nx * dx, 0.2 * nz * dz)
+        rng = np.random.default_rng(int(dx * 10))
+        rx = rng.uniform(0.0, (nx - 1) * dx, 300).astype(np.float32)
+        rz = rng.uniform(0.0, (nz - 1) * dz, 300).astype(np.float32)
+        ours = oracle.picks(T, dx, dz, rx, rz)
+        ref = np.zeros(300, np.float32)
+        Tc = np.ascontiguousarray(T.copy())
+        L.ref_compute_seismogram(Tc.ctypes.data, nx, nz, nb, dx, dz, rx.ctypes.data, rz.ctypes.data, 300,
+                                 ref.ctypes.data)
+        ok = ~np.isnan(ours)
+        assert ok.sum() > 200
+        assert np.array_equal(Tc, T)
+        assert np.array_equal(ours[ok], ref[ok])
