@@ -217,11 +217,40 @@ def build_modeling_host():
     return MOD_LIB
 
 
+MIG_HARNESS_SRC = os.path.join(HERE, "ref_migration_harness.cu")
+MIG_LIB = os.path.join(OUT, "libref_migration_host.so")
+MIG_SRCS = MOD_SRCS + ["src/modeling/eikonal_iso.cu", "src/modeling/eikonal_ani.cu", "src/migration/migration.cu"]
+
+
+def build_migration_host():
+    """The reference's Migration host methods (with the modeling sources they
+    link against) and the wavelet harness, into
+    ``oracle/_ref/libref_migration_host.so``; None without the reference
+    sources."""
+    srcs = [os.path.join(REF, r) for r in MIG_SRCS]
+    if not all(os.path.exists(x) for x in srcs):
+        return None
+    stub = os.path.join(OUT, "stub")
+    os.makedirs(stub, exist_ok=True)
+    with open(os.path.join(stub, "fftw3.h"), "w") as f:
+        f.write(FFTW_STUB)
+    newest = max(os.path.getmtime(x) for x in srcs + [MIG_HARNESS_SRC])
+    if os.path.exists(MIG_LIB) and os.path.getmtime(MIG_LIB) >= newest:
+        return MIG_LIB
+    cmd = ["nvcc", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-O2", "--std=c++17",
+           "-gencode", "arch=compute_103a,code=sm_103a", "-I", stub, "-I", os.path.join(REF, "src", "migration"),
+           *srcs, MIG_HARNESS_SRC, "-o", MIG_LIB + ".tmp"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    os.replace(MIG_LIB + ".tmp", MIG_LIB)
+    return MIG_LIB
+
+
 def build():
     build_cubins()
     build_harness()
     build_inversion_host()
     build_modeling_host()
+    build_migration_host()
 
 
 def available():

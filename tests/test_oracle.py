@@ -660,3 +660,23 @@ def test_picks_match_reference_code(oracle):
         assert ok.sum() > 200
         assert np.array_equal(Tc, T)
         assert np.array_equal(ours[ok], ref[ok])
+
+
+@pytest.mark.parametrize("fmax,dt", [(25.0, 2e-3), (30.0, 1e-3), (12.5, 4e-3), (45.0, 5e-4)])
+def test_wavelet_matches_reference_code(oracle, fmax, dt):
+    """The oracle's Ricker wavelet equals the reference's own
+    Migration::set_wavelet (src/migration/migration.cu:54-71, compiled from the
+    reference sources) bit for bit: length and samples."""
+    import ctypes as C
+    from oracle import build_ref
+    lib = build_ref.build_migration_host()
+    if lib is None:
+        pytest.skip("reference sources not present")
+    L = C.CDLL(lib)
+    L.ref_set_wavelet.argtypes = [C.c_float, C.c_float, C.c_void_p, C.c_int]
+    L.ref_set_wavelet.restype = C.c_int
+    ref = np.zeros(4096, np.float32)
+    nw = L.ref_set_wavelet(fmax, dt, ref.ctypes.data, ref.size)
+    ours = oracle.kirchhoff_wavelet(fmax, dt)
+    assert nw > 0 and len(ours) == nw
+    assert np.array_equal(ours, ref[:nw])
