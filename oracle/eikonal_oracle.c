@@ -2,6 +2,14 @@
  * CPU oracle for the SeisFAT2D fast-sweeping eikonal path (test infrastructure;
  * see eikonal_oracle.h for what each function restates). Build with
  * -ffp-contract=off so that every FP32 operation rounds once, in source order.
+ *
+ * Pinned to the reference itself: the solver (isotropic and anisotropic)
+ * against the reference's own kernels, compiled from its sources and run on
+ * a GB300 (tests/golden/*.npz, tests/test_gpu_reference.py); the padding,
+ * Cij quantisation, picks, smoothing and Kirchhoff wavelet against the
+ * reference's own host methods, compiled from its sources by
+ * oracle/build_ref.py (tests/test_oracle.py). The adjoint has no counterpart
+ * in the reference; it is checked against finite differences.
  */
 #include "eikonal_oracle.h"
 
