@@ -5,7 +5,7 @@
  *
  * Pinned to the reference itself: the solver (isotropic and anisotropic)
  * against the reference's own kernels, compiled from its sources and run on
- * a GB300 (tests/golden/*.npz, tests/test_gpu_reference.py); the padding,
+ * a GB300 (the npz files of tests/golden, tests/test_gpu_reference.py); the padding,
  * Cij quantisation, picks, smoothing and Kirchhoff wavelet against the
  * reference's own host methods, compiled from its sources by
  * oracle/build_ref.py (tests/test_oracle.py). The adjoint has no counterpart
