@@ -558,8 +558,7 @@ def test_smoothing_matches_reference_code(oracle, stdv, samples):
     """The oracle's model_smoothing restatement equals the reference's own
     Inversion::model_smoothing / smooth_matrix (src/inversion/inversion.cpp:
     347-447, compiled from the reference source by oracle/build_ref.py) bit
-    for bit. Needs the reference sources (present where the fixtures are
-    made, not on the GPU machines)."""
+    for bit. Skipped where the reference sources are absent."""
     import ctypes as C
     from oracle import build_ref
     lib = build_ref.build_inversion_host()
