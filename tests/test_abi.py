@@ -45,3 +45,43 @@ def test_engine_refuses_missing_library(tmp_path, monkeypatch):
         assert "no CPU fallback" in str(e)
     else:
         raise AssertionError("load() must fail without the library")
+
+
+def test_every_entry_point_rejects_a_null_context(engine_lib):
+    """Host-side argument checks, no device work: every entry point that takes
+    a context returns SF_ERR_ARG for a null one (destroying a null context is
+    a no-op, as free(NULL) is), and the no-allocation solver rejects a null
+    field."""
+    from seisfat2d_gb300 import _lib
+    L = _lib.load()
+    skip = {"sf_ctx_create", "sf_status_string", "sf_ctx_last_error", "sf_time_propagation_noalloc"}
+    for name, (res, args) in sorted(_lib.SIGNATURES.items()):
+        if name in skip:
+            continue
+        vals = []
+        for a in args:
+            if a in (C.c_int, C.c_uint, C.c_long, C.c_size_t):
+                vals.append(0)
+            elif a in (C.c_float, C.c_double):
+                vals.append(0.0)
+            elif isinstance(a, type) and issubclass(a, C.Array):
+                vals.append(a())
+            else:
+                vals.append(None)
+        st = getattr(L, name)(*vals)
+        assert st == (0 if name == "sf_ctx_destroy" else 1), (name, st)
+    assert L.sf_ctx_last_error(None) == b"null context"
+    st = L.sf_time_propagation_noalloc(None, 10, 10, 1.0, 1.0, 0.0, 0.0, None, None)
+    assert st == 1
+
+
+def test_context_creation_fails_cleanly_without_a_gpu(engine_lib):
+    import pytest
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from seisfat2d_gb300 import _lib
+    L = _lib.load()
+    ctx = C.c_void_p()
+    st = L.sf_ctx_create(C.byref(ctx), 40, 20, 10.0, 10.0, 0)
+    assert st == 2 and not ctx.value  # SF_ERR_CUDA, no context handed out
