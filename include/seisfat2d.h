@@ -44,6 +44,7 @@ extern "C" {
 /* arithmetic of the FP32 sweeps (sf_set_arithmetic) */
 #define SF_ARITH_REFERENCE 0 /* the reference build's: FP32 init, nvcc's FMAs (default) */
 #define SF_ARITH_IEEE 1      /* every operation rounded once, FP64 3x3 initialisation */
+#define SF_ARITH_COMPENSATED 2 /* traveltimes carried as FP32 pairs hi + lo (see sf_set_arithmetic) */
 
 /* strip-loop forms (sf_set_strip_loop) */
 #define SF_LOOP_AUTO -1    /* interior-block body when all shots run at once, one window width, a warp per strip */
@@ -120,6 +121,14 @@ int sf_batch_table(sf_ctx* ctx, int shot, float* T, int mem, void* stream);
 int sf_batch_adjoint(sf_ctx* ctx, const float* pick_grad, int pg_mem, float* grad, int grad_mem,
                      void* stream);
 
+/* Branch codes of shot `shot` (caller order) of the last SF_KEEP_TAPE batch:
+ * 4 x ncols x nzz bytes, [sweep][window column][row], one code per node and
+ * sweep (bits 0-2: candidate 0 none/kept, 1 t1d1, 2 t1d2, 3 2D, 4 and 5 the
+ * edge updates; bits 3-4: the slowness cell (i-1+b3, j-1+b4) that candidate
+ * read). No counterpart in the reference: it lets a checker evaluate the same
+ * branch pattern in FP64. Synchronises the stream. */
+int sf_batch_tape_codes(sf_ctx* ctx, int shot, uint8_t* codes, int mem, void* stream);
+
 /* Anisotropic batches (sf_batch_forward with ani = 1 and SF_KEEP_TAPE) tape
  * the second, qP solve. Their adjoint (sf_batch_adjoint or
  * sf_batch_misfit_gradient) multiplies each shot's gradient with respect to
@@ -149,7 +158,16 @@ int sf_synchronize(sf_ctx* ctx, void* stream);
  * nvcc with its default FMA contraction): FP32 initialisation and fused
  * multiply-adds for t1d1, t1d2, the 2D numerator and the discriminant.
  * SF_ARITH_IEEE rounds every operation once and evaluates the 3x3
- * initialisation in FP64. */
+ * initialisation in FP64. SF_ARITH_COMPENSATED (no counterpart in the
+ * reference) solves the same scheme with every traveltime carried as an
+ * unevaluated FP32 pair hi + lo: the update's branch tests and increments
+ * are formed from differences of the pairs and the winning candidate is
+ * added to its base time with TwoSum, so rounding no longer accumulates
+ * along a sweep (the FP32 field stays within about 1e-7 of an FP64 solve,
+ * where the other two drift to about 1e-5, and the adjoint's coefficients,
+ * which depend on differences of neighbouring times, follow). The
+ * traveltimes callers see are the hi parts; tapes, picks and gradients keep
+ * their formats. At most 8 warps per CTA (sf_set_launch). */
 int sf_set_arithmetic(sf_ctx* ctx, int mode);
 int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
 
@@ -164,10 +182,12 @@ int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
  * holds until exit: grids with ceil(nzz/32) * nxx > 262144 are rejected with
  * SF_ERR_RANGE. The first call on a device sets that device up (looks up the
  * array's device address, sets the kernel's shared-memory limit); make it
- * before any stream capture. Calls share the array: calls that overlap on the
- * GPU (other streams, other threads) race and must be serialised by the
- * caller. Synchronises `stream`; returns SF_ERR_TIMEOUT if an in-kernel wait
- * gave up. */
+ * before any stream capture. The first call with new cell sizes (dx, dz) on
+ * a device also checks the node update's fast division for them, in the
+ * array, and waits for that check. Calls share the array: calls that
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. Synchronises `stream`; returns SF_ERR_TIMEOUT
+ * if an in-kernel wait gave up. */
 int sf_time_propagation_noalloc(const float* S, int nx, int nz, float dx, float dz, float sx, float sz,
                                 float* T, void* stream);
 

@@ -21,7 +21,9 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("SF_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: SF_REFERENCE_ROOT, else a folder named `reference`
+# beside this repository
+REF = os.environ.get("SF_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 OUT = os.path.join(HERE, "_ref")
 BUILD = os.path.join(HERE, "_build")
 CUBINS = {"modeling": "src/modeling/modeling.cu", "eikonal_ani": "src/modeling/eikonal_ani.cu",

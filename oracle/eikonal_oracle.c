@@ -433,6 +433,176 @@ static double node64(int sweep, int i, int j, int nzz, int ncols, const float* S
     return upd64(TAT(i, j), tv, te, tev, s1a, s1b, s2a, s2b, sref, k, dr1, dc1a, dc2, dr2a, rec);
 }
 
+#define TP(k, i, j) (((size_t)(k) * ncols + (size_t)(j)) * nzz + (size_t)(i))
+
+static int is_skip(int s, int i, int j, const int si[4], const int sj[4])
+{
+    return i == si[s] && j == sj[s];
+}
+
+/*
+ * Compensated FP32 update (orc_set_arith(2); no counterpart in the reference).
+ * A traveltime is an unevaluated sum hi + lo of two FP32 values. All the
+ * update's decisions and increments depend on differences of the upwind
+ * times only, so they are formed from the pairs, (a.h - b.h) + (a.l - b.l),
+ * and the candidates are compared in FP32 next to a nearby finite time (the
+ * two 1D ones next to te, the 1D and the 2D or edge winner next to tev, the
+ * winner and the old value next to the winner's base), never next to the
+ * 1e6 sentinel; the winner is its base time plus its FP32 increment, added
+ * with Knuth's TwoSum and
+ * renormalised with Dekker's Fast2Sum (D. E. Knuth, TAOCP vol. 2, 4.2.2;
+ * T. J. Dekker, Numer. Math. 18, 1971). The rounding error of each node is
+ * then relative to its increment instead of its time, so it no longer
+ * accumulates along the sweep. Same candidates, branch tests and tape
+ * coefficients as upd32 (IEEE operations, no contraction); hi is the
+ * traveltime that callers see.
+ */
+typedef struct {
+    float h, l;
+} ff_t;
+
+static ff_t ff_add(ff_t a, float b)
+{
+    const float s = a.h + b, bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b - bb);
+    const float l = e + a.l, h = s + l;
+    ff_t r = {h, l - (h - s)};
+    return r;
+}
+
+static float ff_diff(ff_t a, ff_t b) { return (a.h - b.h) + (a.l - b.l); }
+
+static ff_t updc(ff_t told, ff_t tv, ff_t te, ff_t tev, float s1a, float s1b, float s2a, float s2b, float sref,
+                 const k32* k, int dr1, int dc1a, int dc2, int dr2a, rec_t* rec)
+{
+    const float dte = ff_diff(te, tev), dtv = ff_diff(tv, tev), dvt = ff_diff(tv, te);
+    const float m1 = fminf(s1a, s1b), m2 = fminf(s2a, s2b);
+    const float i1 = k->dz * m1, i2 = k->dx * m2;   /* t1d1 = tv + i1, t1d2 = te + i2 */
+    const int w11 = (dvt + i1) <= i2;                /* t1d1 <= t1d2, compared next to te */
+    const float o1D = w11 ? dtv + i1 : dte + i2;     /* the 1D winner's offset to tev */
+    float o3 = SF_BIG, o4 = SF_BIG, o5 = SF_BIG, inc = 0.0f;
+    int br = 0;
+    float rr = 0.0f, dd = 0.0f, q = 0.0f, qq = 0.0f;
+    const float D = k->dz2i + k->dx2i;
+    if ((dvt <= k->dx * sref) && (-dvt <= k->dz * sref) && (dte >= 0.0f) && (dtv >= 0.0f)) {
+        dd = -2.0f * dvt; /* ta - tb = 2 (te - tv) */
+        rr = sqrtf(4.0f * sref * sref * D - k->dz2i * k->dx2i * dd * dd);
+        o3 = (rr - dvt * (k->dx2i - k->dz2i)) / D; /* t1 = tev + o3 */
+        br = 3;
+    } else if ((dte <= sref * k->dz * k->dz / k->hyp) && (dte > 0.0f)) {
+        q = dte / k->dz;
+        qq = sqrtf(sref * sref - q * q);
+        inc = k->dx * qq; /* t2 = te + inc */
+        o4 = dte + inc;
+        br = 4;
+    } else if ((dtv <= sref * k->dx * k->dx / k->hyp) && (dtv > 0.0f)) {
+        q = dtv / k->dx;
+        qq = sqrtf(sref * sref - q * q);
+        inc = k->dz * qq; /* t3 = tv + inc */
+        o5 = dtv + inc;
+        br = 5;
+    }
+    /* a 2D or edge candidate needs tev close to its base, so both winners'
+     * offsets to tev are exact enough to compare */
+    const float o2D = fminf(o3, fminf(o4, o5));
+    const int w1 = o1D <= o2D;
+    ff_t base;
+    float bi;
+    if (w1) {
+        base = w11 ? tv : te;
+        bi = w11 ? i1 : i2;
+    } else {
+        base = (br == 3) ? tev : (br == 4 ? te : tv);
+        bi = (br == 3) ? o3 : inc;
+    }
+    if (rec) {
+        rec->code = 0;
+        rec->c1 = 0.0;
+        rec->c2 = 0.0;
+    }
+    /* the candidate replaces told when it is smaller, compared next to its base */
+    if (!(bi < ff_diff(told, base))) return told;
+    if (rec) {
+        if (w1) {
+            if (w11) {
+                int dc = (s1a <= s1b) ? dc1a : 1;
+                rec->code = 1 | (dr1 << 3) | (dc << 4);
+                rec->c2 = k->dz;
+            } else {
+                int dr = (s2a <= s2b) ? dr2a : 1;
+                rec->code = 2 | (dr << 3) | (dc2 << 4);
+                rec->c2 = k->dx;
+            }
+        } else {
+            rec->code = br | (dr1 << 3) | (dc2 << 4);
+            if (br == 3) {
+                float kA = k->dz2i - k->dx2i;
+                float k2K = 2.0f * (k->dz2i * k->dx2i);
+                if (rr > 0.0f) {
+                    rec->c1 = (kA + (k2K * dd) / rr) / D;
+                    rec->c2 = (4.0f * sref) / rr;
+                } else {
+                    rec->c1 = kA / D;
+                }
+            } else {
+                float hx = (br == 4) ? k->dx : k->dz, hq = (br == 4) ? k->dz : k->dx;
+                if (qq > 0.0f) {
+                    rec->c1 = (hx * q) / (hq * qq);
+                    rec->c2 = (hx * sref) / qq;
+                }
+            }
+        }
+    }
+    return ff_add(base, bi);
+}
+
+/* One compensated solve (1 pass, any DAG order gives the same bits): T gets
+ * the hi parts; the initial 3x3 values enter with lo = 0. */
+static void solve_comp(int nzz, int ncols, const float* S, int ldS, float dx, float dz, int sIdz, int sIdx_loc,
+                       const float init[9], float* T, uint8_t* code, float* c1, float* c2)
+{
+    k32 k = make_k32(dx, dz);
+    int si[4], sj[4];
+    orc_skip_cells(ncols, nzz, si, sj);
+    float* L = (float*)calloc((size_t)nzz * ncols, sizeof(float));
+    for (size_t n = 0; n < (size_t)nzz * ncols; n++) T[n] = SF_BIG;
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) TAT(sIdz + a - 1, sIdx_loc + b - 1) = init[a + 3 * b];
+    if (code) {
+        memset(code, 0, (size_t)4 * ncols * nzz);
+        for (size_t n = 0; n < (size_t)4 * ncols * nzz; n++) c1[n] = c2[n] = 0.0f;
+    }
+#define PAIR(i, j) ((ff_t){TAT(i, j), L[(size_t)(i) + (size_t)(j) * nzz]})
+    for (int s = 0; s < 4; s++) {
+        int sz, sx;
+        sweep_signs(s, &sz, &sx);
+        for (int jj = 1; jj <= ncols - 2; jj++) {
+            int j = (sx > 0) ? jj : ncols - 1 - jj;
+            for (int ii = 1; ii <= nzz - 2; ii++) {
+                int i = (sz > 0) ? ii : nzz - 1 - ii;
+                if (is_skip(s, i, j, si, sj)) continue;
+                int i1 = (sz > 0) ? i - 1 : i, j1 = (sx > 0) ? j - 1 : j;
+                float s1a = SAT(i1, imax(j - 1, 1)), s1b = SAT(i1, imin(j, ncols - 1));
+                float s2a = SAT(imax(i - 1, 1), j1), s2b = SAT(imin(i, nzz - 1), j1);
+                int dr1 = (sz > 0) ? 0 : 1, dc2 = (sx > 0) ? 0 : 1;
+                int dc1a = (j - 1 >= 1) ? 0 : 1, dr2a = (i - 1 >= 1) ? 0 : 1;
+                rec_t r;
+                ff_t v = updc(PAIR(i, j), PAIR(i - sz, j), PAIR(i, j - sx), PAIR(i - sz, j - sx), s1a, s1b, s2a,
+                              s2b, SAT(i1, j1), &k, dr1, dc1a, dc2, dr2a, code ? &r : NULL);
+                TAT(i, j) = v.h;
+                L[(size_t)i + (size_t)j * nzz] = v.l;
+                if (code) {
+                    code[TP(s, i, j)] = (uint8_t)r.code;
+                    c1[TP(s, i, j)] = (float)r.c1;
+                    c2[TP(s, i, j)] = (float)r.c2;
+                }
+            }
+        }
+    }
+#undef PAIR
+    free(L);
+}
+
 static void init_field_f32(float* T, int nzz, int ncols, int sIdz, int sIdx_loc, const float init[9])
 {
     for (size_t n = 0; n < (size_t)nzz * ncols; n++) T[n] = SF_BIG; /* time_set */
@@ -447,14 +617,14 @@ static void init_field_f64(double* T, int nzz, int ncols, int sIdz, int sIdx_loc
         for (int a = 0; a < 3; a++) TAT(sIdz + a - 1, sIdx_loc + b - 1) = init[a + 3 * b];
 }
 
-static int is_skip(int s, int i, int j, const int si[4], const int sj[4])
-{
-    return i == si[s] && j == sj[s];
-}
 
 void orc_solve_f32(int nzz, int ncols, const float* S, int ldS, float dx, float dz, int sIdz,
                    int sIdx_loc, const float init[9], float* T, int passes, int order)
 {
+    if (g_arith == 2) {
+        solve_comp(nzz, ncols, S, ldS, dx, dz, sIdz, sIdx_loc, init, T, NULL, NULL, NULL);
+        return;
+    }
     k32 k = make_k32(dx, dz);
     int si[4], sj[4];
     orc_skip_cells(ncols, nzz, si, sj);
@@ -785,6 +955,114 @@ void orc_seed_lambda_f64(int nzz, int ncols, int c0, float dx, float dz, int nb,
     }
 }
 
+/* FP64 picks of one FP64 window field: the 16 FP64 Catmull-Rom weights of
+ * orc_pick_weights_f64 times the nodes, NaN where the stencil leaves the
+ * window. */
+void orc_picks_f64(const double* T, int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
+                   const float* rz, int nrec, double* out)
+{
+    for (int r = 0; r < nrec; r++) {
+        int i, j;
+        double w[16];
+        if (orc_pick_weights_f64(rx[r], rz[r], dx, dz, nb, nzz, ncols, c0, &i, &j, w)) {
+            out[r] = NAN;
+            continue;
+        }
+        double acc = 0.0;
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++) acc += w[a * 4 + b] * TAT(i + b - 1, j + a - 1);
+        out[r] = acc;
+    }
+}
+
+/* FP64 misfit of a batch on the padded slowness S: 0.5 sum over shots and
+ * receivers (in order) of (p - tobs)^2, p the FP64 picks of the FP64 1-pass
+ * solve with its own branches and the FP64 initialisation; receivers
+ * without a pick or NaN tobs are left out. T is nzz x max(ncols) scratch. */
+static double misfit_f64(int nzz, int nb, const float* S, float dx, float dz, int nshots, const float* sx,
+                         const float* sz, const int* c0, const int* ncols, const float* rx, const float* rz,
+                         int nrec, const double* tobs, double* T, double* pk)
+{
+    double J = 0.0;
+    for (int b = 0; b < nshots; b++) {
+        int sIdx, sIdz;
+        orc_source_index(sx[b], sz[b], dx, dz, nb, &sIdx, &sIdz);
+        double init[9];
+        orc_init_block_f64(S, nzz, sx[b], sz[b], dx, dz, nb, sIdx, sIdz, init);
+        const float* Sw = S + (size_t)c0[b] * nzz;
+        orc_solve_f64(nzz, ncols[b], Sw, nzz, dx, dz, sIdz, sIdx - c0[b], init, T, 1, 0.0, 1);
+        orc_picks_f64(T, nzz, ncols[b], c0[b], dx, dz, nb, rx, rz, nrec, pk);
+        for (int r = 0; r < nrec; r++) {
+            const double d = pk[r] - tobs[(size_t)b * nrec + r];
+            if (d == d) J += 0.5 * d * d;
+        }
+    }
+    return J;
+}
+
+double orc_misfit_f64(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots, const float* sx,
+                      const float* sz, const int* c0, const int* ncols, const float* rx, const float* rz, int nrec,
+                      const double* tobs)
+{
+    (void)nxx;
+    int mc = 1;
+    for (int b = 0; b < nshots; b++) mc = ncols[b] > mc ? ncols[b] : mc;
+    double* T = (double*)malloc(sizeof(double) * (size_t)nzz * mc);
+    double* pk = (double*)malloc(sizeof(double) * (nrec > 0 ? nrec : 1));
+    const double J = misfit_f64(nzz, nb, S, dx, dz, nshots, sx, sz, c0, ncols, rx, rz, nrec, tobs, T, pk);
+    free(T);
+    free(pk);
+    return J;
+}
+
+/* Central finite differences of orc_misfit_f64: for each cell (ci[q], cj[q])
+ * of the padded grid, the misfit with that slowness replaced by sp[q] =
+ * RN32(s (1 + rel)) and by sm[q] = RN32(s (1 - rel)) (both FP32 values, so
+ * the step sp - sm is exact), one (cell, sign) per thread. Returns the
+ * threads used. */
+int orc_fd_misfit_f64(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots, const float* sx,
+                      const float* sz, const int* c0, const int* ncols, const float* rx, const float* rz, int nrec,
+                      const double* tobs, int ncells, const int* ci, const int* cj, double rel, float* sp,
+                      float* sm, double* Jp, double* Jm, int nthreads)
+{
+    int used = 1;
+    int mc = 1;
+    for (int b = 0; b < nshots; b++) mc = ncols[b] > mc ? ncols[b] : mc;
+    const size_t npad = (size_t)nzz * nxx;
+    for (int q = 0; q < ncells; q++) {
+        const double s = S[(size_t)ci[q] + (size_t)cj[q] * nzz];
+        sp[q] = (float)(s * (1.0 + rel));
+        sm[q] = (float)(s * (1.0 - rel));
+    }
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    used = nthreads;
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+        float* Sc = (float*)malloc(sizeof(float) * npad);
+        double* T = (double*)malloc(sizeof(double) * (size_t)nzz * mc);
+        double* pk = (double*)malloc(sizeof(double) * (nrec > 0 ? nrec : 1));
+        memcpy(Sc, S, sizeof(float) * npad);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+        for (int t = 0; t < 2 * ncells; t++) {
+            const int q = t >> 1;
+            const size_t at = (size_t)ci[q] + (size_t)cj[q] * nzz;
+            Sc[at] = (t & 1) ? sm[q] : sp[q];
+            const double J = misfit_f64(nzz, nb, Sc, dx, dz, nshots, sx, sz, c0, ncols, rx, rz, nrec, tobs, T, pk);
+            if (t & 1) Jm[q] = J;
+            else Jp[q] = J;
+            Sc[at] = S[at];
+        }
+        free(Sc);
+        free(T);
+        free(pk);
+    }
+    return used;
+}
+
 /* -------------------------------------------------------------- full shot */
 
 int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, int c0, int ncols,
@@ -857,12 +1135,14 @@ int orc_batch_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, 
 
 /* ---------------------------------------------------------------- adjoint */
 
-#define TP(k, i, j) (((size_t)(k) * ncols + (size_t)(j)) * nzz + (size_t)(i))
-
 void orc_solve_tape_f32(int nzz, int ncols, const float* S, int ldS, float dx, float dz, int sIdz,
                         int sIdx_loc, const float init[9], float* T, uint8_t* code, float* c1,
                         float* c2)
 {
+    if (g_arith == 2) {
+        solve_comp(nzz, ncols, S, ldS, dx, dz, sIdz, sIdx_loc, init, T, code, c1, c2);
+        return;
+    }
     k32 k = make_k32(dx, dz);
     int si[4], sj[4];
     orc_skip_cells(ncols, nzz, si, sj);
@@ -910,6 +1190,78 @@ void orc_solve_tape_f64(int nzz, int ncols, const float* S, int ldS, double dx, 
                 code[TP(s, i, j)] = (uint8_t)r.code;
                 c1[TP(s, i, j)] = r.c1;
                 c2[TP(s, i, j)] = r.c2;
+            }
+        }
+    }
+}
+
+/*
+ * The FP64 evaluation of a given branch pattern: node (i, j) of sweep s takes
+ * the candidate and the slowness cell that code_in names (an FP32 tape's
+ * codes), with upd64's formulas; code 0 keeps the old value. The recorded
+ * coefficients are upd64's for that candidate. This is the same discrete
+ * scheme as the FP32 solve that wrote code_in, evaluated in FP64: its
+ * adjoint (orc_adjoint_f64 with code_in) differs from the FP32 adjoint only
+ * by FP32 rounding, while an FP64 solve that chooses its own branches also
+ * differs wherever near-tied candidates fall the other way. A radicand that
+ * rounding has pushed below zero counts as zero.
+ */
+static double follow64(int cd, double told, double tv, double te, double tev, const float* S, int ldS,
+                       int i, int j, const k64* k, double* c1, double* c2)
+{
+    const int br = cd & 7;
+    *c1 = 0.0;
+    *c2 = 0.0;
+    if (br == 0) return told;
+    const double s = SAT(i - 1 + ((cd >> 3) & 1), j - 1 + ((cd >> 4) & 1));
+    switch (br) {
+    case 1: *c2 = k->dz; return tv + k->dz * s;
+    case 2: *c2 = k->dx; return te + k->dx * s;
+    case 3: {
+        const double D = k->dz2i + k->dx2i;
+        const double ta = tev + te - tv, tb = tev - te + tv, dd = ta - tb;
+        const double disc = 4.0 * s * s * D - k->dz2i * k->dx2i * dd * dd;
+        const double rr = disc > 0.0 ? sqrt(disc) : 0.0;
+        if (rr > 0.0) {
+            *c1 = ((k->dz2i - k->dx2i) + 2.0 * k->dz2i * k->dx2i * dd / rr) / D;
+            *c2 = 4.0 * s / rr;
+        } else {
+            *c1 = (k->dz2i - k->dx2i) / D;
+        }
+        return ((tb * k->dz2i + ta * k->dx2i) + rr) / D;
+    }
+    default: {
+        const double hx = (br == 4) ? k->dx : k->dz, hq = (br == 4) ? k->dz : k->dx;
+        const double base = (br == 4) ? te : tv;
+        const double q = (base - tev) / hq;
+        const double arg = s * s - q * q;
+        const double qq = arg > 0.0 ? sqrt(arg) : 0.0;
+        if (qq > 0.0) {
+            *c1 = hx * q / (hq * qq);
+            *c2 = hx * s / qq;
+        }
+        return base + hx * qq;
+    }
+    }
+}
+
+void orc_solve_follow_f64(int nzz, int ncols, const float* S, int ldS, double dx, double dz, int sIdz,
+                          int sIdx_loc, const double init[9], const uint8_t* code_in, double* T, double* c1,
+                          double* c2)
+{
+    k64 k = make_k64(dx, dz);
+    init_field_f64(T, nzz, ncols, sIdz, sIdx_loc, init);
+    for (size_t n = 0; n < (size_t)4 * ncols * nzz; n++) c1[n] = c2[n] = 0.0;
+    for (int s = 0; s < 4; s++) {
+        int sz, sx;
+        sweep_signs(s, &sz, &sx);
+        for (int jj = 1; jj <= ncols - 2; jj++) {
+            int j = (sx > 0) ? jj : ncols - 1 - jj;
+            for (int ii = 1; ii <= nzz - 2; ii++) {
+                int i = (sz > 0) ? ii : nzz - 1 - ii;
+                const size_t t = TP(s, i, j);
+                TAT(i, j) = follow64(code_in[t], TAT(i, j), TAT(i - sz, j), TAT(i, j - sx), TAT(i - sz, j - sx), S,
+                                     ldS, i, j, &k, &c1[t], &c2[t]);
             }
         }
     }

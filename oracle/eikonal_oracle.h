@@ -116,6 +116,31 @@ void orc_solve_tape_f64(int nzz, int ncols, const float* S, int ldS, double dx, 
                         int sIdz, int sIdx_loc, const double init[9], double* T,
                         uint8_t* code, double* c1, double* c2);
 
+/* FP64 solve that follows a given branch pattern: every node takes the
+ * candidate and slowness cell named by code_in (tape layout above, e.g. the
+ * codes of an FP32 taped solve) instead of choosing its own, and records the
+ * FP64 coefficients of that candidate. With orc_adjoint_f64 over code_in it
+ * gives the FP64 adjoint of the same discrete scheme as the FP32 tape. */
+void orc_solve_follow_f64(int nzz, int ncols, const float* S, int ldS, double dx, double dz, int sIdz,
+                          int sIdx_loc, const double init[9], const uint8_t* code_in, double* T, double* c1,
+                          double* c2);
+
+/* FP64 picks of an FP64 window field (weights of orc_pick_weights_f64). */
+void orc_picks_f64(const double* T, int nzz, int ncols, int c0, float dx, float dz, int nb, const float* rx,
+                   const float* rz, int nrec, double* out);
+
+/* FP64 misfit 0.5 sum (p - tobs)^2 of a batch of shot windows (tobs nshots x
+ * nrec, NaN entries skipped), p from the FP64 1-pass solve choosing its own
+ * branches; and its central finite differences on a list of padded cells
+ * (the slowness s replaced by RN32(s(1 +- rel)), returned in sp / sm). */
+double orc_misfit_f64(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots, const float* sx,
+                      const float* sz, const int* c0, const int* ncols, const float* rx, const float* rz, int nrec,
+                      const double* tobs);
+int orc_fd_misfit_f64(int nzz, int nxx, int nb, const float* S, float dx, float dz, int nshots, const float* sx,
+                      const float* sz, const int* c0, const int* ncols, const float* rx, const float* rz, int nrec,
+                      const double* tobs, int ncells, const int* ci, const int* cj, double rel, float* sp,
+                      float* sm, double* Jp, double* Jm, int nthreads);
+
 /* Reverse sweeps over a tape. lam: adjoint of the final T (nzz x ncols), in
  * place; on return it holds the adjoint of the initial field. grad (nzz x
  * ncols, column stride nzz) receives += dJ/dS for the window, including the

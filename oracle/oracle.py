@@ -57,6 +57,17 @@ def lib():
                                          C.c_int, C.c_int, f32p, f32p, u8p, f32p, f32p]
         L.orc_solve_tape_f64.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_double, C.c_double,
                                          C.c_int, C.c_int, f64p, f64p, u8p, f64p, f64p]
+        L.orc_solve_follow_f64.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_double, C.c_double,
+                                           C.c_int, C.c_int, f64p, u8p, f64p, f64p, f64p]
+        L.orc_picks_f64.argtypes = [f64p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, f32p, f32p,
+                                    C.c_int, f64p]
+        L.orc_misfit_f64.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float, C.c_int, f32p, f32p,
+                                     i32p, i32p, f32p, f32p, C.c_int, f64p]
+        L.orc_misfit_f64.restype = C.c_double
+        L.orc_fd_misfit_f64.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float, C.c_int, f32p,
+                                        f32p, i32p, i32p, f32p, f32p, C.c_int, f64p, C.c_int, i32p, i32p,
+                                        C.c_double, f32p, f32p, f64p, f64p, C.c_int]
+        L.orc_fd_misfit_f64.restype = C.c_int
         L.orc_adjoint_f32.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, u8p, f32p, f32p, f32p,
                                       f32p, f32p]
         L.orc_adjoint_f64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, u8p, f64p, f64p, f64p,
@@ -103,7 +114,7 @@ def set_arith(mode):
     """'ieee' (every operation rounded once, FP64 init) or 'reference' (the
     reference build's FP32 init and FMAs)."""
     global _arith
-    _arith = {"ieee": 0, "reference": 1}[mode] if isinstance(mode, str) else int(mode)
+    _arith = {"ieee": 0, "reference": 1, "compensated": 2}[mode] if isinstance(mode, str) else int(mode)
     lib().orc_set_arith(_arith)
 
 
@@ -418,16 +429,23 @@ def kirchhoff_angle_forward(S, Ts, Tr, xsrc, xrec, gathers, nt, dt, dx, dz, aper
     return out
 
 
-def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False):
+def solve_tape(S, dx, dz, sx, sz, nb=3, c0=0, ncols=None, fp64=False, follow=None):
     """Forward with tape. Returns (T, code, c1, c2, sIdz, sIdx_loc); tape arrays
-    have shape (4, ncols, nzz)."""
+    have shape (4, ncols, nzz). fp64 with follow (codes (4, ncols, nzz) of an
+    FP32 tape): the FP64 solve takes those branches instead of its own."""
     S = _f32(S)
     nxx, nzz = S.shape
     ncols = nxx - c0 if ncols is None else ncols
     v, sIdx, sIdz = init_block(S, sx, sz, dx, dz, nb)
     Sw = np.ascontiguousarray(S[c0:c0 + ncols])
     code = np.zeros((4, ncols, nzz), np.uint8)
-    if fp64:
+    if fp64 and follow is not None:
+        code = np.ascontiguousarray(follow, np.uint8).reshape(4, ncols, nzz).copy()
+        T = np.zeros((ncols, nzz), np.float64)
+        c1 = np.zeros((4, ncols, nzz), np.float64)
+        c2 = np.zeros_like(c1)
+        lib().orc_solve_follow_f64(nzz, ncols, Sw, nzz, dx, dz, sIdz, sIdx - c0, v, code, T, c1, c2)
+    elif fp64:
         T = np.zeros((ncols, nzz), np.float64)
         c1 = np.zeros((4, ncols, nzz), np.float64)
         c2 = np.zeros_like(c1)
@@ -491,10 +509,12 @@ def seed_lambda(ncols, nzz, dx, dz, rx, rz, pg, c0=0, nb=3, fp64=False):
     return lam
 
 
-def batch_gradient(S, dx, dz, shots, rx, rz, pick_grad, nb=3, fp64=False):
+def batch_gradient(S, dx, dz, shots, rx, rz, pick_grad, nb=3, fp64=False, follow=None):
     """Oracle of sf_batch_adjoint: per shot (window) tape + seed + reverse
     sweeps, shot gradients summed in FP64 in shot order onto the padded grid.
-    Returns (grad (nxx, nzz), picks (nshots, nrec))."""
+    Returns (grad (nxx, nzz), picks (nshots, nrec)). fp64 with follow (one
+    code array (4, ncols, nzz) per shot, e.g. an FP32 engine's tape codes):
+    the FP64 adjoint of the same branch pattern."""
     S = _f32(S)
     nxx, nzz = S.shape
     total = np.zeros((nxx, nzz), np.float64)
@@ -503,7 +523,8 @@ def batch_gradient(S, dx, dz, shots, rx, rz, pick_grad, nb=3, fp64=False):
         sx, sz = s[0], s[1]
         c0 = int(s[2]) if len(s) > 2 else 0
         nc = int(s[3]) if len(s) > 3 and s[3] > 0 else nxx - c0
-        T, code, c1, c2, sIdz, sloc = solve_tape(S, dx, dz, sx, sz, nb, c0, nc, fp64=fp64)
+        T, code, c1, c2, sIdz, sloc = solve_tape(S, dx, dz, sx, sz, nb, c0, nc, fp64=fp64,
+                                                 follow=None if follow is None else follow[b])
         if fp64:
             pk = np.full(len(rx), np.nan)
             for r in range(len(rx)):
@@ -519,3 +540,49 @@ def batch_gradient(S, dx, dz, shots, rx, rz, pick_grad, nb=3, fp64=False):
         g, _ = adjoint((code, c1, c2, sIdz, sloc), lam, d, fp64=fp64)
         total[c0:c0 + nc] += g.astype(np.float64)
     return (total if fp64 else total.astype(np.float32)), picks_out
+
+
+def picks_f64(T, dx, dz, rx, rz, nb=3, c0=0):
+    """FP64 picks of an FP64 window field (ncols, nzz)."""
+    T = np.ascontiguousarray(T, np.float64)
+    ncols, nzz = T.shape
+    out = np.zeros(len(rx), np.float64)
+    lib().orc_picks_f64(T, nzz, ncols, c0, dx, dz, nb, _f32(rx), _f32(rz), len(rx), out)
+    return out
+
+
+def _shot_arrays(shots, nxx):
+    sx = _f32([s[0] for s in shots])
+    sz = _f32([s[1] for s in shots])
+    c0 = np.array([int(s[2]) if len(s) > 2 else 0 for s in shots], np.int32)
+    nc = np.array([int(s[3]) if len(s) > 3 and s[3] > 0 else nxx - int(c0[k]) for k, s in enumerate(shots)],
+                  np.int32)
+    return sx, sz, c0, nc
+
+
+def misfit_f64(S, dx, dz, shots, rx, rz, t_obs, nb=3):
+    """FP64 misfit 0.5 sum (p - t_obs)^2 of the FP64 1-pass solves (own branches)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    sx, sz, c0, nc = _shot_arrays(shots, nxx)
+    tobs = np.ascontiguousarray(np.asarray(t_obs, np.float64).reshape(len(shots), len(rx)))
+    return lib().orc_misfit_f64(nzz, nxx, nb, S, dx, dz, len(shots), sx, sz, c0, nc, _f32(rx), _f32(rz),
+                                len(rx), tobs)
+
+
+def fd_misfit_f64(S, dx, dz, shots, rx, rz, t_obs, cells, rel=1e-5, nb=3, nthreads=0):
+    """Central finite differences of misfit_f64 on padded cells [(i, j), ...]
+    (row i, column j): returns (dJ/dS per cell, (J+ - J-) values, threads)."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    sx, sz, c0, nc = _shot_arrays(shots, nxx)
+    tobs = np.ascontiguousarray(np.asarray(t_obs, np.float64).reshape(len(shots), len(rx)))
+    ci = np.ascontiguousarray([c[0] for c in cells], np.int32)
+    cj = np.ascontiguousarray([c[1] for c in cells], np.int32)
+    n = len(cells)
+    sp, sm = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    jp, jm = np.zeros(n), np.zeros(n)
+    used = lib().orc_fd_misfit_f64(nzz, nxx, nb, S, dx, dz, len(shots), sx, sz, c0, nc, _f32(rx), _f32(rz),
+                                   len(rx), tobs, n, ci, cj, rel, sp, sm, jp, jm, nthreads)
+    d = (jp - jm) / (sp.astype(np.float64) - sm.astype(np.float64))
+    return d, jp - jm, used

@@ -22,6 +22,7 @@ SF_LAYOUT_MODEL = 0
 SF_LAYOUT_PADDED = 1
 SF_ARITH_REFERENCE = 0
 SF_ARITH_IEEE = 1
+SF_ARITH_COMPENSATED = 2
 SF_KEEP_TAPE = 1
 SF_KEEP_TABLES = 2
 
@@ -51,6 +52,7 @@ SIGNATURES = {
                                    C.c_int, C.c_int, VP]),
     "sf_batch_table": (C.c_int, [VP, C.c_int, VP, C.c_int, VP]),
     "sf_batch_adjoint": (C.c_int, [VP, VP, C.c_int, VP, C.c_int, VP]),
+    "sf_batch_tape_codes": (C.c_int, [VP, C.c_int, VP, C.c_int, VP]),
     "sf_batch_misfit_gradient": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_double), VP, C.c_int, VP]),
     "sf_batch_stiffness_gradient": (C.c_int, [VP, VP, VP, C.c_int, VP]),
     "sf_synchronize": (C.c_int, [VP, VP]),

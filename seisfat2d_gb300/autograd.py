@@ -5,7 +5,9 @@ S is the padded slowness (nxx, nzz) on the engine's device. Forward runs one
 taped batched forward through the C ABI; backward runs the adjoint-state
 reverse sweeps (sf_batch_adjoint) with the incoming pick gradients and
 returns dJ/dS on the padded grid. Each forward supports one backward (the
-tape is consumed).
+tape is consumed), and only while the engine still holds that forward's tape:
+a later forward, plan iteration or adjoint on the same engine replaces it,
+and backward then raises instead of differentiating another batch.
 """
 import torch
 
@@ -22,12 +24,17 @@ class EikonalPicks(torch.autograd.Function):
                              stream=torch.cuda.current_stream(S.device))
         engine.synchronize(torch.cuda.current_stream(S.device))
         ctx.engine = engine
+        ctx.generation = engine.tape_generation
         ctx.shape = S.shape
         ctx.device = S.device
         return picks
 
     @staticmethod
     def backward(ctx, grad_picks):
+        if ctx.engine.tape_generation != ctx.generation:
+            raise RuntimeError("EikonalPicks.backward: the engine's tape belongs to a later call; run each "
+                               "forward's backward before the next forward on the same engine, or use one "
+                               "engine per forward")
         g = torch.empty(ctx.shape, dtype=torch.float32, device=ctx.device)
         stream = torch.cuda.current_stream(ctx.device)
         ctx.engine.batch_adjoint(grad_picks.detach().contiguous().float(), out=g, stream=stream)

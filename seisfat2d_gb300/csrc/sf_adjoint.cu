@@ -297,6 +297,10 @@ int sf_adj_enqueue(sf_ctx* c, AdjLaunch& A, const float* d_pg, float* d_grad, un
     A.p.epoch = epoch;
     A.g.grad = d_grad;
     CK(cudaMemsetAsync(A.p.bar, 0, A.nctr * sizeof(unsigned), st));
+    if (c->hand_stale_a) {  // the epoch wrapped (sf_next_epoch)
+        CK(cudaMemsetAsync(c->d_hand2, 0, c->cap_hand2, st));
+        c->hand_stale_a = false;
+    }
     c->last_fused = A.fused;
     if (A.fused) {
         // one launch: the gather's tiles start as the last reverse sweep finishes them

@@ -23,6 +23,7 @@ struct Consts {
     float D;           // dz2i + dx2i
     float K;           // dz2i * dx2i
     float kA;          // dz2i - dx2i      (tape coefficient)
+    float kB;          // dx2i - dz2i      (compensated 2D increment)
     float k2K;         // 2 * (dz2i*dx2i)  (tape coefficient)
     // correctly rounded reciprocals of the four divisors and, per divisor, whether
     // Markstein's correction step has been verified to equal IEEE division for
@@ -171,6 +172,128 @@ __device__ __forceinline__ float node_update(float told, float tv, float te, flo
         }
     }
     return tnew;
+}
+
+// Compensated update (SF_ARITH_COMPENSATED; no counterpart in the
+// reference). Traveltimes are unevaluated sums hi + lo of two FP32 values.
+// Every decision and increment of the update depends only on differences of
+// the upwind times, so these are formed from the pairs, (a.h - b.h) + (a.l -
+// b.l), and the candidates are compared in FP32 next to a nearby finite time
+// (the two 1D ones next to te, the 1D and the 2D or edge winner next to tev,
+// the winner and the old value next to the winner's base), never next to
+// the 1e6 sentinel; the winner is its base time plus its FP32 increment,
+// added with Knuth's TwoSum and renormalised with Dekker's Fast2Sum. A node's rounding error is then
+// relative to its increment instead of its time and does not accumulate
+// along the sweep. Same candidates, branch tests, tape codes and coefficient
+// formulas as node_update; each operation rounded once, in the order of the
+// oracle's restatement (updc in oracle/eikonal_oracle.c).
+__device__ __forceinline__ void ff_add(float ah, float al, float b, float& h, float& l)
+{
+    const float s = fadd(ah, b), bb = fsub(s, ah);
+    const float e = fadd(fsub(ah, fsub(s, bb)), fsub(b, bb));
+    const float t = fadd(e, al);
+    h = fadd(s, t);
+    l = fsub(t, fsub(h, s));
+}
+__device__ __forceinline__ float ff_diff(float ah, float al, float bh, float bl)
+{
+    return fadd(fsub(ah, bh), fsub(al, bl));
+}
+
+template <bool TAPE, bool EXACT = false, bool SQ = false>
+__device__ __forceinline__ void node_update_comp(float toh, float tol, float tvh, float tvl, float teh, float tel,
+                                                 float tevh, float tevl, float s1a, float s1b, float s2a, float s2b,
+                                                 float sref, const Consts& k, int dr1, int dc1a, int dc2, int dr2a,
+                                                 float& oh, float& ol, Rec& rec, bool& bad)
+{
+    const float dte = ff_diff(teh, tel, tevh, tevl);
+    const float dtv = ff_diff(tvh, tvl, tevh, tevl);
+    const float dvt = ff_diff(tvh, tvl, teh, tel);
+    const float m1 = fminf(s1a, s1b), m2 = fminf(s2a, s2b);
+    const float i1 = fmul(k.dz, m1), i2 = fmul(k.dx, m2);  // t1d1 = tv + i1, t1d2 = te + i2
+    const bool w11 = fadd(dvt, i1) <= i2;                  // t1d1 <= t1d2, compared next to te
+    const float o1D = w11 ? fadd(dtv, i1) : fadd(dte, i2); // the 1D winner's offset to tev
+    const float dxs = fmul(k.dx, sref);
+    const float dzs = SQ ? dxs : fmul(k.dz, sref);
+    const bool c2d = (dvt <= dxs) && (-dvt <= dzs) && (dte >= 0.0f) && (dtv >= 0.0f);
+    const float thz = fdiv_k<EXACT>(fmul(fmul(sref, k.dz), k.dz), k.hyp, k.rhyp, k.mflags & 4, bad);
+    const float thx = SQ ? thz : fdiv_k<EXACT>(fmul(fmul(sref, k.dx), k.dx), k.hyp, k.rhyp, k.mflags & 4, bad);
+    const bool c2 = !c2d && (dte <= thz) && (dte > 0.0f);        // t2: from te, step dz
+    const bool c3 = !c2d && !c2 && (dtv <= thx) && (dtv > 0.0f);  // t3: from tv, step dx
+    const bool ce = c2 || c3;
+    // one root for the 2D and the edge candidates (operands selected per lane)
+    const float hq = SQ ? k.dz : (c2 ? k.dz : k.dx);
+    const float rq = SQ ? k.rdz : (c2 ? k.rdz : k.rdx);
+    const bool vq = SQ ? (k.mflags & 2) : (c2 ? (k.mflags & 2) : (k.mflags & 1));
+    const float hx = SQ ? k.dz : (c2 ? k.dx : k.dz);
+    const float dq = c2 ? dte : dtv;
+    const float qe = fdiv_k<EXACT>(ce ? dq : hq, hq, rq, vq, bad);
+    const float dd = fmul(-2.0f, dvt);  // ta - tb = 2 (te - tv)
+    const float disc = fsub(fmul(fmul(fmul(4.0f, sref), sref), k.D), fmul(fmul(k.K, dd), dd));
+    const float earg = fsub(fmul(sref, sref), fmul(qe, qe));
+    const float root = fsqrt(c2d ? disc : (ce ? earg : 1.0f));
+    const float o3v = fdiv_k<EXACT>(c2d ? fsub(root, fmul(dvt, k.kB)) : k.D, k.D, k.rD, k.mflags & 8, bad);
+    const float inc = ce ? fmul(hx, root) : 0.0f;
+    const float o3 = c2d ? o3v : kBig;
+    const float oq = fadd(dq, inc);
+    const float o4 = c2 ? oq : kBig;
+    const float o5 = c3 ? oq : kBig;
+    // a 2D or edge candidate needs tev close to its base, so both winners'
+    // offsets to tev are exact enough to compare
+    const float o2D = fminf(o3, fminf(o4, o5));
+    const int br = c2d ? 3 : (c2 ? 4 : (c3 ? 5 : 0));
+    // the winner's base and increment
+    const bool w1 = o1D <= o2D;
+    float bh, bl, bi;
+    if (w1) {
+        bh = w11 ? tvh : teh;
+        bl = w11 ? tvl : tel;
+        bi = w11 ? i1 : i2;
+    } else {
+        bh = (br == 3) ? tevh : (br == 4 ? teh : tvh);
+        bl = (br == 3) ? tevl : (br == 4 ? tel : tvl);
+        bi = (br == 3) ? o3v : inc;
+    }
+    // the candidate replaces told when it is smaller, compared next to its base
+    const bool upd = bi < ff_diff(toh, tol, bh, bl);
+    float nh, nl;
+    ff_add(bh, bl, bi, nh, nl);
+    oh = upd ? nh : toh;
+    ol = upd ? nl : tol;
+    if (TAPE) {
+        rec.code = 0;
+        rec.c1 = 0.0f;
+        rec.c2 = 0.0f;
+        if (upd) {
+            if (w1) {
+                if (w11) {
+                    int dc = (s1a <= s1b) ? dc1a : 1;
+                    rec.code = (uint8_t)(1 | (dr1 << 3) | (dc << 4));
+                    rec.c2 = k.dz;
+                } else {
+                    int dr = (s2a <= s2b) ? dr2a : 1;
+                    rec.code = (uint8_t)(2 | (dr << 3) | (dc2 << 4));
+                    rec.c2 = k.dx;
+                }
+            } else if (br != 0) {
+                rec.code = (uint8_t)(br | (dr1 << 3) | (dc2 << 4));
+                if (br == 3) {
+                    if (root > 0.0f) {
+                        rec.c1 = fdiv_k<EXACT>(fadd(k.kA, fdiv(fmul(k.k2K, dd), root)), k.D, k.rD, k.mflags & 8, bad);
+                        rec.c2 = fdiv(fmul(4.0f, sref), root);
+                    } else {
+                        rec.c1 = fdiv_k<EXACT>(k.kA, k.D, k.rD, k.mflags & 8, bad);
+                    }
+                } else {
+                    const float hq2 = SQ ? k.dz : ((br == 4) ? k.dz : k.dx);
+                    if (root > 0.0f) {
+                        rec.c1 = fdiv(fmul(hx, qe), fmul(hq2, root));
+                        rec.c2 = fdiv(fmul(hx, sref), root);
+                    }
+                }
+            }
+        }
+    }
 }
 
 // Near-source value of node (zi, xi) in the reference build's FP32

@@ -76,6 +76,9 @@ int sf_dev_reserve_zero(sf_ctx* c, void** p, size_t* cap, size_t bytes)
 
 unsigned sf_next_epoch(sf_ctx* c)
 {
+    // after a wrap an epoch's tags could meet pairs an earlier cycle left in
+    // the handoff buffers: the next forward and adjoint launches clear them
+    if (c->epoch == (1u << 22) - 1) c->hand_stale_f = c->hand_stale_a = true;
     c->epoch = (c->epoch % ((1u << 22) - 1)) + 1;
     return c->epoch;
 }
@@ -131,9 +134,9 @@ __global__ void k_picks(const float* __restrict__ T, int nzz, int ncols, int c0,
 
 }  // namespace
 
-size_t sf_fwd_smem_bytes(int warps)
+size_t sf_fwd_smem_bytes(int warps, bool comp)
 {
-    return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * sizeof(WarpRing);
+    return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * (comp ? sizeof(WarpRingC) : sizeof(WarpRing));
 }
 
 // ------------------------------------------------------------------ context
@@ -163,6 +166,7 @@ extern "C" int sf_ctx_create(sf_ctx** out, int nx, int nz, float dx, float dz, i
     k.D = k.dz2i + k.dx2i;
     k.K = k.dz2i * k.dx2i;
     k.kA = k.dz2i - k.dx2i;
+    k.kB = k.dx2i - k.dz2i;
     k.k2K = 2.0f * k.K;
     int st = sf_cuda_check(c, cudaSetDevice(device), "cudaSetDevice");
     if (st == SF_OK) {
@@ -194,7 +198,7 @@ extern "C" int sf_ctx_destroy(sf_ctx* c)
     void* bufs[] = {c->d_S, c->d_flags, c->d_shots, c->d_T, c->d_rx, c->d_rz, c->d_picks, c->d_Sq,
                     c->d_tcode, c->d_tc1, c->d_tc2, c->d_model, c->d_cij_all, c->d_hand, c->d_ctr,
                     c->d_skern, c->d_upd, c->d_wav, c->d_mig, c->d_kgeo, c->d_kint, c->d_kpart,
-                    c->d_vfac, c->d_gcij, c->d_fuse};
+                    c->d_vfac, c->d_gcij, c->d_fuse, c->d_Tl};
     for (void* b : bufs)
         if (b) cudaFree(b);
     delete c;
@@ -224,7 +228,8 @@ extern "C" int sf_set_launch(sf_ctx* c, int warps, int gang_warps)
 extern "C" int sf_set_arithmetic(sf_ctx* c, int mode)
 {
     if (!c) return SF_ERR_ARG;
-    if (mode != SF_ARITH_REFERENCE && mode != SF_ARITH_IEEE) return sf_fail(c, SF_ERR_ARG, "unknown arithmetic");
+    if (mode != SF_ARITH_REFERENCE && mode != SF_ARITH_IEEE && mode != SF_ARITH_COMPENSATED)
+        return sf_fail(c, SF_ERR_ARG, "unknown arithmetic");
     c->arith = mode;
     c->plan_dirty = true;
     return SF_OK;
@@ -319,35 +324,47 @@ int sf_verify_divisors(sf_ctx* c)
 
 namespace sf {
 // accessors of the k_shots instantiations: tape, reference arithmetic,
-// anisotropic taped (VTI), interior-block body
-const void* sf_kshots_0000();
-const void* sf_kshots_0001();
-const void* sf_kshots_0100();
-const void* sf_kshots_0101();
-const void* sf_kshots_1000();
-const void* sf_kshots_1001();
-const void* sf_kshots_1100();
-const void* sf_kshots_1101();
-const void* sf_kshots_1010();
-const void* sf_kshots_1110();
+// anisotropic taped (VTI), interior-block body, compensated arithmetic
+const void* sf_kshots_00000();
+const void* sf_kshots_00010();
+const void* sf_kshots_01000();
+const void* sf_kshots_01010();
+const void* sf_kshots_10000();
+const void* sf_kshots_10010();
+const void* sf_kshots_11000();
+const void* sf_kshots_11010();
+const void* sf_kshots_10100();
+const void* sf_kshots_11100();
+const void* sf_kshots_00001();
+const void* sf_kshots_00011();
+const void* sf_kshots_10001();
+const void* sf_kshots_10011();
+const void* sf_kshots_10101();
 }  // namespace sf
 
-// Anisotropic taped batches run the general loops only.
-const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior)
+// Anisotropic taped batches run the general loops only; the compensated
+// arithmetic has no reference-build variant.
+const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior, bool comp)
 {
     vti = vti && tape;
     if (vti) interior = false;
-    switch (((int)tape << 3) | ((int)ref << 2) | ((int)vti << 1) | (int)interior) {
-    case 0x0: return sf::sf_kshots_0000();
-    case 0x1: return sf::sf_kshots_0001();
-    case 0x4: return sf::sf_kshots_0100();
-    case 0x5: return sf::sf_kshots_0101();
-    case 0x8: return sf::sf_kshots_1000();
-    case 0x9: return sf::sf_kshots_1001();
-    case 0xc: return sf::sf_kshots_1100();
-    case 0xd: return sf::sf_kshots_1101();
-    case 0xa: return sf::sf_kshots_1010();
-    case 0xe: return sf::sf_kshots_1110();
+    if (comp) ref = false;
+    switch (((int)tape << 4) | ((int)ref << 3) | ((int)vti << 2) | ((int)interior << 1) | (int)comp) {
+    case 0x00: return sf::sf_kshots_00000();
+    case 0x02: return sf::sf_kshots_00010();
+    case 0x08: return sf::sf_kshots_01000();
+    case 0x0a: return sf::sf_kshots_01010();
+    case 0x10: return sf::sf_kshots_10000();
+    case 0x12: return sf::sf_kshots_10010();
+    case 0x18: return sf::sf_kshots_11000();
+    case 0x1a: return sf::sf_kshots_11010();
+    case 0x14: return sf::sf_kshots_10100();
+    case 0x1c: return sf::sf_kshots_11100();
+    case 0x01: return sf::sf_kshots_00001();
+    case 0x03: return sf::sf_kshots_00011();
+    case 0x11: return sf::sf_kshots_10001();
+    case 0x13: return sf::sf_kshots_10011();
+    case 0x15: return sf::sf_kshots_10101();
     default: return nullptr;
     }
 }
@@ -375,9 +392,10 @@ bool sf_interior_loops(sf_ctx* c, const void* kernel, size_t smem, int G)
 
 int sf_fwd_setup(sf_ctx* c)
 {
-    size_t mx = sf_fwd_smem_bytes(kMaxWarps);
-    for (int k = 0; k < 16; k++) {
-        const void* f = sf_kshots_kernel(k & 8, k & 4, k & 2, k & 1);
+    for (int k = 0; k < 32; k++) {
+        const bool comp = k & 1;
+        const size_t mx = comp ? sf_fwd_smem_bytes(kMaxWarpsComp, true) : sf_fwd_smem_bytes(kMaxWarps, false);
+        const void* f = sf_kshots_kernel(k & 16, k & 8, k & 4, k & 2, comp);
         if (f) CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
     }
     return sf_adj_setup(c);
@@ -591,10 +609,13 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     const int nshots = (int)c->hshots.size();
     const size_t nzz = c->nzz;
     const int nstrips = (c->nzz + 31) / 32;
-    const size_t smem = sf_fwd_smem_bytes(c->warps);
+    const bool comp = c->arith == SF_ARITH_COMPENSATED;
+    if (comp && c->warps > kMaxWarpsComp)
+        return sf_fail(c, SF_ERR_ARG, "the compensated arithmetic runs at most 8 warps per CTA (sf_set_launch)");
+    const size_t smem = sf_fwd_smem_bytes(c->warps, comp);
     const bool ref = c->arith == SF_ARITH_REFERENCE;
     const bool vti = tape && ani;
-    const void* kern = sf_kshots_kernel(tape, ref, vti, false);
+    const void* kern = sf_kshots_kernel(tape, ref, vti, false, comp);
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
     if (rc) return rc;
@@ -603,7 +624,7 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     // kernel that runs (every CTA of a gang resident at once)
     c->batch_interior = !vti && !(tape && c->warps > kMaxWarpsTapedInterior) && sf_interior_loops(c, kern, smem, G);
     if (c->batch_interior) {
-        const void* ik = sf_kshots_kernel(tape, ref, vti, true);
+        const void* ik = sf_kshots_kernel(tape, ref, vti, true, comp);
         int Gi, NGi;
         rc = sf_gang_shape(c, ik, smem, nshots, nstrips, gang_warps, &Gi, &NGi);
         if (rc) return rc;
@@ -626,12 +647,17 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     const size_t tfloats = keep_tables ? (size_t)c->batch_T_floats : (size_t)NG * t_per_gang;
     rc = sf_dev_reserve(c, (void**)&c->d_T, &c->cap_T, tfloats * sizeof(float));
     if (rc) return rc;
+    if (comp) {
+        rc = sf_dev_reserve(c, (void**)&c->d_Tl, &c->cap_Tl, tfloats * sizeof(float));
+        if (rc) return rc;
+    }
     if (ani) {
         rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)NG * nzz * c->batch_maxcols * sizeof(float));
         if (rc) return rc;
     }
-    rc = sf_dev_reserve_zero(c, (void**)&c->d_hand, &c->cap_hand,
-                             (size_t)NG * 4 * nstrips * c->batch_maxcols * sizeof(unsigned long long));
+    const size_t hand_bytes =
+        (size_t)NG * 4 * nstrips * c->batch_maxcols * sizeof(unsigned long long) * (comp ? 2 : 1);
+    rc = sf_dev_reserve_zero(c, (void**)&c->d_hand, &c->cap_hand, hand_bytes);
     if (rc) return rc;
     const size_t nctr = (size_t)NG;
     rc = sf_dev_reserve(c, (void**)&c->d_ctr, &c->cap_ctr, nctr * sizeof(unsigned));
@@ -657,6 +683,7 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     p.NG = NG;
     p.maxcols = c->batch_maxcols;
     p.Tpool = c->d_T;
+    p.Tlpool = comp ? c->d_Tl : nullptr;
     p.t_per_gang = t_per_gang;
     p.err = c->d_flags + 1;          // flags[1]: error flag
     p.hand = c->d_hand;
@@ -686,7 +713,7 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     L->block = dim3(c->warps * 32);
     L->smem = smem;
     L->nctr = nctr;
-    L->hand_bytes = (size_t)NG * 4 * nstrips * c->batch_maxcols * sizeof(unsigned long long);
+    L->hand_bytes = hand_bytes;
     return SF_OK;
 }
 
@@ -710,6 +737,10 @@ int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cuda
     L.p.picks = d_picks;
     L.p.epoch = epoch;
     CK(cudaMemsetAsync(L.p.bar, 0, L.nctr * sizeof(unsigned), st));
+    if (c->hand_stale_f) {
+        CK(cudaMemsetAsync(c->d_hand, 0, c->cap_hand, st));
+        c->hand_stale_f = false;
+    }
     int rc = sf_kt_begin(c, SF_KT_FORWARD, st);
     if (rc) return rc;
     void* args[] = {&L.p};
@@ -814,6 +845,44 @@ extern "C" int sf_batch_table(sf_ctx* c, int shot, float* T, int mem, void* stre
     CK(cudaMemcpyAsync(T, c->d_T + d.t_off, sizeof(float) * (size_t)c->nzz * d.ncols,
                        mem == SF_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
     if (mem == SF_MEM_HOST) return sf_check_flags(c, st);
+    return SF_OK;
+}
+
+// The tape is kept per (sweep, strip) in the strip's skewed step order: entry
+// [step * 32 + lane] is the node of row 32k + lane (rows downward, sweeps 0
+// and 2) or 32k + 31 - lane (upward, sweeps 1 and 3) and window column of
+// march step - lane (columns rightward, sweeps 0 and 1, else leftward).
+// This entry point unskews one shot's codes into [sweep][column][row].
+extern "C" int sf_batch_tape_codes(sf_ctx* c, int shot, uint8_t* codes, int mem, void* stream)
+{
+    if (!c || !codes) return SF_ERR_ARG;
+    if (!c->tape_valid) return sf_fail(c, SF_ERR_STATE, "last batch did not keep a tape");
+    if (shot < 0 || shot >= (int)c->hshots.size()) return sf_fail(c, SF_ERR_ARG, "shot out of range");
+    CK(cudaSetDevice(c->dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const ShotDev& d = c->hshots[c->tables_index[shot]];
+    const int nzz = c->nzz, ncols = d.ncols, nstrips = (nzz + 31) / 32;
+    const size_t per_strip = (size_t)(ncols + 31) * 32;
+    std::vector<uint8_t> raw(4 * (size_t)nstrips * per_strip), out(4 * (size_t)ncols * nzz, 0);
+    CK(cudaMemcpyAsync(raw.data(), c->d_tcode + d.tape_off, raw.size(), cudaMemcpyDeviceToHost, st));
+    int rc = sf_check_flags(c, st);
+    if (rc) return rc;
+    for (int sw = 0; sw < 4; sw++) {
+        const bool zdown = (sw == 0 || sw == 2), xright = (sw == 0 || sw == 1);
+        for (int k = 0; k < nstrips; k++) {
+            const uint8_t* blk = raw.data() + ((size_t)sw * nstrips + k) * per_strip;
+            for (int step = 0; step < ncols + 31; step++)
+                for (int lane = 0; lane < 32; lane++) {
+                    const int r = zdown ? 32 * k + lane : 32 * k + 31 - lane, m = step - lane;
+                    if (r >= nzz || m < 0 || m >= ncols) continue;
+                    const int j = xright ? m : ncols - 1 - m;
+                    out[((size_t)sw * ncols + j) * nzz + r] = blk[(size_t)step * 32 + lane];
+                }
+        }
+    }
+    CK(cudaMemcpyAsync(codes, out.data(), out.size(),
+                       mem == SF_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost, st));
+    CK(cudaStreamSynchronize(st));
     return SF_OK;
 }
 

@@ -80,6 +80,7 @@ struct sf_ctx {
 
     sf::ShotDev* d_shots = nullptr; size_t cap_shots = 0;
     float* d_T = nullptr; size_t cap_T = 0;
+    float* d_Tl = nullptr; size_t cap_Tl = 0;  // lo parts of the traveltimes (compensated arithmetic)
     float* d_rx = nullptr; size_t cap_rx = 0;
     float* d_rz = nullptr; size_t cap_rz = 0;
     float* d_picks = nullptr; size_t cap_picks = 0;
@@ -87,6 +88,7 @@ struct sf_ctx {
     unsigned long long* d_hand = nullptr; size_t cap_hand = 0;
     unsigned* d_ctr = nullptr; size_t cap_ctr = 0;
     unsigned epoch = 0;  // launches so far (handoff tags)
+    bool hand_stale_f = false, hand_stale_a = false;  // the epoch wrapped: clear the handoff buffers
     int last_G = 1, last_NG = 1;
     uint8_t* d_tcode = nullptr; size_t cap_tcode = 0;
     float* d_tc1 = nullptr; size_t cap_tc1 = 0;
@@ -163,9 +165,9 @@ unsigned sf_next_epoch(sf_ctx* c);
 int sf_check_flags(sf_ctx* c, cudaStream_t st);
 int sf_fwd_setup(sf_ctx* c);
 int sf_verify_divisors(sf_ctx* c);
-size_t sf_fwd_smem_bytes(int warps);
+size_t sf_fwd_smem_bytes(int warps, bool comp);
 // k_shots instantiation (one object file each, sf_shots_inst.cu)
-const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior);
+const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior, bool comp);
 // whether the batch of hshots, G CTAs per shot, runs the interior-block body
 bool sf_interior_loops(sf_ctx* c, const void* kernel, size_t smem, int G);
 void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4]);

@@ -31,9 +31,10 @@ struct FwdParams {
     int NG;               // gangs; gang k solves shots k, k+NG, ...
     int maxcols;          // widest window of the batch
     float* Tpool;
+    float* Tlpool;        // compensated: lo parts of the traveltimes, same layout as Tpool
     long long t_per_gang; // > 0: each gang reuses Tpool + gang * t_per_gang
     int* err;
-    unsigned long long* hand;  // tagged strip handoff pairs: per gang [4 sweeps][nstrips][maxcols]
+    unsigned long long* hand;  // tagged strip handoff pairs: per gang [4 sweeps][nstrips][maxcols] (x2 compensated)
     unsigned* bar;        // per gang barrier counter
     unsigned epoch;       // launch number (tags: epoch << 10 | shot-solve number)
     // anisotropy
@@ -102,18 +103,21 @@ __device__ __forceinline__ GangPos gang_pos(int G)
 // runs the strips of its slot. No barrier between sweeps: consecutive sweeps
 // run the rows in opposite directions, a warp rereads only rows it wrote
 // itself, and the handoff chain orders everything else. Square cells (dx and
-// dz equal) run the strip loops' square-cell form.
-template <bool TAPE, bool REF, bool INTERIOR>
+// dz equal) run the strip loops' square-cell form. COMP: compensated
+// arithmetic, lo parts in Tl, two handoff pairs per column.
+template <bool TAPE, bool REF, bool INTERIOR, bool COMP>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPos& gp, const float* Sw,
-                             int ldS, float* T, unsigned tag, CtaShared* cs, WarpRing* rings)
+                             int ldS, float* T, float* Tl, unsigned tag, CtaShared* cs, unsigned char* rings)
 {
     const int nzz = p.nzz, ncols = sh.ncols;
     const int nstrips = (nzz + 31) >> 5;
-    unsigned long long* hb = p.hand + (size_t)gp.gang * 4 * nstrips * p.maxcols;
+    constexpr size_t HS = COMP ? 2 : 1;
+    unsigned long long* hb = p.hand + (size_t)gp.gang * 4 * nstrips * p.maxcols * HS;
     StripArgs a;
     a.S = Sw;
     a.ldS = ldS;
     a.T = T;
+    a.Tl = Tl;
     a.nzz = nzz;
     a.ncols = ncols;
     a.nstrips = nstrips;
@@ -121,7 +125,7 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
     a.sIdx = sh.sIdx - sh.c0;
     a.kc = p.kc;
     a.init = cs->init;
-    a.ring = rings + gp.warp;
+    a.ring = rings + (size_t)gp.warp * ring_bytes<COMP>();
     a.sh = cs;
     a.err = p.err;
     a.tcode = nullptr;
@@ -133,13 +137,13 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
         const bool szpos = !(sw == 1 || sw == 3);
         a.skip_i = sh.skip_i[sw];
         a.skip_j = sh.skip_j[sw];
-        unsigned long long* hs = hb + (size_t)sw * nstrips * p.maxcols;
+        unsigned long long* hs = hb + (size_t)sw * nstrips * p.maxcols * HS;
         const int first = szpos ? gp.slot : ((nstrips - 1 - gp.slot) % gp.slots + gp.slots) % gp.slots;
 #pragma unroll 1
         for (int pidx = first; pidx < nstrips; pidx += gp.slots) {
             a.k = szpos ? pidx : nstrips - 1 - pidx;
-            a.h_in = (pidx > 0) ? hs + (size_t)pidx * p.maxcols : nullptr;
-            a.h_out = (pidx < nstrips - 1) ? hs + (size_t)(pidx + 1) * p.maxcols : nullptr;
+            a.h_in = (pidx > 0) ? hs + (size_t)pidx * p.maxcols * HS : nullptr;
+            a.h_out = (pidx < nstrips - 1) ? hs + (size_t)(pidx + 1) * p.maxcols * HS : nullptr;
             if (TAPE) {
                 size_t base = tape_strip_base(sh.tape_off, sw, a.k, nstrips, ncols);
                 a.tcode = p.tcode + base;
@@ -148,17 +152,17 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
             }
             if (p.kc.dx == p.kc.dz) {
                 switch (sw) {
-                case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR, true>(a); break;
-                case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR, true>(a); break;
-                case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR, true>(a); break;
-                default: run_strip<-1, -1, false, TAPE, REF, INTERIOR, true>(a); break;
+                case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR, true, COMP>(a); break;
+                case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR, true, COMP>(a); break;
+                case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR, true, COMP>(a); break;
+                default: run_strip<-1, -1, false, TAPE, REF, INTERIOR, true, COMP>(a); break;
                 }
             } else {
                 switch (sw) {
-                case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR, false>(a); break;
-                case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR, false>(a); break;
-                case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR, false>(a); break;
-                default: run_strip<-1, -1, false, TAPE, REF, INTERIOR, false>(a); break;
+                case 0: run_strip<1, 1, true, TAPE, REF, INTERIOR, false, COMP>(a); break;
+                case 1: run_strip<-1, 1, false, TAPE, REF, INTERIOR, false, COMP>(a); break;
+                case 2: run_strip<1, -1, false, TAPE, REF, INTERIOR, false, COMP>(a); break;
+                default: run_strip<-1, -1, false, TAPE, REF, INTERIOR, false, COMP>(a); break;
                 }
             }
         }
@@ -170,15 +174,18 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
 // hold at once, so every gang's CTAs are resident together. VTI (with TAPE):
 // anisotropic shots whose second (qP) solve is taped, with the qP pass
 // writing its derivative factors. INTERIOR: the strip loops' bounds-test-free
-// body for interior blocks (see run_strip).
-template <bool TAPE, bool REF, bool VTI, bool INTERIOR>
+// body for interior blocks (see run_strip). COMP: compensated arithmetic
+// (node_update_comp; the 3x3 initial values are the FP64 ones rounded once).
+template <bool TAPE, bool REF, bool VTI, bool INTERIOR, bool COMP = false>
 // (kMaxWarps * 32, 1): with the block size alone as the bound ptxas caps the
 // kernel at 64 registers and spills the strip loop's state to local memory.
-__global__ void __launch_bounds__(((TAPE && INTERIOR) ? kMaxWarpsTapedInterior : kMaxWarps) * 32, 1) k_shots(FwdParams p)
+__global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? kMaxWarpsTapedInterior : kMaxWarps)) * 32, 1)
+    k_shots(FwdParams p)
 {
+    static_assert(!(COMP && REF), "the compensated arithmetic has no reference-build variant");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
-    WarpRing* rings = reinterpret_cast<WarpRing*>(smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15)));
+    unsigned char* rings = smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15));
     const int tid = threadIdx.x;
     const GangPos gp = gang_pos(p.G);
     const int nzz = p.nzz;
@@ -194,11 +201,13 @@ __global__ void __launch_bounds__(((TAPE && INTERIOR) ? kMaxWarpsTapedInterior :
         const ShotDev sh = p.shots[b];
         const int ncols = sh.ncols;
         float* T = (p.t_per_gang > 0) ? p.Tpool + (size_t)gp.gang * p.t_per_gang : p.Tpool + sh.t_off;
+        float* Tl = !COMP ? nullptr
+                          : (p.t_per_gang > 0) ? p.Tlpool + (size_t)gp.gang * p.t_per_gang : p.Tlpool + sh.t_off;
         const float* Sw = p.S + (size_t)sh.c0 * nzz;
         const unsigned tag = (p.epoch << 10) | (unsigned)((it * nsolves) & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE && !VTI, REF, INTERIOR>(p, sh, gp, Sw, nzz, T, tag, cs, rings);
+        solve_window<TAPE && !VTI, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings);
         // taped isotropic batches never set ani: their kernels carry no qP pass
         if ((!TAPE || VTI) && p.ani) {
             // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
@@ -251,7 +260,7 @@ __global__ void __launch_bounds__(((TAPE && INTERIOR) ? kMaxWarpsTapedInterior :
                         __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
             }
             __syncthreads();
-            solve_window<TAPE, REF, INTERIOR>(p, sh, gp, Sq, nzz, T, tag + 1u, cs, rings);
+            solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sq, nzz, T, Tl, tag + 1u, cs, rings);
         }
         // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {

@@ -53,8 +53,12 @@ struct FwdBlock {
     static_assert(LOOK % U == 0 && kRing % U == 0 && kRing >= 32 + LOOK + U, "ring too small");
 };
 constexpr int kSP = 36;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff pair at 34..35
+constexpr int kSPc = 40;    // compensated: S slot pitch, handoff pairs {hi,tag},{lo,tag} at 36..39
 constexpr int kTP = 32;     // T slot pitch
 constexpr int kMaxWarps = 16;
+// compensated kernels keep a second traveltime ring (the lo parts): at most
+// 8 warps per CTA fit in shared memory
+constexpr int kMaxWarpsComp = 8;
 // the taped interior-block forward kernels bound their CTAs to 8 warps, which
 // lets them keep more of the block's state in registers (measured 2.6%
 // faster on the headline batch; the other kernels measured slower that way)
@@ -66,6 +70,17 @@ struct WarpRing {
     float S[kRing * kSP];
     float T[kRing * kTP];
 };
+
+// Ring of the compensated strip loop: S with two handoff pairs per slot, the
+// hi and the lo parts of the traveltimes.
+struct WarpRingC {
+    float S[kRing * kSPc];
+    float T[kRing * kTP];
+    float L[kRing * kTP];
+};
+
+template <bool COMP>
+constexpr size_t ring_bytes() { return COMP ? sizeof(WarpRingC) : sizeof(WarpRing); }
 
 // Per-CTA shared state (static part), followed by the CTA's WarpRing blocks in
 // dynamic shared memory.
@@ -128,6 +143,7 @@ struct StripArgs {
     const float* S;   // slowness of the window, column stride ldS
     int ldS;
     float* T;         // traveltimes of the window, column stride nzz
+    float* Tl;        // compensated: their lo parts, same layout
     int nzz, ncols;
     int k;            // strip index: rows [32k, 32k+32)
     int nstrips;
@@ -135,7 +151,7 @@ struct StripArgs {
     int skip_i, skip_j;
     Consts kc;
     const float* init;  // 9 values in shared memory
-    WarpRing* ring;
+    unsigned char* ring;  // this warp's WarpRing (WarpRingC when compensated)
     CtaShared* sh;
     const unsigned long long* h_in;  // {value, tag} of the upwind strip's row by march column (nullptr: first strip)
     unsigned long long* h_out;       // pairs this strip feeds to the next one (nullptr: last strip)
@@ -200,8 +216,10 @@ __device__ __forceinline__ unsigned wait_counter(const unsigned* p, unsigned tar
 // INTERIOR: blocks whose marches all lie inside the window run a body without
 // bounds tests (fewer instructions per step, more code); otherwise every block
 // runs the general body. SQ: square cells (node_update). All forms give the
-// same bits.
-template <int SZ, int SX, bool SW0, bool TAPE, bool REF, bool INTERIOR, bool SQ>
+// same bits. COMP: compensated arithmetic (node_update_comp): every
+// traveltime the loop carries, stages, hands on and writes back is a pair
+// (hi, lo); the second handoff pair of a column carries lo.
+template <int SZ, int SX, bool SW0, bool TAPE, bool REF, bool INTERIOR, bool SQ, bool COMP = false>
 __device__ __forceinline__ void run_strip(const StripArgs& a)
 {
     constexpr int kU = FwdBlock<TAPE>::U, kLook = FwdBlock<TAPE>::LOOK, kAhead = FwdBlock<TAPE>::AHEAD;
@@ -217,8 +235,12 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     const int dc2 = (SX > 0) ? 0 : 1;
     const int dr2a = (r - 1 >= 1) ? 0 : 1;
 
-    float* Sring = a.ring->S;
-    float* Tring = a.ring->T;
+    constexpr int SP = COMP ? kSPc : kSP;    // S slot pitch
+    constexpr int PQ = COMP ? 36 : 34;       // first handoff pair in an S slot
+    float* Sring = COMP ? reinterpret_cast<WarpRingC*>(a.ring)->S : reinterpret_cast<WarpRing*>(a.ring)->S;
+    float* Tring = COMP ? reinterpret_cast<WarpRingC*>(a.ring)->T : reinterpret_cast<WarpRing*>(a.ring)->T;
+    float* Lring = COMP ? reinterpret_cast<WarpRingC*>(a.ring)->L : nullptr;
+    constexpr int HS = COMP ? 2 : 1;         // handoff pairs per column
 
     // global rows this lane stages
     const int ls_row = rb - 1 + lane;
@@ -239,25 +261,34 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
     const float* pS = Sg + (size_t)ls_row + (long long)col_of(0) * (long long)ldS;
     const float* pX = Sg + (size_t)(rb + 31) + (long long)col_of(0) * (long long)ldS;
     const float* pT = Tg + (size_t)(rb + lane) + (long long)col_of(0) * (long long)nzz;
+    const float* pTl = COMP ? a.Tl + (size_t)(rb + lane) + (long long)col_of(0) * (long long)nzz : nullptr;
     const long long dS = dcol * (long long)ldS, dT = dcol * (long long)nzz;
     // FAST: every march the call touches lies inside the window (no bounds tests)
     auto prefetch = [&](int q, int slot, auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
         if (FAST || q < ncols) {
-            if (ls_ok) cp_async4(&Sring[slot * kSP + lane], pS);
-            if (lx_ok) cp_async4(&Sring[slot * kSP + 32], pX);
-            if (!SW0 && lt_ok) cp_async4(&Tring[slot * kTP + lane], pT);
-            if (consumer) cp_async8(&Sring[slot * kSP + 34], a.h_in + q);  // upwind-row pair of march q
+            if (ls_ok) cp_async4(&Sring[slot * SP + lane], pS);
+            if (lx_ok) cp_async4(&Sring[slot * SP + 32], pX);
+            if (!SW0 && lt_ok) {
+                cp_async4(&Tring[slot * kTP + lane], pT);
+                if (COMP) cp_async4(&Lring[slot * kTP + lane], pTl);
+            }
+            // upwind-row pair(s) of march q
+            if (consumer) {
+                if (COMP) cp_async16(&Sring[slot * SP + PQ], a.h_in + 2 * q);
+                else cp_async8(&Sring[slot * SP + PQ], a.h_in + q);
+            }
         }
         cp_commit();
         pS += dS;
         pX += dS;
         pT += dT;
+        if (COMP) pTl += dT;
     };
 
     // let the previous strip get kAhead columns ahead before the first
     // prefetches of its values
-    if (consumer) wait_pair(a.h_in + min(kAhead, ncols - 1), a.tag, sh, a.err);
+    if (consumer) wait_pair(a.h_in + HS * min(kAhead, ncols - 1), a.tag, sh, a.err);
     __syncwarp();
 
     // prologue: march columns 0 .. kLook-1
@@ -266,11 +297,13 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
     // running destinations: write-back of march column s-31 (row r), tape entry s*32+lane
     float* pW = Tg + (size_t)r + (long long)col_of(0) * (long long)nzz;
+    float* pWl = COMP ? a.Tl + (size_t)r + (long long)col_of(0) * (long long)nzz : nullptr;
     uint8_t* pcode = TAPE ? a.tcode + lane : nullptr;
     float* pc1 = TAPE ? a.tc1 + lane : nullptr;
     float* pc2 = TAPE ? a.tc2 + lane : nullptr;
 
     float tn = 0.0f, tvp = 0.0f;                          // own last result, last upwind value
+    float tnl = 0.0f, tvpl = 0.0f;                        // their lo parts (compensated)
     float cU = 0.0f, cI = 0.0f;                           // carried S of rows r-1, r
     const int nsteps = ncols + 31;
     int b0 = 0;                                           // ring slot of march s0
@@ -294,8 +327,8 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
         int ml = b0 - lane;                               // slot of march s0 - lane
         if (ml < 0) ml += kRing;
         int msl[kU];
-        float nU[kU], nI[kU], told[kU];
-        unsigned long long pr[kU];
+        float nU[kU], nI[kU], told[kU], toldl[kU];
+        unsigned long long pr[kU], prl[kU];
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             int ms = ml + u;
@@ -303,10 +336,12 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             msl[u] = ms;
             // S of the new column: march m (SX>0) or m+1 (SX<0)
             const int ns = (SX > 0) ? ms : (ms + 1 == kRing ? 0 : ms + 1);
-            nU[u] = Sring[ns * kSP + tix];
-            nI[u] = Sring[ns * kSP + six];
+            nU[u] = Sring[ns * SP + tix];
+            nI[u] = Sring[ns * SP + six];
             told[u] = SW0 ? kBig : Tring[ms * kTP + tix];
-            pr[u] = consumer ? *reinterpret_cast<const unsigned long long*>(&Sring[ms * kSP + 34]) : 0ull;
+            toldl[u] = (COMP && !SW0) ? Lring[ms * kTP + tix] : 0.0f;
+            pr[u] = consumer ? *reinterpret_cast<const unsigned long long*>(&Sring[ms * SP + PQ]) : 0ull;
+            prl[u] = (COMP && consumer) ? *reinterpret_cast<const unsigned long long*>(&Sring[ms * SP + PQ + 2]) : 0ull;
         }
         if (consumer) {
             // a pair the previous strip had not written when it was prefetched:
@@ -314,14 +349,15 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 #pragma unroll
             for (int u = 0; u < kU; u++) {
                 const int s = s0 + u;
-                if ((FAST || s < ncols) && tag_of(pr[u]) != a.tag) {
-                    pr[u] = pack_tag(wait_pair(a.h_in + s, a.tag, sh, a.err), a.tag);
-                    wait_pair(a.h_in + min(s + kAhead, ncols - 1), a.tag, sh, a.err);
+                if ((FAST || s < ncols) && (tag_of(pr[u]) != a.tag || (COMP && tag_of(prl[u]) != a.tag))) {
+                    pr[u] = pack_tag(wait_pair(a.h_in + HS * s, a.tag, sh, a.err), a.tag);
+                    if (COMP) prl[u] = pack_tag(wait_pair(a.h_in + HS * s + 1, a.tag, sh, a.err), a.tag);
+                    wait_pair(a.h_in + HS * min(s + kAhead, ncols - 1), a.tag, sh, a.err);
                 }
             }
         }
 
-        float tnw[kU];
+        float tnw[kU], tnwl[kU];
         bool actv[kU];
         Rec rec[kU];
         // the block's kU node updates; EXACT divides with IEEE division
@@ -336,19 +372,27 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             const int j = col_of(m);
             // upwind value from the lane above (or the previous strip)
             float tv = __shfl_up_sync(0xffffffffu, tn, 1);
-            if (consumer && (FAST || s < ncols)) tv = val_of(pr[u]);
+            float tvl = COMP ? __shfl_up_sync(0xffffffffu, tnl, 1) : 0.0f;
+            if (consumer && (FAST || s < ncols)) {
+                tv = val_of(pr[u]);
+                if (COMP) tvl = val_of(prl[u]);
+            }
             const float te = tn, tev = tvp;
+            const float tel = tnl, tevl = tvpl;
 
-            float to = told[u];
+            float to = told[u], tol = toldl[u];
             if (SW0 && src_rows) {
                 const int da = r - a.sIdz + 1, db = j - a.sIdx + 1;
-                if (da >= 0 && da < 3 && db >= 0 && db < 3) to = a.init[da + 3 * db];
+                if (da >= 0 && da < 3 && db >= 0 && db < 3) {
+                    to = a.init[da + 3 * db];
+                    tol = 0.0f;
+                }
             }
             float U_j, I_j, U_jm, I_jm;
             if (SX > 0) { U_j = nU[u]; I_j = nI[u]; U_jm = cU; I_jm = cI; }
             else        { U_j = cU; I_j = cI; U_jm = nU[u]; I_jm = nI[u]; }
 
-            float tnew = to;
+            float tnew = to, tnewl = tol;
             rec[u].code = 0; rec[u].c1 = 0.0f; rec[u].c2 = 0.0f;
             const bool inner = act && irow && (FAST || ((j >= 1) && (j <= ncols - 2))) &&
                                !(r == a.skip_i && j == a.skip_j);
@@ -363,27 +407,39 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             const float sref = (SX > 0) ? Si1_jm : Si1_j;  // S[i1][j1]
             const int dc1a = (j - 1 >= 1) ? 0 : 1;
             bool bad_u = false;
-            if (inner)
-                tnew = node_update<TAPE, REF, EXACT, SQ>(to, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc,
-                                                         dr1, dc1a, dc2, dr2a, rec[u], bad_u);
+            if (inner) {
+                if constexpr (COMP)
+                    node_update_comp<TAPE, EXACT, SQ>(to, tol, tv, tvl, te, tel, tev, tevl, s1a, s1b, s2a, s2b, sref,
+                                                      a.kc, dr1, dc1a, dc2, dr2a, tnew, tnewl, rec[u], bad_u);
+                else
+                    tnew = node_update<TAPE, REF, EXACT, SQ>(to, tv, te, tev, s1a, s1b, s2a, s2b, sref, a.kc,
+                                                             dr1, dc1a, dc2, dr2a, rec[u], bad_u);
+            }
             bad |= bad_u;
             tnw[u] = tnew;
+            tnwl[u] = tnewl;
             actv[u] = act;
             // carry state
-            if (act) tn = tnew;
+            if (act) {
+                tn = tnew;
+                tnl = tnewl;
+            }
             tvp = tv;
+            tvpl = tvl;
             cU = nU[u];
             cI = nI[u];
         }
         return bad;
         };
         {
-            const float tn0 = tn, tvp0 = tvp, cU0 = cU, cI0 = cI;
+            const float tn0 = tn, tvp0 = tvp, cU0 = cU, cI0 = cI, tnl0 = tnl, tvpl0 = tvpl;
             // a quotient outside the range the fast division was verified on
             // (one vote per block): the block again with IEEE division
             if (__any_sync(0xffffffffu, updates(std::false_type{}))) {
                 tn = tn0;
                 tvp = tvp0;
+                tnl = tnl0;
+                tvpl = tvpl0;
                 cU = cU0;
                 cI = cI0;
                 updates(std::true_type{});
@@ -393,14 +449,20 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             const int s = s0 + u;
-            if (actv[u]) Tring[msl[u] * kTP + tix] = tnw[u];
+            if (actv[u]) {
+                Tring[msl[u] * kTP + tix] = tnw[u];
+                if (COMP) Lring[msl[u] * kTP + tix] = tnwl[u];
+            }
             if (TAPE && (FAST || s < nsteps)) {
                 pcode[32 * u] = actv[u] ? rec[u].code : (uint8_t)0;
                 pc1[32 * u] = rec[u].c1;
                 pc2[32 * u] = rec[u].c2;
             }
             // feed the next strip: lane 31 just finished march s-31
-            if (lane == 31 && a.h_out != nullptr && actv[u]) st_u64(a.h_out + (s - 31), pack_tag(tnw[u], a.tag));
+            if (lane == 31 && a.h_out != nullptr && actv[u]) {
+                st_u64(a.h_out + HS * (s - 31), pack_tag(tnw[u], a.tag));
+                if (COMP) st_u64(a.h_out + HS * (s - 31) + 1, pack_tag(tnwl[u], a.tag));
+            }
         }
         if (TAPE) {
             pcode += 32 * kU;
@@ -416,8 +478,12 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
             if (FAST || (s >= 31 && s < nsteps)) {
                 int ws = wb + u;
                 if (ws >= kRing) ws -= kRing;
-                if (vrow) *pW = Tring[ws * kTP + tix];
+                if (vrow) {
+                    *pW = Tring[ws * kTP + tix];
+                    if (COMP) *pWl = Lring[ws * kTP + tix];
+                }
                 pW += dT;
+                if (COMP) pWl += dT;
             }
         }
         b0 += kU;

@@ -59,6 +59,16 @@ class Engine:
         self.nx, self.nz, self.dx, self.dz = int(nx), int(nz), float(dx), float(dz)
         self.nxx, self.nzz, self.nb = a.value, b.value, c.value
         self.device = device
+        # the tape of the last taped batch: a counter that every call which
+        # replaces or consumes the tape advances, and the batch's (shots,
+        # receivers), so an adjoint can be checked against the forward it
+        # differentiates
+        self.tape_generation = 0
+        self.tape_shape = None
+
+    def _tape_changed(self, shape=None):
+        self.tape_generation += 1
+        self.tape_shape = shape
 
     def close(self):
         if self._ctx:
@@ -116,6 +126,7 @@ class Engine:
         if out is None:
             out = np.zeros((self.nxx, self.nzz), np.float32)
         p, mem, keep = _ptr(out)
+        self._tape_changed()
         self._check(self.L.sf_time_propagation(self._ctx, 1 if ani else 0, float(sx), float(sz), p, mem,
                                                _stream_ptr(stream)), "sf_time_propagation")
         return out
@@ -156,6 +167,7 @@ class Engine:
             out = np.zeros((ns, nr), np.float32)
         p, mem, keep = _ptr(out)
         flags = (SF_KEEP_TAPE if keep_tape else 0) | (SF_KEEP_TABLES if keep_tables else 0)
+        self._tape_changed((ns, nr) if keep_tape else None)
         self._check(self.L.sf_batch_forward(self._ctx, 1 if ani else 0, tab, ns,
                                             C.c_void_p(rx.ctypes.data), C.c_void_p(rz.ctypes.data), nr,
                                             p, mem, flags, _stream_ptr(stream)), "sf_batch_forward")
@@ -169,13 +181,35 @@ class Engine:
                     "sf_batch_table")
         return out
 
+    def _check_adjoint_args(self, per_shot, out, what):
+        """The C ABI cannot see buffer sizes: check them against the taped
+        batch (without one the C call reports SF_ERR_STATE)."""
+        if self.tape_shape is None:
+            return
+        n = int(np.prod(per_shot.shape)) if hasattr(per_shot, "shape") else len(per_shot)
+        if n != self.tape_shape[0] * self.tape_shape[1]:
+            raise ValueError(f"{what}: {n} values for a taped batch of {self.tape_shape[0]} shots x "
+                             f"{self.tape_shape[1]} receivers")
+        if out is not None and tuple(out.shape) != (self.nxx, self.nzz):
+            raise ValueError(f"{what}: output of shape {tuple(out.shape)}, expected {(self.nxx, self.nzz)}")
+
     def batch_adjoint(self, pick_grad, out=None, stream=None):
+        self._check_adjoint_args(pick_grad, out, "batch_adjoint")
         if out is None:
             out = np.zeros((self.nxx, self.nzz), np.float32)
         pg, pmem, k1 = _ptr(pick_grad)
         p, mem, k2 = _ptr(out)
+        self._tape_changed()  # the reverse sweeps consume the tape
         self._check(self.L.sf_batch_adjoint(self._ctx, pg, pmem, p, mem, _stream_ptr(stream)),
                     "sf_batch_adjoint")
+        return out
+
+    def tape_codes(self, shot, ncols, stream=None):
+        """Branch codes (4, ncols, nzz) of one shot of the last taped batch:
+        [sweep, window column, row], the oracle's tape layout."""
+        out = np.zeros((4, ncols, self.nzz), np.uint8)
+        self._check(self.L.sf_batch_tape_codes(self._ctx, int(shot), C.c_void_p(out.ctypes.data), SF_MEM_HOST,
+                                               _stream_ptr(stream)), "sf_batch_tape_codes")
         return out
 
     def stiffness_gradient(self, stream=None):
@@ -192,11 +226,13 @@ class Engine:
         """Misfit 1/2 sum (pick - t_obs)^2 of the taped batch and its slowness
         gradient (padded (nxx, nzz)). With want_misfit False and a device
         ``out`` the call only enqueues work on ``stream`` (misfit is None)."""
+        self._check_adjoint_args(t_obs, out, "misfit_gradient")
         if out is None:
             out = np.zeros((self.nxx, self.nzz), np.float32)
         po, omem, k1 = _ptr(t_obs)
         p, mem, k2 = _ptr(out)
         mis = C.c_double()
+        self._tape_changed()  # the reverse sweeps consume the tape
         self._check(self.L.sf_batch_misfit_gradient(self._ctx, po, omem, C.byref(mis) if want_misfit else None,
                                                     p, mem, _stream_ptr(stream)), "sf_batch_misfit_gradient")
         return (mis.value if want_misfit else None), out
@@ -350,11 +386,13 @@ class Engine:
         picks (nshots, nrec) f32; with t_obs, grad (nxx, nzz) f32 and
         optionally misfit (1,) f64."""
         a = self._plan_args(t_obs, picks, misfit, grad)
+        self._tape_changed(self._plan if t_obs is None else None)  # with t_obs the tape is consumed
         self._check(self.L.sf_plan_iteration(self._ctx, *a, _stream_ptr(stream)), "sf_plan_iteration")
 
     def plan_graph_launch(self, picks, t_obs=None, grad=None, misfit=None, stream=None):
         """The same iteration replayed from the context's CUDA graph."""
         a = self._plan_args(t_obs, picks, misfit, grad)
+        self._tape_changed(self._plan if t_obs is None else None)
         self._check(self.L.sf_plan_graph_launch(self._ctx, *a, _stream_ptr(stream)), "sf_plan_graph_launch")
 
     def plan_autotune(self, picks, t_obs=None, grad=None, misfit=None, reps=3, stream=None):
@@ -362,6 +400,7 @@ class Engine:
         (warps_per_cta, gang_warps, ms_per_iteration)."""
         a = self._plan_args(t_obs, picks, misfit, grad)
         w, g, ms = C.c_int(), C.c_int(), C.c_float()
+        self._tape_changed(self._plan if t_obs is None else None)
         self._check(self.L.sf_plan_autotune(self._ctx, *a, int(reps), _stream_ptr(stream), C.byref(w), C.byref(g),
                                             C.byref(ms)), "sf_plan_autotune")
         return w.value, g.value, ms.value
@@ -382,15 +421,19 @@ class Engine:
     def synchronize(self, stream=None):
         self._check(self.L.sf_synchronize(self._ctx, _stream_ptr(stream)), "sf_synchronize")
 
+    ARITHMETICS = {"reference": _lib.SF_ARITH_REFERENCE, "ieee": _lib.SF_ARITH_IEEE,
+                   "compensated": _lib.SF_ARITH_COMPENSATED}
+
     def set_arithmetic(self, mode):
-        """'reference' (the reference build's FP32 arithmetic) or 'ieee'."""
-        m = {"reference": _lib.SF_ARITH_REFERENCE, "ieee": _lib.SF_ARITH_IEEE}[mode]
-        self._check(self.L.sf_set_arithmetic(self._ctx, m), "sf_set_arithmetic")
+        """'reference' (the reference build's FP32 arithmetic), 'ieee' (every
+        operation rounded once) or 'compensated' (traveltimes carried as FP32
+        pairs; see sf_set_arithmetic)."""
+        self._check(self.L.sf_set_arithmetic(self._ctx, self.ARITHMETICS[mode]), "sf_set_arithmetic")
 
     def get_arithmetic(self):
         v = C.c_int()
         self.L.sf_get_arithmetic(self._ctx, C.byref(v))
-        return "reference" if v.value == _lib.SF_ARITH_REFERENCE else "ieee"
+        return {m: k for k, m in self.ARITHMETICS.items()}[v.value]
 
     def set_launch(self, warps=0, gang_warps=0):
         """warps per CTA (0 keeps it) and warps per shot (0: automatic)."""

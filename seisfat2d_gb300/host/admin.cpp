@@ -2,24 +2,11 @@
 
 #include <algorithm>
 #include <fstream>
-#include <iomanip>
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
 
 #include "seisfat2d.h"
-
-int nextpow2(int n)
-{
-    if (n == 0) return 1;
-    n--;
-    n |= n >> 1;
-    n |= n >> 2;
-    n |= n >> 4;
-    n |= n >> 8;
-    n |= n >> 16;
-    return n + 1;
-}
 
 bool str2bool(std::string s)
 {
@@ -80,26 +67,6 @@ std::vector<std::string> split(std::string s, char delimiter)
     std::istringstream ts(s);
     while (getline(ts, token, delimiter)) tokens.push_back(token);
     return tokens;
-}
-
-std::string format1Decimal(float x)
-{
-    std::ostringstream oss;
-    oss << std::fixed << std::setprecision(1) << x;
-    return oss.str();
-}
-
-float cubic1d(float P[4], float dx)
-{
-    return P[1] + 0.5f * dx * (P[2] - P[0] + dx * (2.0f * P[0] - 5.0f * P[1] + 4.0f * P[2] - P[3] +
-                                                   dx * (3.0f * (P[1] - P[2]) + P[3] - P[0])));
-}
-
-float cubic2d(float P[4][4], float dx, float dy)
-{
-    float p[4];
-    for (int k = 0; k < 4; k++) p[k] = cubic1d(P[k], dy);
-    return cubic1d(p, dx);
 }
 
 void sf_check(int status, void* ctx, const char* what)

@@ -7,7 +7,6 @@
 #include <string>
 #include <vector>
 
-int nextpow2(int n);                                   // admin.cpp:3-13
 bool str2bool(std::string s);                          // admin.cpp:15-23 (anything but "true" is false)
 void import_binary_float(std::string path, float* array, int n);   // admin.cpp:25-35
 void export_binary_float(std::string path, float* array, int n);   // admin.cpp:37-49
@@ -19,9 +18,6 @@ void import_text_file(std::string path, std::vector<std::string>& elements);
 // '#', and has every space removed. Missing key -> "".
 std::string catch_parameter(std::string target, std::string file);
 std::vector<std::string> split(std::string s, char delimiter);     // admin.cpp:102-113
-std::string format1Decimal(float x);                               // admin.cpp:115-120
-float cubic1d(float P[4], float dx);                               // admin.cpp:121-124
-float cubic2d(float P[4][4], float dx, float dy);                  // admin.cpp:126-133
 
 // Throws std::runtime_error with the engine's message for a non-zero status.
 void sf_check(int status, void* ctx, const char* what);

@@ -22,7 +22,7 @@ def setup(nx=70, nz=36, seed=3, noise=0.02, arith="ieee"):
     return e, m
 
 
-@pytest.mark.parametrize("arith", ["ieee", "reference"])
+@pytest.mark.parametrize("arith", ["ieee", "reference", "compensated"])
 def test_adjoint_bitexact_vs_oracle(oracle, engine_lib, cuda, arith):
     e, m = setup(arith=arith)
     oracle.set_arith(arith)
@@ -193,3 +193,27 @@ def test_fused_gather_same_bits(engine_lib, cuda, warps):
         e.synchronize()
         assert e.fused_gather() == (True, True)
         assert np.array_equal(grad.cpu().numpy(), res[False][2])
+
+
+def test_autograd_backward_refuses_a_replaced_tape(engine_lib, cuda):
+    """Two forwards on one engine before the backward: the first forward's
+    backward would differentiate the second batch's tape, so it raises; the
+    second's backward equals the direct adjoint."""
+    import torch
+    from seisfat2d_gb300.autograd import EikonalPicks
+    e, m = setup(nx=50, nz=30, seed=9)
+    rx, rz = surface_receivers(e.nx, 10.0, step=3)
+    S = torch.tensor(e.get_slowness(), device="cuda", requires_grad=True)
+    p1 = EikonalPicks.apply(S, e, [(100.0, 0.0)], rx, rz)
+    p2 = EikonalPicks.apply(S, e, [(100.0, 0.0), (300.0, 50.0)], rx, rz)
+    with pytest.raises(RuntimeError, match="tape belongs to a later call"):
+        torch.nansum(p1).backward(retain_graph=True)
+    S.grad = None
+    torch.nansum(p2).backward()
+    e.batch_forward([(100.0, 0.0), (300.0, 50.0)], rx, rz, keep_tape=True)
+    pg = np.where(np.isnan(p2.detach().cpu().numpy()), np.nan, 1.0).astype(np.float32)
+    assert np.array_equal(S.grad.cpu().numpy(), e.batch_adjoint(pg))
+    # a pick gradient of the wrong size never reaches the device
+    e.batch_forward([(100.0, 0.0)], rx, rz, keep_tape=True)
+    with pytest.raises(ValueError, match="taped batch of 1 shots"):
+        e.batch_adjoint(np.zeros((2, len(rx)), np.float32))

@@ -44,7 +44,7 @@ def dev_buffers(torch, e, tobs):
                 misfit=torch.empty(1, dtype=torch.float64, device=dev))
 
 
-@pytest.mark.parametrize("arith", ["reference", "ieee"])
+@pytest.mark.parametrize("arith", ["reference", "ieee", "compensated"])
 def test_plan_iteration_equals_batch_calls(oracle, engine_lib, cuda, arith):
     e, m, rx, rz = make(arith=arith)
     tobs = observed(e, rx, rz)

@@ -33,6 +33,32 @@ def test_noalloc_matches_time_propagation_twice(engine_lib, cuda):
         assert np.array_equal(T.cpu().numpy(), ref)
 
 
+def test_noalloc_sequence_of_grids_matches_time_propagation(engine_lib, cuda):
+    """Calls that change the grid between them, each equal to the allocating
+    entry point bit for bit: a tall square-cell grid (10 strips, more than the
+    8 warps of the call's CTA, so warps run several strips), a small grid
+    with dx != dz, then the tall grid again (the per-call epoch keeps the
+    second call from taking pairs the first left in the shared array)."""
+    import torch
+    from seisfat2d_gb300 import Engine
+    from seisfat2d_gb300._lib import SF_OK
+    cases = [(200, 300, 10.0, 10.0, 77, (650.0, 0.0)), (90, 40, 12.5, 7.5, 78, (400.0, 120.0)),
+             (200, 300, 10.0, 10.0, 77, (1300.0, 1700.0))]
+    for nx, nz, dx, dz, seed, (sx, sz) in cases:
+        m = smooth_model(nx, nz, 10.0, seed=seed, noise=0.03)
+        e = Engine(nx, nz, dx, dz)
+        e.set_slowness(m)
+        S = torch.tensor(e.get_slowness(), device="cuda")
+        ref = e.time_propagation(sx, sz)
+        T = torch.full((e.nxx, e.nzz), -1.0, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        st = engine_lib.sf_time_propagation_noalloc(C.c_void_p(S.data_ptr()), nx, nz, dx, dz, sx, sz,
+                                                    C.c_void_p(T.data_ptr()), None)
+        assert st == SF_OK
+        assert np.array_equal(T.cpu().numpy(), ref), (nx, nz, dx, dz)
+        del e
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(engine_lib, cuda):
     from seisfat2d_gb300._lib import SF_ERR_RANGE
     # ceil(1006/32) * 8506 = 32 * 8506 > 262144 values: refused before any GPU work
