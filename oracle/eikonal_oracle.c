@@ -415,7 +415,10 @@ static float node32(int sweep, int i, int j, int nzz, int ncols, const float* S,
     return upd32(TAT(i, j), tv, te, tev, s1a, s1b, s2a, s2b, sref, k, dr1, dc1a, dc2, dr2a, rec);
 }
 
-static double node64(int sweep, int i, int j, int nzz, int ncols, const float* S, int ldS,
+/* S or, when Sd is given, the FP64 slowness Sd (same layout) */
+#define SAT64(i, j) (Sd ? Sd[(size_t)(i) + (size_t)(j) * ldS] : (double)SAT(i, j))
+
+static double node64(int sweep, int i, int j, int nzz, int ncols, const float* S, const double* Sd, int ldS,
                      const double* T, const k64* k, rec_t* rec)
 {
     int sz, sx;
@@ -425,9 +428,9 @@ static double node64(int sweep, int i, int j, int nzz, int ncols, const float* S
     double tv = TAT(i - sz, j);
     double te = TAT(i, j - sx);
     double tev = TAT(i - sz, j - sx);
-    double s1a = SAT(i1, imax(j - 1, 1)), s1b = SAT(i1, imin(j, ncols - 1));
-    double s2a = SAT(imax(i - 1, 1), j1), s2b = SAT(imin(i, nzz - 1), j1);
-    double sref = SAT(i1, j1);
+    double s1a = SAT64(i1, imax(j - 1, 1)), s1b = SAT64(i1, imin(j, ncols - 1));
+    double s2a = SAT64(imax(i - 1, 1), j1), s2b = SAT64(imin(i, nzz - 1), j1);
+    double sref = SAT64(i1, j1);
     int dr1 = (sz > 0) ? 0 : 1, dc2 = (sx > 0) ? 0 : 1;
     int dc1a = (j - 1 >= 1) ? 0 : 1, dr2a = (i - 1 >= 1) ? 0 : 1;
     return upd64(TAT(i, j), tv, te, tev, s1a, s1b, s2a, s2b, sref, k, dr1, dc1a, dc2, dr2a, rec);
@@ -559,12 +562,13 @@ static ff_t updc(ff_t told, ff_t tv, ff_t te, ff_t tev, float s1a, float s1b, fl
 /* One compensated solve (1 pass, any DAG order gives the same bits): T gets
  * the hi parts; the initial 3x3 values enter with lo = 0. */
 static void solve_comp(int nzz, int ncols, const float* S, int ldS, float dx, float dz, int sIdz, int sIdx_loc,
-                       const float init[9], float* T, uint8_t* code, float* c1, float* c2)
+                       const float init[9], float* T, float* Lout, uint8_t* code, float* c1, float* c2)
 {
     k32 k = make_k32(dx, dz);
     int si[4], sj[4];
     orc_skip_cells(ncols, nzz, si, sj);
-    float* L = (float*)calloc((size_t)nzz * ncols, sizeof(float));
+    float* L = Lout ? Lout : (float*)calloc((size_t)nzz * ncols, sizeof(float));
+    if (Lout) memset(L, 0, sizeof(float) * (size_t)nzz * ncols);
     for (size_t n = 0; n < (size_t)nzz * ncols; n++) T[n] = SF_BIG;
     for (int b = 0; b < 3; b++)
         for (int a = 0; a < 3; a++) TAT(sIdz + a - 1, sIdx_loc + b - 1) = init[a + 3 * b];
@@ -600,7 +604,7 @@ static void solve_comp(int nzz, int ncols, const float* S, int ldS, float dx, fl
         }
     }
 #undef PAIR
-    free(L);
+    if (!Lout) free(L);
 }
 
 static void init_field_f32(float* T, int nzz, int ncols, int sIdz, int sIdx_loc, const float init[9])
@@ -622,7 +626,7 @@ void orc_solve_f32(int nzz, int ncols, const float* S, int ldS, float dx, float 
                    int sIdx_loc, const float init[9], float* T, int passes, int order)
 {
     if (g_arith == 2) {
-        solve_comp(nzz, ncols, S, ldS, dx, dz, sIdz, sIdx_loc, init, T, NULL, NULL, NULL);
+        solve_comp(nzz, ncols, S, ldS, dx, dz, sIdz, sIdx_loc, init, T, NULL, NULL, NULL, NULL);
         return;
     }
     k32 k = make_k32(dx, dz);
@@ -661,9 +665,20 @@ void orc_solve_f32(int nzz, int ncols, const float* S, int ldS, float dx, float 
         }
 }
 
+static int solve_f64_any(int nzz, int ncols, const float* S, const double* Sd, int ldS, double dx, double dz,
+                         int sIdz, int sIdx_loc, const double init[9], double* T, int passes, double tol,
+                         int max_passes);
+
 int orc_solve_f64(int nzz, int ncols, const float* S, int ldS, double dx, double dz, int sIdz,
                   int sIdx_loc, const double init[9], double* T, int passes, double tol,
                   int max_passes)
+{
+    return solve_f64_any(nzz, ncols, S, NULL, ldS, dx, dz, sIdz, sIdx_loc, init, T, passes, tol, max_passes);
+}
+
+static int solve_f64_any(int nzz, int ncols, const float* S, const double* Sd, int ldS, double dx, double dz,
+                         int sIdz, int sIdx_loc, const double init[9], double* T, int passes, double tol,
+                         int max_passes)
 {
     k64 k = make_k64(dx, dz);
     int si[4], sj[4];
@@ -682,7 +697,7 @@ int orc_solve_f64(int nzz, int ncols, const float* S, int ldS, double dx, double
                     int i = (sz > 0) ? ii : nzz - 1 - ii;
                     if (is_skip(s, i, j, si, sj)) continue;
                     double old = TAT(i, j);
-                    double nv = node64(s, i, j, nzz, ncols, S, ldS, T, &k, NULL);
+                    double nv = node64(s, i, j, nzz, ncols, S, Sd, ldS, T, &k, NULL);
                     TAT(i, j) = nv;
                     if (old < 1e6 && old - nv > change) change = old - nv;
                     if (old >= 1e6 && nv < 1e6) change = 1e30;
@@ -726,9 +741,33 @@ static float decode_c(uint16_t c, float mn, float mx)
 }
 
 /* eikonal_ani.cu:47-111 */
+/* Central differences T(i+1) - T(i-1) and T(j+1) - T(j-1) at window index
+ * it; of the pairs (T, L) in the compensated arithmetic (L not NULL). */
+static void central_diffs(const float* T, const float* L, size_t it, int nzz, float* dzr, float* dxr)
+{
+    if (L) {
+        *dzr = (T[it + 1] - T[it - 1]) + (L[it + 1] - L[it - 1]);
+        *dxr = (T[it + nzz] - T[it - nzz]) + (L[it + nzz] - L[it - nzz]);
+    } else {
+        *dzr = T[it + 1] - T[it - 1];
+        *dxr = T[it + nzz] - T[it - nzz];
+    }
+}
+
+static void qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* L, const float* Sin, int ldS,
+                          float dx, float dz, int sIdz, int sIdx_loc, const uint16_t* const codes[6],
+                          const float mm[12], float* Sout);
+
 void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* Sin, int ldS,
                        float dx, float dz, int sIdz, int sIdx_loc,
                        const uint16_t* const codes[6], const float mm[12], float* Sout)
+{
+    qslowness_f32(nzz, ncols, nb, T, NULL, Sin, ldS, dx, dz, sIdz, sIdx_loc, codes, mm, Sout);
+}
+
+static void qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* L, const float* Sin, int ldS,
+                          float dx, float dz, int sIdz, int sIdx_loc, const uint16_t* const codes[6],
+                          const float mm[12], float* Sout)
 {
     for (int j = 0; j < ncols; j++)
         for (int i = 0; i < nzz; i++) {
@@ -738,8 +777,10 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
             Sout[it] = s;
             if (!((i >= nb) && (i < nzz - nb) && (j >= nb) && (j < ncols - nb))) continue;
             if ((i == sIdz) && (j == sIdx_loc)) continue;
-            float dTz = 0.5f * (T[it + 1] - T[it - 1]) / dz;
-            float dTx = 0.5f * (T[it + nzz] - T[it - nzz]) / dx;
+            float dzr, dxr;
+            central_diffs(T, L, it, nzz, &dzr, &dxr);
+            float dTz = 0.5f * dzr / dz;
+            float dTx = 0.5f * dxr / dx;
             const int ref = g_arith == 1;
             float norm = sqrtf(ref ? fmaf(dTz, dTz, dTx * dTx) : dTx * dTx + dTz * dTz);
             float p0 = dTx / norm, p1 = dTz / norm;
@@ -776,6 +817,72 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
         }
 }
 
+/* FP64 twin of orc_qslowness_f32 (eikonal_ani.cu:47-111 evaluated in FP64,
+ * the uint16 codes decoded in FP64): Sout (FP64) gets the qP slowness of the
+ * interior cells except the source node and Sin elsewhere. */
+void orc_qslowness_f64(int nzz, int ncols, int nb, const double* T, const float* Sin, int ldS, double dx,
+                       double dz, int sIdz, int sIdx_loc, const uint16_t* const codes[6], const float mm[12],
+                       double* Sout)
+{
+    for (int j = 0; j < ncols; j++)
+        for (int i = 0; i < nzz; i++) {
+            size_t is = (size_t)i + (size_t)j * ldS;
+            size_t it = (size_t)i + (size_t)j * nzz;
+            double s = Sin[is];
+            Sout[it] = s;
+            if (!((i >= nb) && (i < nzz - nb) && (j >= nb) && (j < ncols - nb))) continue;
+            if ((i == sIdz) && (j == sIdx_loc)) continue;
+            double dTz = 0.5 * (T[it + 1] - T[it - 1]) / dz;
+            double dTx = 0.5 * (T[it + nzz] - T[it - nzz]) / dx;
+            double norm = sqrt(dTx * dTx + dTz * dTz);
+            double p0 = dTx / norm, p1 = dTz / norm;
+            double c[6];
+            for (int q = 0; q < 6; q++)
+                c[q] = (double)mm[2 * q] + ((double)codes[q][is] - 1.0) * ((double)mm[2 * q + 1] - (double)mm[2 * q]) /
+                                           65534.0;
+            /* c11, c13, c15, c33, c35, c55 */
+            double Ro = c[3] * s * s;
+            double C0 = c[0] / Ro / Ro, C3 = c[1] / Ro / Ro, C6 = c[2] / Ro / Ro;
+            double C4 = c[3] / Ro / Ro, C7 = c[4] / Ro / Ro, C8 = c[5] / Ro / Ro;
+            double Gxx = C0 * p0 * p0 + C8 * p1 * p1 + 2.0 * C6 * p0 * p1;
+            double Gzz = C8 * p0 * p0 + C4 * p1 * p1 + 2.0 * C7 * p0 * p1;
+            double Gxz = C6 * p0 * p0 + C7 * p1 * p1 + (C3 + C8) * p0 * p1;
+            double coeff1 = Gxx + Gzz, coeff2 = Gxx - Gzz;
+            double det = sqrt(coeff2 * coeff2 / 4.0 + Gxz * Gxz);
+            double g0 = coeff1 / 2.0 + det, g1 = coeff1 / 2.0 - det;
+            if (g0 < g1) g0 = g1;
+            Sout[it] = 1.0 / sqrt(g0 * Ro);
+        }
+}
+
+/* The whole two-pass anisotropic shot (eikonal_ani.cu:33-45) in FP64: FP64
+ * initialisation and solve, FP64 qP field from the FP64 traveltimes, FP64
+ * initialisation from it and the second FP64 solve. T: nzz x ncols (FP64).
+ * Returns 0, or -1 for a source outside its window. */
+int orc_shot_ani_f64(int nzz, int nxx, int nb, const float* S, float dx, float dz, int c0, int ncols, float sx,
+                     float sz, const uint16_t* const codes[6], const float mm[12], double* T)
+{
+    int sIdx, sIdz;
+    orc_source_index(sx, sz, dx, dz, nb, &sIdx, &sIdz);
+    const int sloc = sIdx - c0;
+    if (sIdz < 1 || sIdz > nzz - 2 || sloc < 1 || sloc > ncols - 2 || c0 < 0 || c0 + ncols > nxx) return -1;
+    const size_t n = (size_t)nzz * ncols;
+    const float* Sw = S + (size_t)c0 * nzz;
+    double init[9], dist[9];
+    orc_init_block_f64(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, init);
+    solve_f64_any(nzz, ncols, Sw, NULL, nzz, dx, dz, sIdz, sloc, init, T, 1, 0.0, 1);
+    double* Sq = (double*)malloc(n * sizeof(double));
+    const uint16_t* cw[6];
+    for (int q = 0; q < 6; q++) cw[q] = codes[q] + (size_t)c0 * nzz;
+    orc_qslowness_f64(nzz, ncols, nb, T, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
+    init_dist_f64(nb, sx, sz, dx, dz, sIdx, sIdz, dist);
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) init[a + 3 * b] = Sq[(size_t)(sIdz + a - 1) + (size_t)(sloc + b - 1) * nzz] * dist[a + 3 * b];
+    solve_f64_any(nzz, ncols, NULL, Sq, nzz, dx, dz, sIdz, sloc, init, T, 1, 0.0, 1);
+    free(Sq);
+    return 0;
+}
+
 /* Derivatives of one node's qP slowness with the direction p = grad T /
  * |grad T| of the first solve held fixed: Sq = S sqrt(c33 / lambda), lambda the
  * larger eigenvalue of the Christoffel matrix along p, v its unit eigenvector;
@@ -783,12 +890,11 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
  * dSq/dC13 = -Sq px pz vx vz / lambda. FP32, each operation rounded once, in
  * this order (the engine's qp_factors in sf_device.cuh); (1, 0, 0) for a zero
  * gradient or a non-positive eigenvalue. */
-static void qp_factors_f32(float tzp, float tzm, float txp, float txm, float s, float dx, float dz, float c11,
-                           float c13, float c15, float c33, float c35, float c55, float* fS, float* f11,
-                           float* f13)
+static void qp_factors_f32(float dzr, float dxr, float s, float dx, float dz, float c11, float c13, float c15,
+                           float c33, float c35, float c55, float* fS, float* f11, float* f13)
 {
-    float dTz = (0.5f * (tzp - tzm)) / dz;
-    float dTx = (0.5f * (txp - txm)) / dx;
+    float dTz = (0.5f * dzr) / dz;
+    float dTx = (0.5f * dxr) / dx;
     float nrm = sqrtf(dTx * dTx + dTz * dTz);
     *fS = 1.0f;
     *f11 = 0.0f;
@@ -817,9 +923,20 @@ static void qp_factors_f32(float tzp, float tzm, float txp, float txm, float s, 
 
 /* The factors over a window, as the qP pass runs (interior nodes except the
  * source; the others keep S: (1, 0, 0)). */
+static void qp_factors_all(int nzz, int ncols, int nb, const float* T, const float* L, const float* Sin, int ldS,
+                           float dx, float dz, int sIdz, int sIdx_loc, const uint16_t* const codes[6],
+                           const float mm[12], float* fS, float* f11, float* f13);
+
 void orc_qp_factors(int nzz, int ncols, int nb, const float* T, const float* Sin, int ldS, float dx, float dz,
                     int sIdz, int sIdx_loc, const uint16_t* const codes[6], const float mm[12], float* fS,
                     float* f11, float* f13)
+{
+    qp_factors_all(nzz, ncols, nb, T, NULL, Sin, ldS, dx, dz, sIdz, sIdx_loc, codes, mm, fS, f11, f13);
+}
+
+static void qp_factors_all(int nzz, int ncols, int nb, const float* T, const float* L, const float* Sin, int ldS,
+                           float dx, float dz, int sIdz, int sIdx_loc, const uint16_t* const codes[6],
+                           const float mm[12], float* fS, float* f11, float* f13)
 {
     for (int j = 0; j < ncols; j++)
         for (int i = 0; i < nzz; i++) {
@@ -830,7 +947,9 @@ void orc_qp_factors(int nzz, int ncols, int nb, const float* T, const float* Sin
             f13[it] = 0.0f;
             if (!((i >= nb) && (i < nzz - nb) && (j >= nb) && (j < ncols - nb))) continue;
             if ((i == sIdz) && (j == sIdx_loc)) continue;
-            qp_factors_f32(T[it + 1], T[it - 1], T[it + nzz], T[it - nzz], Sin[is], dx, dz,
+            float dzr, dxr;
+            central_diffs(T, L, it, nzz, &dzr, &dxr);
+            qp_factors_f32(dzr, dxr, Sin[is], dx, dz,
                            decode_c(codes[0][is], mm[0], mm[1]), decode_c(codes[1][is], mm[2], mm[3]),
                            decode_c(codes[2][is], mm[4], mm[5]), decode_c(codes[3][is], mm[6], mm[7]),
                            decode_c(codes[4][is], mm[8], mm[9]), decode_c(codes[5][is], mm[10], mm[11]),
@@ -1085,12 +1204,16 @@ int orc_shot_f32(int nzz, int nxx, int nb, const float* S, float dx, float dz, i
         orc_init_block_f64(S, nzz, sx, sz, dx, dz, nb, sIdx, sIdz, iv);
         for (int q = 0; q < 9; q++) init[q] = (float)iv[q];
     }
-    orc_solve_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sloc, init, Tw, 1, 1);
+    /* compensated: the qP pass reads the lo parts of the first solve too */
+    float* L = (ani && g_arith == 2) ? (float*)malloc(n * sizeof(float)) : NULL;
+    if (L) solve_comp(nzz, ncols, Sw, nzz, dx, dz, sIdz, sloc, init, Tw, L, NULL, NULL, NULL);
+    else orc_solve_f32(nzz, ncols, Sw, nzz, dx, dz, sIdz, sloc, init, Tw, 1, 1);
     if (ani) {
         float* Sq = (float*)malloc(n * sizeof(float));
         const uint16_t* cw[6];
         for (int c = 0; c < 6; c++) cw[c] = codes[c] + (size_t)c0 * nzz;
-        orc_qslowness_f32(nzz, ncols, nb, Tw, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
+        qslowness_f32(nzz, ncols, nb, Tw, L, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
+        free(L);
         /* second initialisation reads the qP slowness (eikonal_ani.cu:40-41) */
         for (int b = 0; b < 3; b++)
             for (int a = 0; a < 3; a++) {
@@ -1140,7 +1263,7 @@ void orc_solve_tape_f32(int nzz, int ncols, const float* S, int ldS, float dx, f
                         float* c2)
 {
     if (g_arith == 2) {
-        solve_comp(nzz, ncols, S, ldS, dx, dz, sIdz, sIdx_loc, init, T, code, c1, c2);
+        solve_comp(nzz, ncols, S, ldS, dx, dz, sIdz, sIdx_loc, init, T, NULL, code, c1, c2);
         return;
     }
     k32 k = make_k32(dx, dz);
@@ -1186,7 +1309,7 @@ void orc_solve_tape_f64(int nzz, int ncols, const float* S, int ldS, double dx, 
                 int i = (sz > 0) ? ii : nzz - 1 - ii;
                 if (is_skip(s, i, j, si, sj)) continue;
                 rec_t r;
-                TAT(i, j) = node64(s, i, j, nzz, ncols, S, ldS, T, &k, &r);
+                TAT(i, j) = node64(s, i, j, nzz, ncols, S, NULL, ldS, T, &k, &r);
                 code[TP(s, i, j)] = (uint8_t)r.code;
                 c1[TP(s, i, j)] = r.c1;
                 c2[TP(s, i, j)] = r.c2;
@@ -1413,10 +1536,13 @@ int orc_batch_gradient_f32(int nzz, int nxx, int nb, const float* S, float dx, f
             float* Sq = (float*)malloc(n * sizeof(float));
             const uint16_t* cw[6];
             for (int q = 0; q < 6; q++) cw[q] = codes[q] + (size_t)c0[b] * nzz;
-            orc_solve_f32(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, 1, 1);
-            orc_qslowness_f32(nzz, nc, nb, T, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
-            orc_qp_factors(nzz, nc, nb, T, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, fS, fS + off[nshots],
+            float* L = (g_arith == 2) ? (float*)malloc(n * sizeof(float)) : NULL;
+            if (L) solve_comp(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, L, NULL, NULL, NULL);
+            else orc_solve_f32(nzz, nc, Sw, nzz, dx, dz, sIdz, sloc, init, T, 1, 1);
+            qslowness_f32(nzz, nc, nb, T, L, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, Sq);
+            qp_factors_all(nzz, nc, nb, T, L, Sw, nzz, dx, dz, sIdz, sloc, cw, mm, fS, fS + off[nshots],
                            fS + 2 * off[nshots]);
+            free(L);
             for (int bb = 0; bb < 3; bb++)
                 for (int a = 0; a < 3; a++) {
                     int zi = sIdz + a - 1, xl = sloc + bb - 1;

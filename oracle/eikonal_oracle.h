@@ -74,6 +74,15 @@ void orc_qslowness_f32(int nzz, int ncols, int nb, const float* T, const float* 
                        float dx, float dz, int sIdz, int sIdx_loc,
                        const uint16_t* const codes[6], const float mm[12], float* Sout);
 
+/* FP64 twins of the anisotropic path: the qP pass (FP64 traveltimes in,
+ * FP64 slowness out, codes decoded in FP64) and the whole two-pass shot in
+ * FP64 (T: nzz x ncols doubles; returns -1 for a source outside). */
+void orc_qslowness_f64(int nzz, int ncols, int nb, const double* T, const float* Sin, int ldS, double dx,
+                       double dz, int sIdz, int sIdx_loc, const uint16_t* const codes[6], const float mm[12],
+                       double* Sout);
+int orc_shot_ani_f64(int nzz, int nxx, int nb, const float* S, float dx, float dz, int c0, int ncols, float sx,
+                     float sz, const uint16_t* const codes[6], const float mm[12], double* T);
+
 /* Receiver picks by the reference's 4x4 Catmull-Rom rule on a window whose
  * first padded column is c0. Receivers whose stencil leaves the window's
  * columns [1, ncols-2] or rows [1, nzz-2] give NaN. */

@@ -59,6 +59,9 @@ def lib():
                                          C.c_int, C.c_int, f64p, f64p, u8p, f64p, f64p]
         L.orc_solve_follow_f64.argtypes = [C.c_int, C.c_int, f32p, C.c_int, C.c_double, C.c_double,
                                            C.c_int, C.c_int, f64p, u8p, f64p, f64p, f64p]
+        L.orc_shot_ani_f64.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float, C.c_int, C.c_int,
+                                       C.c_float, C.c_float, C.c_void_p * 6, f32p, f64p]
+        L.orc_shot_ani_f64.restype = C.c_int
         L.orc_picks_f64.argtypes = [f64p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, f32p, f32p,
                                     C.c_int, f64p]
         L.orc_misfit_f64.argtypes = [C.c_int, C.c_int, C.c_int, f32p, C.c_float, C.c_float, C.c_int, f32p, f32p,
@@ -586,3 +589,16 @@ def fd_misfit_f64(S, dx, dz, shots, rx, rz, t_obs, cells, rel=1e-5, nb=3, nthrea
                                    len(rx), tobs, n, ci, cj, rel, sp, sm, jp, jm, nthreads)
     d = (jp - jm) / (sp.astype(np.float64) - sm.astype(np.float64))
     return d, jp - jm, used
+
+
+def shot_ani_f64(S, dx, dz, sx, sz, ani, nb=3, c0=0, ncols=None):
+    """The two-pass anisotropic shot in FP64 (FP64 first solve, qP field and
+    second solve); ani = (codes[6], mm[12]). Returns T (ncols, nzz) float64."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    ncols = nxx - c0 if ncols is None else ncols
+    arr, keep = _codes_arg(ani[0])
+    T = np.zeros((ncols, nzz), np.float64)
+    if lib().orc_shot_ani_f64(nzz, nxx, nb, S, dx, dz, c0, ncols, sx, sz, arr, _f32(ani[1]), T) != 0:
+        raise ValueError("source outside the window")
+    return T

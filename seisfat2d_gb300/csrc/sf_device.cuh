@@ -365,15 +365,15 @@ __device__ __forceinline__ float decode_c(uint16_t c, float mn, float mx)
 }
 
 // qP phase slowness of one node (eikonal_ani.cu:59-108); codes already
-// decoded. REF: the reference build's FMAs (|grad T|^2 and the three
-// Christoffel sums).
+// decoded. dzr, dxr: the central differences T(i+1) - T(i-1) and T(j+1) -
+// T(j-1) (of the pairs, in the compensated arithmetic). REF: the reference
+// build's FMAs (|grad T|^2 and the three Christoffel sums).
 template <bool REF>
-__device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, float txm, float s,
-                                             float dx, float dz, float c11, float c13, float c15,
-                                             float c33, float c35, float c55)
+__device__ __forceinline__ float qp_slowness(float dzr, float dxr, float s, float dx, float dz, float c11,
+                                             float c13, float c15, float c33, float c35, float c55)
 {
-    float dTz = fdiv(fmul(0.5f, fsub(tzp, tzm)), dz);
-    float dTx = fdiv(fmul(0.5f, fsub(txp, txm)), dx);
+    float dTz = fdiv(fmul(0.5f, dzr), dz);
+    float dTx = fdiv(fmul(0.5f, dxr), dx);
     float norm = fsqrt(REF ? __fmaf_rn(dTz, dTz, fmul(dTx, dTx)) : fadd(fmul(dTx, dTx), fmul(dTz, dTz)));
     float p0 = fdiv(dTx, norm), p1 = fdiv(dTz, norm);
     float Ro = fmul(fmul(c33, s), s);
@@ -422,12 +422,12 @@ __device__ __forceinline__ float qp_slowness(float tzp, float tzm, float txp, fl
 // In FP32 with each operation rounded once (no contraction), so a C
 // restatement gives the same bits; FP32 keeps the pass off the GPU's slow
 // FP64 pipe. A zero gradient or a non-positive eigenvalue gives (1, 0, 0).
-__device__ __forceinline__ void qp_factors(float tzp, float tzm, float txp, float txm, float s, float dx,
-                                           float dz, float c11, float c13, float c15, float c33, float c35,
-                                           float c55, float& fS, float& f11, float& f13)
+__device__ __forceinline__ void qp_factors(float dzr, float dxr, float s, float dx, float dz, float c11,
+                                           float c13, float c15, float c33, float c35, float c55, float& fS,
+                                           float& f11, float& f13)
 {
-    const float dTz = fdiv(fmul(0.5f, fsub(tzp, tzm)), dz);
-    const float dTx = fdiv(fmul(0.5f, fsub(txp, txm)), dx);
+    const float dTz = fdiv(fmul(0.5f, dzr), dz);
+    const float dTx = fdiv(fmul(0.5f, dxr), dx);
     const float nrm = fsqrt(fadd(fmul(dTx, dTx), fmul(dTz, dTz)));
     fS = 1.0f;
     f11 = 0.0f;

@@ -232,11 +232,18 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
                         const float c33 = decode_c(p.cij[3][g], p.mm[6], p.mm[7]);
                         const float c35 = decode_c(p.cij[4][g], p.mm[8], p.mm[9]);
                         const float c55 = decode_c(p.cij[5][g], p.mm[10], p.mm[11]);
-                        out = qp_slowness<REF>(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz, c11,
-                                               c13, c15, c33, c35, c55);
-                        if (VTI)
-                            qp_factors(Tc[1], Tc[-1], Tc[nzz], Tc[-(long)nzz], s, p.kc.dx, p.kc.dz, c11, c13, c15,
-                                       c33, c35, c55, fS, f11, f13);
+                        // central differences; of the pairs in the compensated arithmetic
+                        float dzr, dxr;
+                        if (COMP) {
+                            const float* Lc = Tl + idx;
+                            dzr = ff_diff(Tc[1], Lc[1], Tc[-1], Lc[-1]);
+                            dxr = ff_diff(Tc[nzz], Lc[nzz], Tc[-(long)nzz], Lc[-(long)nzz]);
+                        } else {
+                            dzr = fsub(Tc[1], Tc[-1]);
+                            dxr = fsub(Tc[nzz], Tc[-(long)nzz]);
+                        }
+                        out = qp_slowness<REF>(dzr, dxr, s, p.kc.dx, p.kc.dz, c11, c13, c15, c33, c35, c55);
+                        if (VTI) qp_factors(dzr, dxr, s, p.kc.dx, p.kc.dz, c11, c13, c15, c33, c35, c55, fS, f11, f13);
                     }
                     Sq[idx] = out;
                     if (VTI) {

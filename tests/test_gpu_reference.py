@@ -159,3 +159,33 @@ def test_random_tiny_cases_bitwise(oracle, engine_lib, cuda):
         e.close()
     print(f"random tiny cases differing from the reference kernels: {bad} of 160")
     assert bad == 0
+
+
+def test_anisotropic_config3_full_grid_matches_reference_kernels(oracle, engine_lib, cuda):
+    """The 1601 x 401 VTI workload (1607 x 407 padded), one shot, against the
+    reference's own two-pass kernels on every node; the FP64 anisotropic
+    oracle gives the error of both FP32 fields."""
+    ref = _ref()
+    from seisfat2d_gb300 import Engine
+    from seisfat2d_gb300.synthetic import config3
+    w = config3()
+    S = oracle.expand_boundary(w.slowness)
+    codes, mm = [], []
+    for c in w.cij:
+        cd, mn, mx = oracle.compress(oracle.expand_boundary(c))
+        codes.append(cd)
+        mm += [mn, mx]
+    mm = np.array(mm, np.float32)
+    sx, sz = float(w.shots[50][0]), float(w.shots[50][1])
+    Tr, ms_ref = ref.solve(S, w.dx, w.dz, sx, sz, ani=(codes, mm))
+    e = Engine(w.nx, w.nz, w.dx, w.dz)
+    e.set_slowness(w.slowness)
+    e.set_stiffness_codes(codes, mm)
+    T = e.time_propagation(sx, sz, ani=True)
+    T64 = oracle.shot_ani_f64(S, w.dx, w.dz, sx, sz, (codes, mm))
+    inner = (slice(3, -3), slice(3, -3))
+    er = rel_err(T[inner], T64[inner])
+    print(f"\nVTI 1607x407 shot at x={sx:.1f} m: nodes equal to the reference kernels {np.mean(T == Tr):.6f} "
+          f"(reference solver {ms_ref:.1f} ms); vs the FP64 oracle: max rel {er.max():.2e}, "
+          f"RMS {np.sqrt(np.mean(er ** 2)):.2e}")
+    assert np.array_equal(T, Tr)

@@ -28,7 +28,7 @@ def vti_case(oracle, nx=64, nz=34, seed=5):
     return m, codes, np.array(mm, np.float32)
 
 
-@pytest.mark.parametrize("arith", ["ieee", "reference"])
+@pytest.mark.parametrize("arith", ["ieee", "reference", "compensated"])
 def test_vti_gradient_bitexact_vs_oracle(oracle, engine_lib, cuda, arith):
     from seisfat2d_gb300 import Engine
     m, codes, mm = vti_case(oracle)
