@@ -153,6 +153,21 @@ int sf_batch_misfit_gradient(sf_ctx* ctx, const float* t_obs, int obs_mem, doubl
 /* Waits for `stream` and reports in-kernel failures (SF_ERR_TIMEOUT). */
 int sf_synchronize(sf_ctx* ctx, void* stream);
 
+/* Failure detection (no counterpart in the reference, which checks no CUDA
+ * errors). Every in-kernel wait (a strip waiting for the strip above it, a
+ * gang barrier, a gather tile waiting for its shots) gives up after
+ * `seconds` (0: the default of about 2 s; at most 60), raises the launch's
+ * error flag and lets every other wait of the launch return at once, so the
+ * kernel always finishes; the call that reads the flag returns
+ * SF_ERR_TIMEOUT, the launch's results are void, and the context stays
+ * usable. Applies to launches configured after the call. */
+int sf_set_wait_limit(sf_ctx* ctx, double seconds);
+/* Test of that path: in the next sf_batch_forward / sf_time_propagation
+ * launch only, every strip waits for a handoff tag that no strip writes, so
+ * each wait runs into the limit. Nothing else changes; later launches are
+ * unaffected. */
+int sf_test_stall_next_batch(sf_ctx* ctx);
+
 /* FP32 arithmetic of the solves. SF_ARITH_REFERENCE reproduces the
  * reference build of inner_sweep/time_init (modeling.cu:293-357 compiled by
  * nvcc with its default FMA contraction): FP32 initialisation and fused

@@ -22,7 +22,7 @@ def build(force=False):
     ):
         return LIB
     cmd = [
-        "gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp",
+        "gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp",
         "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing",
         SRC, "-o", LIB + ".tmp", "-lm",
     ]

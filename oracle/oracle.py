@@ -602,3 +602,25 @@ def shot_ani_f64(S, dx, dz, sx, sz, ani, nb=3, c0=0, ncols=None):
     if lib().orc_shot_ani_f64(nzz, nxx, nb, S, dx, dz, c0, ncols, sx, sz, arr, _f32(ani[1]), T) != 0:
         raise ValueError("source outside the window")
     return T
+
+
+def fp64_misfit_gradients(S, dx, dz, shots, rx, rz, t_obs, follow=None, nb=3):
+    """FP64 adjoint-state gradients of the FP64 misfit 0.5 sum (p - t_obs)^2
+    (p the FP64 picks) of a batch of shot windows, summed in shot order onto
+    the padded grid (nxx, nzz): the FP64 solves take their own branches, or
+    with follow (one code array (4, ncols, nzz) per shot, e.g. an FP32
+    engine's sf_batch_tape_codes) the branches those codes name."""
+    S = _f32(S)
+    nxx, nzz = S.shape
+    g = np.zeros((nxx, nzz))
+    tobs = np.asarray(t_obs, np.float64).reshape(len(shots), len(rx))
+    for b, s in enumerate(shots):
+        c0 = int(s[2]) if len(s) > 2 else 0
+        nc = int(s[3]) if len(s) > 3 and s[3] > 0 else nxx - c0
+        T, code, c1, c2, sIdz, sloc = solve_tape(S, dx, dz, s[0], s[1], nb, c0, nc, fp64=True,
+                                                 follow=None if follow is None else follow[b])
+        p = picks_f64(T, dx, dz, rx, rz, nb, c0)
+        lam = seed_lambda(nc, nzz, dx, dz, rx, rz, p - tobs[b], c0, nb, fp64=True)
+        gb, _ = adjoint((code, c1, c2, sIdz, sloc), lam, init_dist(s[0], s[1], dx, dz, nb), fp64=True)
+        g[c0:c0 + nc] += gb
+    return g

@@ -56,6 +56,8 @@ SIGNATURES = {
     "sf_batch_misfit_gradient": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_double), VP, C.c_int, VP]),
     "sf_batch_stiffness_gradient": (C.c_int, [VP, VP, VP, C.c_int, VP]),
     "sf_synchronize": (C.c_int, [VP, VP]),
+    "sf_set_wait_limit": (C.c_int, [VP, C.c_double]),
+    "sf_test_stall_next_batch": (C.c_int, [VP]),
     "sf_set_launch": (C.c_int, [VP, C.c_int, C.c_int]),
     "sf_set_arithmetic": (C.c_int, [VP, C.c_int]),
     "sf_get_arithmetic": (C.c_int, [VP, IP]),

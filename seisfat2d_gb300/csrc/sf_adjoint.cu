@@ -212,6 +212,7 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     p.nrec = c->batch_nrec;
     p.lam_init = c->d_lam_init;
     p.err = c->d_flags + 1;
+    p.wait_ns = c->wait_ns;
     {
         const int nn = c->seed_nodes, ne = c->seed_entries;
         p.nseed = nn;
@@ -236,6 +237,7 @@ int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A)
     g.tcode = c->d_tcode;
     g.vrec = c->d_tc2;
     g.lam_init = c->d_lam_init;
+    g.wait_ns = c->wait_ns;
     if (c->batch_ani) {
         const size_t npad = (size_t)c->nzz * c->nxx;
         rc = sf_dev_reserve(c, (void**)&c->d_gcij, &c->cap_gcij, 2 * npad * sizeof(float));

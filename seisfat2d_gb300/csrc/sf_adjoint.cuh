@@ -312,7 +312,10 @@ __device__ void adjoint_body(const AdjParams& p, const FuseParams* f)
     unsigned long long* hb = p.hand + (size_t)gp.gang * 4 * nstrips * 2 * p.maxcols;
     unsigned* bar = p.bar + gp.gang;
     unsigned nbar = 0;
-    if (tid == 0) cs->abort_flag = 0;
+    if (tid == 0) {
+        cs->abort_flag = 0;
+        cs->wait_ns = p.wait_ns ? p.wait_ns : kSpinNs;
+    }
     __syncthreads();
     int it = 0;
 #pragma unroll 1
@@ -481,15 +484,16 @@ __device__ __forceinline__ void cp_async16_cg(void* smem, const void* gmem)
 
 // Bounded wait of one thread until *p >= target (acquire); false after the
 // limit, with the error flag set.
-__device__ __forceinline__ bool wait_count(const unsigned* p, unsigned target, int* err)
+__device__ __forceinline__ bool wait_count(const unsigned* p, unsigned target, int* err, unsigned long long wait_ns)
 {
     if (ld_acquire_gpu(p) >= target) return true;
     const unsigned long long t0 = global_ns();
+    const unsigned long long lim = wait_ns ? wait_ns : kSpinNs;
     long long n = 0;
     while (ld_acquire_gpu(p) < target) {
         if (*(volatile int*)err) return false;
         __nanosleep(256);
-        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > kSpinNs)) {
+        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > lim)) {
             atomicExch(err, 2);
             return false;
         }
@@ -591,7 +595,7 @@ __device__ bool gather_tile(const GatherParams& p, GatherSmem& sm, int k, int cb
             if (FUSED && sw == 3 && tid == 0) {
                 // the shot's initialisation term is written when its reverse sweeps end
                 const bool src = t.sIdz + 1 >= rb && t.sIdz - 1 < rb + 32 && t.sIdx + 1 >= c && t.sIdx - 1 < c + kGT;
-                if (src && !wait_count(p.shot_done + t.orig, p.done_tag, p.err)) ok = false;
+                if (src && !wait_count(p.shot_done + t.orig, p.done_tag, p.err, p.wait_ns)) ok = false;
             }
             __syncthreads();
             const bool szpos = !(sw == 1 || sw == 3), sxpos = sw < 2;
@@ -733,8 +737,8 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) k_adjoint_gather(AdjParams 
                 // reverse sweep finishes them
                 const int k = p.nstrips - 1 - t / f.nblk, cb = f.nblk - 1 - t % f.nblk;
                 const unsigned cover = (unsigned)(g.blk_ptr[cb + 1] - g.blk_ptr[cb]);
-                ok = wait_count(f.ready + (size_t)k * f.nblk + cb, cover, g.err);
-                if (ok && k + 1 < p.nstrips) ok = wait_count(f.ready + (size_t)(k + 1) * f.nblk + cb, cover, g.err);
+                ok = wait_count(f.ready + (size_t)k * f.nblk + cb, cover, g.err, g.wait_ns);
+                if (ok && k + 1 < p.nstrips) ok = wait_count(f.ready + (size_t)(k + 1) * f.nblk + cb, cover, g.err, g.wait_ns);
             }
             tile_s = t;
             ok_s = ok;

@@ -16,6 +16,7 @@ struct AdjParams {
     unsigned long long* hand;  // per gang [4][nstrips][2 * maxcols] tagged (pv, pev) pairs
     unsigned* bar;          // per gang barrier counter
     unsigned epoch;         // launch number (tags)
+    unsigned long long wait_ns;  // time limit of the bounded waits
     uint8_t* tcode;
     float* tc1;
     float* tc2;
@@ -69,6 +70,7 @@ struct GatherParams {
     const unsigned* shot_done;
     unsigned done_tag;
     int* err;
+    unsigned long long wait_ns;  // time limit of the bounded waits
 };
 
 // The reverse sweeps and the gather in one launch: CTAs [0, nadj) run the

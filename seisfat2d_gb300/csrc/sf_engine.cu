@@ -225,6 +225,22 @@ extern "C" int sf_set_launch(sf_ctx* c, int warps, int gang_warps)
     return SF_OK;
 }
 
+extern "C" int sf_set_wait_limit(sf_ctx* c, double seconds)
+{
+    if (!c) return SF_ERR_ARG;
+    if (!(seconds >= 0.0 && seconds <= 60.0)) return sf_fail(c, SF_ERR_ARG, "wait limit must be in [0, 60] s");
+    c->wait_ns = (unsigned long long)(seconds * 1e9);  // 0: the default of about 2 s
+    c->plan_dirty = true;
+    return SF_OK;
+}
+
+extern "C" int sf_test_stall_next_batch(sf_ctx* c)
+{
+    if (!c) return SF_ERR_ARG;
+    c->stall_next = true;
+    return SF_OK;
+}
+
 extern "C" int sf_set_arithmetic(sf_ctx* c, int mode)
 {
     if (!c) return SF_ERR_ARG;
@@ -686,6 +702,7 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     p.Tlpool = comp ? c->d_Tl : nullptr;
     p.t_per_gang = t_per_gang;
     p.err = c->d_flags + 1;          // flags[1]: error flag
+    p.wait_ns = c->wait_ns;
     p.hand = c->d_hand;
     p.bar = c->d_ctr;
     p.ani = ani;
@@ -753,6 +770,8 @@ int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tabl
 {
     FwdLaunch L;
     int rc = sf_fwd_configure(c, ani, nrec, keep_tables, tape, gang_warps, st, &L);
+    L.p.stall_handoff = c->stall_next ? 1 : 0;  // sf_test_stall_next_batch
+    c->stall_next = false;
     if (!rc) rc = sf_fwd_enqueue(c, L, d_picks, sf_next_epoch(c), st);
     if (rc) return rc;
     c->tables_valid = keep_tables;

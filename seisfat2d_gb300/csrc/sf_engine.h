@@ -56,6 +56,8 @@ struct sf_ctx {
     unsigned* d_fuse = nullptr; size_t cap_fuse = 0;
     bool batch_interior = false;  // the last batch's forward ran the interior-block body
     int arith = SF_ARITH_REFERENCE;
+    unsigned long long wait_ns = 0;  // limit of the in-kernel waits (0: default, about 2 s)
+    bool stall_next = false;          // sf_test_stall_next_batch
     std::string err;
 
     float* d_S = nullptr;       // padded slowness

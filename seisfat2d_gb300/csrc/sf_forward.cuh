@@ -37,6 +37,8 @@ struct FwdParams {
     unsigned long long* hand;  // tagged strip handoff pairs: per gang [4 sweeps][nstrips][maxcols] (x2 compensated)
     unsigned* bar;        // per gang barrier counter
     unsigned epoch;       // launch number (tags: epoch << 10 | shot-solve number)
+    unsigned long long wait_ns;  // time limit of the bounded waits
+    int stall_handoff;    // test of the timeout path: consumers wait for a tag no producer writes
     // anisotropy
     int ani;
     const uint16_t* cij[6];
@@ -132,6 +134,7 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
     a.tc1 = nullptr;
     a.tc2 = nullptr;
     a.tag = tag;
+    a.tag_in = p.stall_handoff ? 1u : tag;  // epoch 0 is never used, zeroed pairs carry tag 0
 #pragma unroll 1
     for (int sw = 0; sw < 4; sw++) {
         const bool szpos = !(sw == 1 || sw == 3);
@@ -192,7 +195,10 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
     const int nstrips = (nzz + 31) >> 5;
     unsigned* bar = p.bar + gp.gang;
     unsigned nbar = 0;
-    if (tid == 0) cs->abort_flag = 0;
+    if (tid == 0) {
+        cs->abort_flag = 0;
+        cs->wait_ns = p.wait_ns ? p.wait_ns : kSpinNs;
+    }
     __syncthreads();
     const int nsolves = p.ani ? 2 : 1;
     int it = 0;

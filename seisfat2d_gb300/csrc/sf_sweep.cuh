@@ -64,7 +64,7 @@ constexpr int kMaxWarpsComp = 8;
 // faster on the headline batch; the other kernels measured slower that way)
 constexpr int kMaxWarpsTapedInterior = 8;
 constexpr long long kSpinLimit = 1ll << 30;          // iterations
-constexpr unsigned long long kSpinNs = 2000000000ull;  // and at most ~2 s
+constexpr unsigned long long kSpinNs = 2000000000ull;  // and at most ~2 s (default; sf_set_wait_limit)
 
 struct WarpRing {
     float S[kRing * kSP];
@@ -87,6 +87,7 @@ constexpr size_t ring_bytes() { return COMP ? sizeof(WarpRingC) : sizeof(WarpRin
 struct CtaShared {
     int abort_flag;
     int item;
+    unsigned long long wait_ns;  // time limit of every bounded wait of the CTA
     float init[9];
 };
 
@@ -156,6 +157,7 @@ struct StripArgs {
     const unsigned long long* h_in;  // {value, tag} of the upwind strip's row by march column (nullptr: first strip)
     unsigned long long* h_out;       // pairs this strip feeds to the next one (nullptr: last strip)
     unsigned tag;                    // tag of this shot's pairs
+    unsigned tag_in;                 // tag a consumer waits for (= tag; 1, which no launch writes, to test the timeout path)
     // tape (TAPE only): base of this sweep/strip, entries [step*32 + lane]
     uint8_t* tcode;
     float* tc1;
@@ -181,7 +183,7 @@ __device__ __forceinline__ float wait_pair(const unsigned long long* p, unsigned
     while (tag_of(e = ld_relaxed_u64(p)) != tag) {
         if (ld_volatile(&sh->abort_flag) || *(volatile int*)err) return 0.0f;
         __nanosleep(32);
-        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > kSpinNs)) {
+        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > sh->wait_ns)) {
             st_volatile(&sh->abort_flag, 1);
             atomicExch(err, 2);
             return 0.0f;
@@ -204,7 +206,7 @@ __device__ __forceinline__ unsigned wait_counter(const unsigned* p, unsigned tar
     while ((v = ld_acquire_gpu(p)) < target) {
         if (ld_volatile(&sh->abort_flag) || *(volatile int*)err) return target;
         __nanosleep(64);
-        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > kSpinNs)) {
+        if (++n > kSpinLimit || ((n & 255) == 0 && global_ns() - t0 > sh->wait_ns)) {
             st_volatile(&sh->abort_flag, 1);
             atomicExch(err, 2);
             return target;
@@ -288,7 +290,7 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
     // let the previous strip get kAhead columns ahead before the first
     // prefetches of its values
-    if (consumer) wait_pair(a.h_in + HS * min(kAhead, ncols - 1), a.tag, sh, a.err);
+    if (consumer) wait_pair(a.h_in + HS * min(kAhead, ncols - 1), a.tag_in, sh, a.err);
     __syncwarp();
 
     // prologue: march columns 0 .. kLook-1
@@ -349,10 +351,10 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 #pragma unroll
             for (int u = 0; u < kU; u++) {
                 const int s = s0 + u;
-                if ((FAST || s < ncols) && (tag_of(pr[u]) != a.tag || (COMP && tag_of(prl[u]) != a.tag))) {
-                    pr[u] = pack_tag(wait_pair(a.h_in + HS * s, a.tag, sh, a.err), a.tag);
-                    if (COMP) prl[u] = pack_tag(wait_pair(a.h_in + HS * s + 1, a.tag, sh, a.err), a.tag);
-                    wait_pair(a.h_in + HS * min(s + kAhead, ncols - 1), a.tag, sh, a.err);
+                if ((FAST || s < ncols) && (tag_of(pr[u]) != a.tag_in || (COMP && tag_of(prl[u]) != a.tag_in))) {
+                    pr[u] = pack_tag(wait_pair(a.h_in + HS * s, a.tag_in, sh, a.err), a.tag_in);
+                    if (COMP) prl[u] = pack_tag(wait_pair(a.h_in + HS * s + 1, a.tag_in, sh, a.err), a.tag_in);
+                    wait_pair(a.h_in + HS * min(s + kAhead, ncols - 1), a.tag_in, sh, a.err);
                 }
             }
         }

@@ -421,6 +421,15 @@ class Engine:
     def synchronize(self, stream=None):
         self._check(self.L.sf_synchronize(self._ctx, _stream_ptr(stream)), "sf_synchronize")
 
+    def set_wait_limit(self, seconds):
+        """Time limit of the in-kernel waits (0: the default, about 2 s)."""
+        self._check(self.L.sf_set_wait_limit(self._ctx, float(seconds)), "sf_set_wait_limit")
+
+    def test_stall_next_batch(self):
+        """Test of the timeout path: the next forward launch's strips wait for
+        a handoff tag nothing writes (sf_test_stall_next_batch)."""
+        self._check(self.L.sf_test_stall_next_batch(self._ctx), "sf_test_stall_next_batch")
+
     ARITHMETICS = {"reference": _lib.SF_ARITH_REFERENCE, "ieee": _lib.SF_ARITH_IEEE,
                    "compensated": _lib.SF_ARITH_COMPENSATED}
 

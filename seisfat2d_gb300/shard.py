@@ -22,13 +22,22 @@ def shard_indices(n, rank, world):
 
 
 def allreduce_gradient(grad, misfit=None, group=None):
-    """Sum of every rank's (grad, misfit) in FP64, rank order; returns
-    (grad_sum float64 numpy array, misfit_sum or None). Uses
-    torch.distributed (any backend; gloo on CPU tensors)."""
+    """Sum of every rank's (grad, misfit) in FP64, in rank order.
+
+    grad: a torch tensor on the device the process group communicates on
+    (CUDA under NCCL, CPU under gloo), or a numpy array (gathered as a CPU
+    tensor, for gloo). misfit: None, a number or a one-element tensor on the
+    same device. Each rank's partial is gathered as it is (no host copy of
+    device tensors) and the partials are added elementwise in rank order in
+    FP64, so every rank gets the same bits whatever the backend's reduction
+    order. Returns (sum, misfit_sum): a float64 tensor on grad's device (a
+    numpy array for numpy input) and, with misfit, a one-element float64
+    tensor on that device (a float for numpy input or a number)."""
     import torch
     import torch.distributed as dist
     world = dist.get_world_size(group)
-    t = torch.as_tensor(np.ascontiguousarray(grad), dtype=torch.float64).cpu()
+    as_numpy = not isinstance(grad, torch.Tensor)
+    t = (torch.from_numpy(np.ascontiguousarray(grad)) if as_numpy else grad).to(torch.float64).contiguous()
     parts = [torch.empty_like(t) for _ in range(world)]
     dist.all_gather(parts, t, group=group)
     total = parts[0].clone()
@@ -36,10 +45,14 @@ def allreduce_gradient(grad, misfit=None, group=None):
         total += p
     msum = None
     if misfit is not None:
-        m = torch.tensor([float(misfit)], dtype=torch.float64)
+        m_is_tensor = isinstance(misfit, torch.Tensor)
+        m = (misfit.reshape(1) if m_is_tensor else torch.tensor([float(misfit)], dtype=torch.float64))
+        m = m.to(torch.float64).to(t.device)
         ms = [torch.empty_like(m) for _ in range(world)]
         dist.all_gather(ms, m, group=group)
-        msum = 0.0
-        for x in ms:
-            msum += float(x.item())
-    return total.numpy(), msum
+        msum = ms[0].clone()
+        for x in ms[1:]:
+            msum += x
+        if as_numpy or not m_is_tensor:
+            msum = float(msum.item())
+    return (total.numpy() if as_numpy else total), msum

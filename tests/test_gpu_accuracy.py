@@ -125,24 +125,6 @@ def config4_gradient_case(oracle, nshots=2, seed=44):
     return w, shots, tobs
 
 
-def fp64_gradients(oracle, S, w, shots, tobs, codes):
-    """FP64 misfit gradients: branches of its own, and following `codes`."""
-    nxx, nzz = S.shape
-    out = []
-    for follow in (None, codes):
-        g = np.zeros((nxx, nzz))
-        for b, s in enumerate(shots):
-            T, code, c1, c2, sIdz, sloc = oracle.solve_tape(S, w.dx, w.dz, s[0], s[1], fp64=True,
-                                                            follow=None if follow is None else follow[b])
-            p = oracle.picks_f64(T, w.dx, w.dz, w.rx, w.rz)
-            lam = oracle.seed_lambda(nxx, nzz, w.dx, w.dz, w.rx, w.rz, p - tobs[b], fp64=True)
-            gb, _ = oracle.adjoint((code, c1, c2, sIdz, sloc), lam, oracle.init_dist(s[0], s[1], w.dx, w.dz),
-                                   fp64=True)
-            g += gb
-        out.append(g)
-    return out
-
-
 @pytest.mark.parametrize("arith", ["compensated", "reference"])
 def test_gradient_config4_vs_fp64_and_finite_differences(oracle, engine_lib, cuda, arith):
     from seisfat2d_gb300 import Engine
@@ -156,7 +138,8 @@ def test_gradient_config4_vs_fp64_and_finite_differences(oracle, engine_lib, cud
     codes = [e.tape_codes(b, nxx) for b in range(len(shots))]  # before the adjoint consumes the tape
     J, g32 = e.misfit_gradient(tobs.astype(np.float32))
     g32 = g32.astype(np.float64)
-    g64, gsb = fp64_gradients(oracle, S, w, shots, tobs, codes)
+    g64 = oracle.fp64_misfit_gradients(S, w.dx, w.dz, shots, w.rx, w.rz, tobs)
+    gsb = oracle.fp64_misfit_gradients(S, w.dx, w.dz, shots, w.rx, w.rz, tobs, follow=codes)
     rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     e_ind, e_sb, e_ties = rl(g32, g64), rl(g32, gsb), rl(gsb, g64)
     # 32 seeded cells with a gradient above 1% of the largest

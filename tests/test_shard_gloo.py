@@ -1,7 +1,9 @@
 """Shot sharding over two ranks (gloo on CPU, no GPU): the ranks' shards
 cover every shot once, and the rank-ordered FP64 reduction of the shard
 gradients (oracle FP32 batch gradients) equals the one-process gradient of
-the whole batch to FP32 rounding, with identical picks per shot."""
+the whole batch to FP32 rounding, with identical picks per shot; the
+reduction gives the same bits for numpy input and for tensors (the form the
+bench's multi-GPU step passes, there as device tensors)."""
 import os
 import socket
 
@@ -39,6 +41,12 @@ def _rank(rank, world, port, outdir):
         mine = shard(shots, rank, world)
         J, g, pk, _ = O.batch_misfit_gradient(Sp, 10.0, 10.0, mine, rx, rz, tobs[idx], nthreads=1)
         gsum, Jsum = allreduce_gradient(g, J)
+        # the engine's calling convention: the gradient and the misfit as tensors
+        # (device tensors under NCCL; CPU tensors here under gloo), no host copy
+        import torch
+        gt, Jt = allreduce_gradient(torch.from_numpy(g), torch.tensor([J], dtype=torch.float64))
+        assert isinstance(gt, torch.Tensor) and gt.dtype == torch.float64
+        assert np.array_equal(gt.numpy(), gsum) and float(Jt.item()) == Jsum
         np.save(os.path.join(outdir, f"r{rank}.npy"), pk)
         np.save(os.path.join(outdir, f"idx{rank}.npy"), np.array(idx))
         if rank == 0:
