@@ -566,6 +566,8 @@ def measure(cfg, a, env, arith, full, steps, warmup):
     peak, peak_kind = load_peaks()
     fwd_bpc = BYTES_PER_CELL_FWD_ANI if ani else BYTES_PER_CELL_FWD
     kname = "k_shots_tape" if fa else ("k_shots_ani" if ani else "k_shots")
+    if arith == "compensated":
+        kname += "_comp"  # its own capture (the lo parts add window traffic); absent ones give no traffic
     stages = {"forward": {"kernel": "sf::k_shots<tape>" if fa else "sf::k_shots", "ms": kt["forward"],
                           "algorithmic_bytes": fwd_bpc * cells, "traffic_file": f"{kname}_cfg{cfg}.txt"}}
     if fa and "gather" in kt:

@@ -43,8 +43,10 @@ void Modeling::create_engine()
 {
     if (ctx) return;
     sf_check(sf_ctx_create(&ctx, nx, nz, dx, dz, 0), nullptr, "sf_ctx_create");
+    // eikonal_arithmetic = reference (default) | ieee | compensated (sf_set_arithmetic)
     std::string arith = catch_parameter("eikonal_arithmetic", parameters);
     if (arith == "ieee") sf_check(sf_set_arithmetic(ctx, SF_ARITH_IEEE), ctx, "sf_set_arithmetic");
+    if (arith == "compensated") sf_check(sf_set_arithmetic(ctx, SF_ARITH_COMPENSATED), ctx, "sf_set_arithmetic");
 }
 
 void Modeling::set_geometry()

@@ -40,6 +40,31 @@ def test_modeling_exe_matches_oracle(oracle, cuda, exes, tmp_path, batch):
         oracle.set_arith("ieee")
 
 
+def test_modeling_exe_compensated_arithmetic(oracle, cuda, exes, tmp_path):
+    """parameters.txt `eikonal_arithmetic = compensated`: the driver's picks
+    equal the oracle's compensated restatement bit for bit."""
+    nx, nz, dx, dz = 90, 50, 10.0, 10.0
+    m = smooth_model(nx, nz, dx, seed=19, noise=0.02)
+    shots = [(150.0, 0.0), (620.0, 35.0)]
+    recs = [(float(x), 10.0) for x in range(0, 890, 20)]
+    p = write_case(str(tmp_path), nx, nz, dx, dz, m, shots, recs, batch=True)
+    with open(p, "a") as f:
+        f.write("eikonal_arithmetic = compensated\n")
+    run(exes["modeling.exe"], p)
+    oracle.set_arith("compensated")
+    try:
+        S = oracle.expand_boundary(m)
+        rx = np.array([r[0] for r in recs], np.float32)
+        rz = np.array([r[1] for r in recs], np.float32)
+        for k, (sx, sz) in enumerate(shots):
+            out = np.fromfile(os.path.join(str(tmp_path), f"out_eikonal_iso_nStations{len(recs)}_shot_{k + 1}.bin"),
+                              np.float32)
+            _, po = oracle.shot(S, dx, dz, sx, sz, rx, rz)
+            assert np.array_equal(out, po, equal_nan=True)
+    finally:
+        oracle.set_arith("ieee")
+
+
 def test_modeling_exe_anisotropic(oracle, cuda, exes, tmp_path):
     from seisfat2d_gb300.synthetic import thomsen_stiffness
     nx, nz, dx, dz = 60, 30, 10.0, 10.0
