@@ -196,8 +196,8 @@ int sf_get_arithmetic(const sf_ctx* ctx, int* mode);
  * static device array of about 8 MiB that every GPU loading the library
  * holds until exit: grids with ceil(nzz/32) * nxx > 262144 are rejected with
  * SF_ERR_RANGE. The first call on a device sets that device up (looks up the
- * array's device address, sets the kernel's shared-memory limit); make it
- * before any stream capture. The first call with new cell sizes (dx, dz) on
+ * array's device address, sets the kernel's shared-memory limit). The first
+ * call with new cell sizes (dx, dz) on
  * a device also checks the node update's fast division for them, in the
  * array, and waits for that check. Calls share the array: calls that
  * overlap on the GPU (other streams, other threads) race and must be
