@@ -134,9 +134,10 @@ __global__ void k_picks(const float* __restrict__ T, int nzz, int ncols, int c0,
 
 }  // namespace
 
-size_t sf_fwd_smem_bytes(int warps, bool comp)
+size_t sf_fwd_smem_bytes(int warps, bool comp, bool taped_iso)
 {
-    return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * (comp ? sizeof(WarpRingC) : sizeof(WarpRing));
+    const int slots = taped_iso ? FwdBlock<true>::RING : FwdBlock<false>::RING;
+    return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * (comp ? ring_bytes<true>(slots) : ring_bytes<false>(slots));
 }
 
 // ------------------------------------------------------------------ context
@@ -410,7 +411,7 @@ int sf_fwd_setup(sf_ctx* c)
 {
     for (int k = 0; k < 32; k++) {
         const bool comp = k & 1;
-        const size_t mx = comp ? sf_fwd_smem_bytes(kMaxWarpsComp, true) : sf_fwd_smem_bytes(kMaxWarps, false);
+        const size_t mx = comp ? sf_fwd_smem_bytes(kMaxWarpsComp, true, false) : sf_fwd_smem_bytes(kMaxWarps, false, false);
         const void* f = sf_kshots_kernel(k & 16, k & 8, k & 4, k & 2, comp);
         if (f) CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
     }
@@ -628,9 +629,9 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     const bool comp = c->arith == SF_ARITH_COMPENSATED;
     if (comp && c->warps > kMaxWarpsComp)
         return sf_fail(c, SF_ERR_ARG, "the compensated arithmetic runs at most 8 warps per CTA (sf_set_launch)");
-    const size_t smem = sf_fwd_smem_bytes(c->warps, comp);
     const bool ref = c->arith == SF_ARITH_REFERENCE;
     const bool vti = tape && ani;
+    const size_t smem = sf_fwd_smem_bytes(c->warps, comp, tape && !vti);
     const void* kern = sf_kshots_kernel(tape, ref, vti, false, comp);
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);

@@ -167,7 +167,7 @@ unsigned sf_next_epoch(sf_ctx* c);
 int sf_check_flags(sf_ctx* c, cudaStream_t st);
 int sf_fwd_setup(sf_ctx* c);
 int sf_verify_divisors(sf_ctx* c);
-size_t sf_fwd_smem_bytes(int warps, bool comp);
+size_t sf_fwd_smem_bytes(int warps, bool comp, bool taped_iso);
 // k_shots instantiation (one object file each, sf_shots_inst.cu)
 const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior, bool comp);
 // whether the batch of hshots, G CTAs per shot, runs the interior-block body

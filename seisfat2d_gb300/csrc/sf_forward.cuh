@@ -109,7 +109,8 @@ __device__ __forceinline__ GangPos gang_pos(int G)
 // arithmetic, lo parts in Tl, two handoff pairs per column.
 template <bool TAPE, bool REF, bool INTERIOR, bool COMP>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPos& gp, const float* Sw,
-                             int ldS, float* T, float* Tl, unsigned tag, CtaShared* cs, unsigned char* rings)
+                             int ldS, float* T, float* Tl, unsigned tag, CtaShared* cs, unsigned char* rings,
+                             size_t ring_stride)
 {
     const int nzz = p.nzz, ncols = sh.ncols;
     const int nstrips = (nzz + 31) >> 5;
@@ -127,7 +128,7 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
     a.sIdx = sh.sIdx - sh.c0;
     a.kc = p.kc;
     a.init = cs->init;
-    a.ring = rings + (size_t)gp.warp * ring_bytes<COMP>();
+    a.ring = rings + (size_t)gp.warp * ring_stride;
     a.sh = cs;
     a.err = p.err;
     a.tcode = nullptr;
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
     unsigned char* rings = smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15));
+    constexpr size_t kRingStride = ring_bytes<COMP>(fwd_ring_slots<TAPE, VTI>());
     const int tid = threadIdx.x;
     const GangPos gp = gang_pos(p.G);
     const int nzz = p.nzz;
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
         const unsigned tag = (p.epoch << 10) | (unsigned)((it * nsolves) & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE && !VTI, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings);
+        solve_window<TAPE && !VTI, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings, kRingStride);
         // taped isotropic batches never set ani: their kernels carry no qP pass
         if ((!TAPE || VTI) && p.ani) {
             // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
                         __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
             }
             __syncthreads();
-            solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sq, nzz, T, Tl, tag + 1u, cs, rings);
+            solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sq, nzz, T, Tl, tag + 1u, cs, rings, kRingStride);
         }
         // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {

@@ -63,7 +63,7 @@ int noalloc_setup(int dev, unsigned char** addr)
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SF_ERR_CUDA;
         if (cudaFuncSetAttribute(sf_kshots_kernel(false, true, false, true, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sf_fwd_smem_bytes(kMaxWarps, false)) != cudaSuccess)
+                                 (int)sf_fwd_smem_bytes(kMaxWarps, false, false)) != cudaSuccess)
             return SF_ERR_CUDA;
         // the tagged pairs must not start with a valid-looking tag
         if (cudaMemset(p, 0, sizeof(g_noalloc_scratch)) != cudaSuccess) return SF_ERR_CUDA;
@@ -191,7 +191,7 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     const int warps = 8;
     void* args[] = {&p};
     if (cudaLaunchKernel(sf_kshots_kernel(false, true, false, true, false), dim3(1), dim3(warps * 32), args,
-                         sf_fwd_smem_bytes(warps, false), st) != cudaSuccess)
+                         sf_fwd_smem_bytes(warps, false, false), st) != cudaSuccess)
         return SF_ERR_CUDA;
     int err = 0;
     if (cudaMemcpyAsync(&err, &dh->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return SF_ERR_CUDA;

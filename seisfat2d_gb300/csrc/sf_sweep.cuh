@@ -38,19 +38,23 @@
 namespace sf {
 
 constexpr int kU = 4;       // march steps per block of the reverse sweeps' strip loop
-constexpr int kRing = 48;   // column slots per warp ring (a multiple of every block size, >= 32 + lead + block)
+constexpr int kRing = 48;   // column slots per warp ring of the reverse sweeps and the plain forward
 
-// Block size and staging lead (march columns, a multiple of the block) of a
-// forward strip loop: 4 and 8 for the plain solve; 2 and 4 for the taped one,
-// which keeps a tape record per step of the block in registers (measured
-// 19% faster than 4 and 8 there). After a stall a consumer lets its producer
-// get `lead` columns ahead (lead + block measured 1% slower).
+// Block size, staging lead (march columns, a multiple of the block) and ring
+// length of a forward strip loop: 4, 8 and 48 slots for the plain solve; 2,
+// 4 and 40 for the taped one, which keeps a tape record per step of the
+// block in registers (measured 19% faster than 4 and 8 there). After a stall
+// a consumer lets its producer get `lead` columns ahead (lead + block
+// measured 1% slower). The ring holds the 32 marches the lanes work on, the
+// lead and two blocks, so a block's prefetches never refill a slot that the
+// block before it still read: RING >= 31 + LOOK + 2 U.
 template <bool TAPE>
 struct FwdBlock {
     static constexpr int U = TAPE ? 2 : 4;
     static constexpr int LOOK = TAPE ? 4 : 8;
     static constexpr int AHEAD = LOOK;
-    static_assert(LOOK % U == 0 && kRing % U == 0 && kRing >= 32 + LOOK + U, "ring too small");
+    static constexpr int RING = TAPE ? 40 : 48;
+    static_assert(LOOK % U == 0 && RING % U == 0 && RING >= 31 + LOOK + 2 * U, "ring too small");
 };
 constexpr int kSP = 36;     // S slot pitch: rows rb-1 .. rb+31 at 0..32, handoff pair at 34..35
 constexpr int kSPc = 40;    // compensated: S slot pitch, handoff pairs {hi,tag},{lo,tag} at 36..39
@@ -66,23 +70,22 @@ constexpr int kMaxWarpsTapedInterior = 8;
 constexpr long long kSpinLimit = 1ll << 30;          // iterations
 constexpr unsigned long long kSpinNs = 2000000000ull;  // and at most ~2 s (default; sf_set_wait_limit)
 
-struct WarpRing {
-    float S[kRing * kSP];
-    float T[kRing * kTP];
-};
-
-// Ring of the compensated strip loop: S with two handoff pairs per slot, the
-// hi and the lo parts of the traveltimes.
-struct WarpRingC {
-    float S[kRing * kSPc];
-    float T[kRing * kTP];
-    float L[kRing * kTP];
-};
-
+// A warp's forward ring of R column slots: S (slot pitch kSP; compensated
+// kSPc, with the two handoff pairs of the hi and the lo parts), T, and in the
+// compensated arithmetic L (the lo parts of the traveltimes), one after the
+// other. Every size is a multiple of 16 bytes.
 template <bool COMP>
-constexpr size_t ring_bytes() { return COMP ? sizeof(WarpRingC) : sizeof(WarpRing); }
+constexpr size_t ring_bytes(int R)
+{
+    return sizeof(float) * (size_t)R * ((COMP ? kSPc : kSP) + (COMP ? 2 : 1) * kTP);
+}
+// Ring slots per warp of a forward kernel: the taped isotropic kernels run
+// only taped strip loops, every other kernel plain ones (the anisotropic
+// taped kernels also for their first solve).
+template <bool TAPE, bool VTI>
+constexpr int fwd_ring_slots() { return (TAPE && !VTI) ? FwdBlock<true>::RING : FwdBlock<false>::RING; }
 
-// Per-CTA shared state (static part), followed by the CTA's WarpRing blocks in
+// Per-CTA shared state (static part), followed by the CTA's warp rings in
 // dynamic shared memory.
 struct CtaShared {
     int abort_flag;
@@ -152,7 +155,7 @@ struct StripArgs {
     int skip_i, skip_j;
     Consts kc;
     const float* init;  // 9 values in shared memory
-    unsigned char* ring;  // this warp's WarpRing (WarpRingC when compensated)
+    unsigned char* ring;  // this warp's ring (ring_bytes<COMP>(FwdBlock<TAPE>::RING) bytes at least)
     CtaShared* sh;
     const unsigned long long* h_in;  // {value, tag} of the upwind strip's row by march column (nullptr: first strip)
     unsigned long long* h_out;       // pairs this strip feeds to the next one (nullptr: last strip)
@@ -225,6 +228,7 @@ template <int SZ, int SX, bool SW0, bool TAPE, bool REF, bool INTERIOR, bool SQ,
 __device__ __forceinline__ void run_strip(const StripArgs& a)
 {
     constexpr int kU = FwdBlock<TAPE>::U, kLook = FwdBlock<TAPE>::LOOK, kAhead = FwdBlock<TAPE>::AHEAD;
+    constexpr int kRing = FwdBlock<TAPE>::RING;
     const int lane = threadIdx.x & 31;
     const int nzz = a.nzz, ncols = a.ncols;
     const int rb = 32 * a.k;
@@ -239,9 +243,9 @@ __device__ __forceinline__ void run_strip(const StripArgs& a)
 
     constexpr int SP = COMP ? kSPc : kSP;    // S slot pitch
     constexpr int PQ = COMP ? 36 : 34;       // first handoff pair in an S slot
-    float* Sring = COMP ? reinterpret_cast<WarpRingC*>(a.ring)->S : reinterpret_cast<WarpRing*>(a.ring)->S;
-    float* Tring = COMP ? reinterpret_cast<WarpRingC*>(a.ring)->T : reinterpret_cast<WarpRing*>(a.ring)->T;
-    float* Lring = COMP ? reinterpret_cast<WarpRingC*>(a.ring)->L : nullptr;
+    float* Sring = reinterpret_cast<float*>(a.ring);
+    float* Tring = Sring + kRing * SP;
+    float* Lring = COMP ? Tring + kRing * kTP : nullptr;
     constexpr int HS = COMP ? 2 : 1;         // handoff pairs per column
 
     // global rows this lane stages
