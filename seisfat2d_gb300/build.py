@@ -22,11 +22,9 @@ NVCC_FLAGS = ARCH + [
 ]
 UNITS = ["sf_engine.cu", "sf_adjoint.cu", "sf_plan.cu", "sf_update.cu", "sf_migration.cu"]
 # k_shots instantiations, one object each from sf_shots_inst.cu: (tape,
-# reference arithmetic, anisotropic taped, interior-block strip loops,
-# compensated arithmetic)
-KSHOTS = [(0, 0, 0, 0, 0), (0, 0, 0, 1, 0), (0, 1, 0, 0, 0), (0, 1, 0, 1, 0), (1, 0, 0, 0, 0), (1, 0, 0, 1, 0),
-          (1, 1, 0, 0, 0), (1, 1, 0, 1, 0), (1, 0, 1, 0, 0), (1, 1, 1, 0, 0),
-          (0, 0, 0, 0, 1), (0, 0, 0, 1, 1), (1, 0, 0, 0, 1), (1, 0, 0, 1, 1), (1, 0, 1, 0, 1)]
+# reference arithmetic, interior-block strip loops, compensated arithmetic)
+KSHOTS = [(0, 0, 0, 0), (0, 0, 1, 0), (0, 1, 0, 0), (0, 1, 1, 0), (1, 0, 0, 0), (1, 0, 1, 0), (1, 1, 0, 0), (1, 1, 1, 0),
+          (0, 0, 0, 1), (0, 0, 1, 1), (1, 0, 0, 1), (1, 0, 1, 1)]
 
 
 def _jobs():
@@ -34,7 +32,7 @@ def _jobs():
     jobs = [(u, [], u.replace(".cu", ".o")) for u in UNITS]
     for v in KSHOTS:
         tag = "".join(str(b) for b in v)
-        defs = [f"-DSF_{k}={'true' if b else 'false'}" for k, b in zip(("TAPE", "REF", "VTI", "INTERIOR", "COMP"), v)]
+        defs = [f"-DSF_{k}={'true' if b else 'false'}" for k, b in zip(("TAPE", "REF", "INTERIOR", "COMP"), v)]
         jobs.append(("sf_shots_inst.cu", defs + [f"-DSF_KSHOTS_NAME=sf_kshots_{tag}"], f"sf_shots_{tag}.o"))
     return jobs
 

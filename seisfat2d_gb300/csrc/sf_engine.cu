@@ -134,9 +134,9 @@ __global__ void k_picks(const float* __restrict__ T, int nzz, int ncols, int c0,
 
 }  // namespace
 
-size_t sf_fwd_smem_bytes(int warps, bool comp, bool taped_iso)
+size_t sf_fwd_smem_bytes(int warps, bool comp, bool tape)
 {
-    const int slots = taped_iso ? FwdBlock<true>::RING : FwdBlock<false>::RING;
+    const int slots = tape ? FwdBlock<true>::RING : FwdBlock<false>::RING;
     return ((sizeof(CtaShared) + 15) & ~size_t(15)) + (size_t)warps * (comp ? ring_bytes<true>(slots) : ring_bytes<false>(slots));
 }
 
@@ -341,49 +341,49 @@ int sf_verify_divisors(sf_ctx* c)
 
 namespace sf {
 // accessors of the k_shots instantiations: tape, reference arithmetic,
-// anisotropic taped (VTI), interior-block body, compensated arithmetic
-const void* sf_kshots_00000();
-const void* sf_kshots_00010();
-const void* sf_kshots_01000();
-const void* sf_kshots_01010();
-const void* sf_kshots_10000();
-const void* sf_kshots_10010();
-const void* sf_kshots_11000();
-const void* sf_kshots_11010();
-const void* sf_kshots_10100();
-const void* sf_kshots_11100();
-const void* sf_kshots_00001();
-const void* sf_kshots_00011();
-const void* sf_kshots_10001();
-const void* sf_kshots_10011();
-const void* sf_kshots_10101();
+// interior-block body, compensated arithmetic
+const void* sf_kshots_0000();
+const void* sf_kshots_0010();
+const void* sf_kshots_0100();
+const void* sf_kshots_0110();
+const void* sf_kshots_1000();
+const void* sf_kshots_1010();
+const void* sf_kshots_1100();
+const void* sf_kshots_1110();
+const void* sf_kshots_0001();
+const void* sf_kshots_0011();
+const void* sf_kshots_1001();
+const void* sf_kshots_1011();
 }  // namespace sf
 
-// Anisotropic taped batches run the general loops only; the compensated
-// arithmetic has no reference-build variant.
-const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior, bool comp)
+// The compensated arithmetic has no reference-build variant.
+const void* sf_kshots_kernel(bool tape, bool ref, bool interior, bool comp)
 {
-    vti = vti && tape;
-    if (vti) interior = false;
     if (comp) ref = false;
-    switch (((int)tape << 4) | ((int)ref << 3) | ((int)vti << 2) | ((int)interior << 1) | (int)comp) {
-    case 0x00: return sf::sf_kshots_00000();
-    case 0x02: return sf::sf_kshots_00010();
-    case 0x08: return sf::sf_kshots_01000();
-    case 0x0a: return sf::sf_kshots_01010();
-    case 0x10: return sf::sf_kshots_10000();
-    case 0x12: return sf::sf_kshots_10010();
-    case 0x18: return sf::sf_kshots_11000();
-    case 0x1a: return sf::sf_kshots_11010();
-    case 0x14: return sf::sf_kshots_10100();
-    case 0x1c: return sf::sf_kshots_11100();
-    case 0x01: return sf::sf_kshots_00001();
-    case 0x03: return sf::sf_kshots_00011();
-    case 0x11: return sf::sf_kshots_10001();
-    case 0x13: return sf::sf_kshots_10011();
-    case 0x15: return sf::sf_kshots_10101();
+    switch (((int)tape << 3) | ((int)ref << 2) | ((int)interior << 1) | (int)comp) {
+    case 0x0: return sf::sf_kshots_0000();
+    case 0x2: return sf::sf_kshots_0010();
+    case 0x4: return sf::sf_kshots_0100();
+    case 0x6: return sf::sf_kshots_0110();
+    case 0x8: return sf::sf_kshots_1000();
+    case 0xa: return sf::sf_kshots_1010();
+    case 0xc: return sf::sf_kshots_1100();
+    case 0xe: return sf::sf_kshots_1110();
+    case 0x1: return sf::sf_kshots_0001();
+    case 0x3: return sf::sf_kshots_0011();
+    case 0x9: return sf::sf_kshots_1001();
+    case 0xb: return sf::sf_kshots_1011();
     default: return nullptr;
     }
+}
+
+// The qP pass kernels: arithmetic (reference / IEEE / compensated) x
+// derivative factors (taped batches).
+const void* sf_kqp_kernel(bool ref, bool comp, bool fact)
+{
+    if (comp) return fact ? (const void*)k_qp<false, true, true> : (const void*)k_qp<false, true, false>;
+    if (ref) return fact ? (const void*)k_qp<true, false, true> : (const void*)k_qp<true, false, false>;
+    return fact ? (const void*)k_qp<false, false, true> : (const void*)k_qp<false, false, false>;
 }
 
 // The interior-block body saves instructions per step but adds code. It
@@ -409,10 +409,10 @@ bool sf_interior_loops(sf_ctx* c, const void* kernel, size_t smem, int G)
 
 int sf_fwd_setup(sf_ctx* c)
 {
-    for (int k = 0; k < 32; k++) {
-        const bool comp = k & 1;
-        const size_t mx = comp ? sf_fwd_smem_bytes(kMaxWarpsComp, true, false) : sf_fwd_smem_bytes(kMaxWarps, false, false);
-        const void* f = sf_kshots_kernel(k & 16, k & 8, k & 4, k & 2, comp);
+    for (int k = 0; k < 16; k++) {
+        const bool tape = k & 8, comp = k & 1;
+        const size_t mx = sf_fwd_smem_bytes(comp ? kMaxWarpsComp : kMaxWarps, comp, tape);
+        const void* f = sf_kshots_kernel(tape, k & 4, k & 2, comp);
         if (f) CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
     }
     return sf_adj_setup(c);
@@ -557,7 +557,7 @@ void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4])
 
 // Builds the device shot table (sorted widest window first for the work
 // queue). Returns SF_ERR_RANGE for a source outside its window.
-int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape)
+int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool tape)
 {
     c->plan_valid = false;  // the planned batch's tables are replaced
     c->hshots.resize(nshots);
@@ -600,12 +600,12 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
             skip_cache.push_back({d.ncols, v});
         }
         d.orig = b;
-        d.t_off = toff;
-        if (keep_tables) toff += (long long)c->nzz * d.ncols;
+        d.t_off = toff;  // per-shot traveltime windows (tables, anisotropic batches)
+        toff += (long long)c->nzz * d.ncols;
         d.tape_off = tape_off;
         if (tape) tape_off += 4LL * nstrips * (d.ncols + 31) * 32;
         d.q_off = q_off;
-        if (tape) q_off += (long long)c->nzz * d.ncols;
+        q_off += (long long)c->nzz * d.ncols;
         maxcols = std::max(maxcols, d.ncols);
         c->hshots[b] = d;
     }
@@ -620,8 +620,13 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tabl
     return SF_OK;
 }
 
-int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, int gang_warps, cudaStream_t st,
-                     FwdLaunch* L)
+// One solve of every shot of the prepared batch: kernel, gang shape,
+// buffers, parameters. per_shot_T: every shot keeps its own traveltime window
+// (tables, anisotropic batches) instead of one window per gang. Sshots: the
+// shots' own slowness windows (the qP slowness of an anisotropic batch's
+// second solve), or nullptr for S.
+int sf_fwd_configure(sf_ctx* c, int nrec, bool per_shot_T, bool tape, int gang_warps, cudaStream_t st,
+                     FwdLaunch* L, const float* Sshots)
 {
     const int nshots = (int)c->hshots.size();
     const size_t nzz = c->nzz;
@@ -630,18 +635,17 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     if (comp && c->warps > kMaxWarpsComp)
         return sf_fail(c, SF_ERR_ARG, "the compensated arithmetic runs at most 8 warps per CTA (sf_set_launch)");
     const bool ref = c->arith == SF_ARITH_REFERENCE;
-    const bool vti = tape && ani;
-    const size_t smem = sf_fwd_smem_bytes(c->warps, comp, tape && !vti);
-    const void* kern = sf_kshots_kernel(tape, ref, vti, false, comp);
+    const size_t smem = sf_fwd_smem_bytes(c->warps, comp, tape);
+    const void* kern = sf_kshots_kernel(tape, ref, false, comp);
     int G, NG;
     int rc = sf_gang_shape(c, kern, smem, nshots, nstrips, gang_warps, &G, &NG);
     if (rc) return rc;
     // the interior-block kernels of taped batches are built for at most
     // kMaxWarpsTapedInterior warps per CTA; the gang shape must come from the
     // kernel that runs (every CTA of a gang resident at once)
-    c->batch_interior = !vti && !(tape && c->warps > kMaxWarpsTapedInterior) && sf_interior_loops(c, kern, smem, G);
+    c->batch_interior = !(tape && c->warps > kMaxWarpsTapedInterior) && sf_interior_loops(c, kern, smem, G);
     if (c->batch_interior) {
-        const void* ik = sf_kshots_kernel(tape, ref, vti, true, comp);
+        const void* ik = sf_kshots_kernel(tape, ref, true, comp);
         int Gi, NGi;
         rc = sf_gang_shape(c, ik, smem, nshots, nstrips, gang_warps, &Gi, &NGi);
         if (rc) return rc;
@@ -653,23 +657,19 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
             c->batch_interior = false;
         }
     }
-    if ((long long)(nshots + NG - 1) / NG * (ani ? 2 : 1) > 1023)
+    if ((long long)(nshots + NG - 1) / NG > 1023)
         return sf_fail(c, SF_ERR_ARG, "too many shots per gang for one launch; split the batch");
     c->last_G = G;
     c->last_NG = NG;
     rc = sf_dev_reserve(c, (void**)&c->d_shots, &c->cap_shots, nshots * sizeof(ShotDev));
     if (rc) return rc;
     CK(cudaMemcpyAsync(c->d_shots, c->hshots.data(), nshots * sizeof(ShotDev), cudaMemcpyHostToDevice, st));
-    const long long t_per_gang = keep_tables ? 0 : (long long)nzz * c->batch_maxcols;
-    const size_t tfloats = keep_tables ? (size_t)c->batch_T_floats : (size_t)NG * t_per_gang;
+    const long long t_per_gang = per_shot_T ? 0 : (long long)nzz * c->batch_maxcols;
+    const size_t tfloats = per_shot_T ? (size_t)c->batch_T_floats : (size_t)NG * t_per_gang;
     rc = sf_dev_reserve(c, (void**)&c->d_T, &c->cap_T, tfloats * sizeof(float));
     if (rc) return rc;
     if (comp) {
         rc = sf_dev_reserve(c, (void**)&c->d_Tl, &c->cap_Tl, tfloats * sizeof(float));
-        if (rc) return rc;
-    }
-    if (ani) {
-        rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)NG * nzz * c->batch_maxcols * sizeof(float));
         if (rc) return rc;
     }
     const size_t hand_bytes =
@@ -684,12 +684,12 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
         rc = sf_dev_reserve(c, (void**)&c->d_tcode, &c->cap_tcode, n);
         if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc1, &c->cap_tc1, n * sizeof(float));
         if (!rc) rc = sf_dev_reserve(c, (void**)&c->d_tc2, &c->cap_tc2, n * sizeof(float));
-        if (!rc && ani) rc = sf_dev_reserve(c, (void**)&c->d_vfac, &c->cap_vfac, 3 * (size_t)c->batch_q_cells * sizeof(float));
         if (rc) return rc;
     }
     FwdParams& p = L->p;
     std::memset(&p, 0, sizeof(p));
     p.S = c->d_S;
+    p.Sshots = Sshots;
     p.nzz = c->nzz;
     p.nxx = c->nxx;
     p.nb = c->nb;
@@ -706,22 +706,10 @@ int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, 
     p.wait_ns = c->wait_ns;
     p.hand = c->d_hand;
     p.bar = c->d_ctr;
-    p.ani = ani;
-    if (ani) {
-        const size_t npad = (size_t)c->nxx * c->nzz;
-        for (int q = 0; q < 6; q++) p.cij[q] = c->d_cij_all + q * npad;
-        std::memcpy(p.mm, c->mm, sizeof(p.mm));
-        p.Sq = c->d_Sq;
-        p.sq_per_gang = (long long)nzz * c->batch_maxcols;
-    }
     if (tape) {
         p.tcode = c->d_tcode;
         p.tc1 = c->d_tc1;
         p.tc2 = c->d_tc2;
-        if (ani) {
-            p.vfac = c->d_vfac;
-            p.vfac_total = c->batch_q_cells;
-        }
     }
     p.rx = c->d_rx;
     p.rz = c->d_rz;
@@ -750,7 +738,8 @@ int sf_kt_end(sf_ctx* c, int k, cudaStream_t st)
     return SF_OK;
 }
 
-int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st)
+// One forward launch (counters zeroed first), without the kernel timing.
+int sf_fwd_launch(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st)
 {
     L.p.picks = d_picks;
     L.p.epoch = epoch;
@@ -759,21 +748,84 @@ int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cuda
         CK(cudaMemsetAsync(c->d_hand, 0, c->cap_hand, st));
         c->hand_stale_f = false;
     }
-    int rc = sf_kt_begin(c, SF_KT_FORWARD, st);
-    if (rc) return rc;
     void* args[] = {&L.p};
     CK(cudaLaunchKernel(L.kern, L.grid, L.block, args, L.smem, st));
+    return SF_OK;
+}
+
+int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st)
+{
+    int rc = sf_kt_begin(c, SF_KT_FORWARD, st);
+    if (!rc) rc = sf_fwd_launch(c, L, d_picks, epoch, st);
+    if (rc) return rc;
     return sf_kt_end(c, SF_KT_FORWARD, st);
+}
+
+// The qP pass of the prepared anisotropic batch (k_qp) over the traveltime
+// windows of the first solves: the qP slowness windows into d_Sq, and with
+// `fact` the derivative factors into d_vfac.
+int sf_qp_launch(sf_ctx* c, bool fact, cudaStream_t st)
+{
+    QpParams q;
+    std::memset(&q, 0, sizeof(q));
+    q.S = c->d_S;
+    q.nzz = c->nzz;
+    q.nb = c->nb;
+    q.kc = c->kc;
+    q.shots = c->d_shots;
+    q.nshots = (int)c->hshots.size();
+    q.Tpool = c->d_T;
+    q.Tlpool = c->d_Tl;
+    const size_t npad = (size_t)c->nxx * c->nzz;
+    for (int k = 0; k < 6; k++) q.cij[k] = c->d_cij_all + k * npad;
+    std::memcpy(q.mm, c->mm, sizeof(q.mm));
+    q.Sq = c->d_Sq;
+    q.vfac = fact ? c->d_vfac : nullptr;
+    q.vfac_total = c->batch_q_cells;
+    const bool comp = c->arith == SF_ARITH_COMPENSATED, ref = c->arith == SF_ARITH_REFERENCE;
+    // x: enough CTAs of 256 threads for the widest window, grid-strided; y: the shots
+    const long long cells = (long long)c->nzz * c->batch_maxcols;
+    const unsigned gx = (unsigned)std::min<long long>((cells + 255) / 256, 2048);
+    const unsigned gy = (unsigned)std::min(q.nshots, 65535);
+    void* args[] = {&q};
+    CK(cudaLaunchKernel(sf_kqp_kernel(ref, comp, fact), dim3(gx, gy), dim3(256), args, 0, st));
+    return SF_OK;
 }
 
 int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
                     cudaStream_t st)
 {
-    FwdLaunch L;
-    int rc = sf_fwd_configure(c, ani, nrec, keep_tables, tape, gang_warps, st, &L);
-    L.p.stall_handoff = c->stall_next ? 1 : 0;  // sf_test_stall_next_batch
+    const bool stall = c->stall_next;  // sf_test_stall_next_batch
     c->stall_next = false;
-    if (!rc) rc = sf_fwd_enqueue(c, L, d_picks, sf_next_epoch(c), st);
+    int rc;
+    if (!ani) {
+        FwdLaunch L;
+        rc = sf_fwd_configure(c, nrec, keep_tables, tape, gang_warps, st, &L, nullptr);
+        L.p.stall_handoff = stall ? 1 : 0;
+        if (!rc) rc = sf_fwd_enqueue(c, L, d_picks, sf_next_epoch(c), st);
+    } else {
+        // eikonal_ani.cu:33-45: solve on S, qP pass, solve on the qP slowness;
+        // every shot keeps its window between the launches
+        rc = sf_dev_reserve(c, (void**)&c->d_Sq, &c->cap_Sq, (size_t)c->batch_q_cells * sizeof(float));
+        if (!rc && tape)
+            rc = sf_dev_reserve(c, (void**)&c->d_vfac, &c->cap_vfac, 3 * (size_t)c->batch_q_cells * sizeof(float));
+        FwdLaunch L1, L2;
+        if (!rc) rc = sf_fwd_configure(c, 0, true, false, gang_warps, st, &L1, nullptr);
+        if (!rc) rc = sf_fwd_configure(c, nrec, true, tape, gang_warps, st, &L2, c->d_Sq);
+        if (rc) return rc;
+        // the second configuration may have grown the shared buffers
+        L1.p.shots = c->d_shots;
+        L1.p.Tpool = c->d_T;
+        L1.p.Tlpool = L2.p.Tlpool;
+        L1.p.hand = c->d_hand;
+        L1.p.bar = c->d_ctr;
+        L1.p.stall_handoff = L2.p.stall_handoff = stall ? 1 : 0;
+        rc = sf_kt_begin(c, SF_KT_FORWARD, st);
+        if (!rc) rc = sf_fwd_launch(c, L1, nullptr, sf_next_epoch(c), st);
+        if (!rc) rc = sf_qp_launch(c, tape, st);
+        if (!rc) rc = sf_fwd_launch(c, L2, d_picks, sf_next_epoch(c), st);
+        if (!rc) rc = sf_kt_end(c, SF_KT_FORWARD, st);
+    }
     if (rc) return rc;
     c->tables_valid = keep_tables;
     c->tape_valid = tape;
@@ -830,7 +882,7 @@ extern "C" int sf_batch_forward(sf_ctx* c, int ani, const sf_shot* shots, int ns
     cudaStream_t st = (cudaStream_t)stream;
     c->tape_valid = false;
     c->tables_valid = false;
-    int rc = sf_prepare_shots(c, shots, nshots, tables, tape);
+    int rc = sf_prepare_shots(c, shots, nshots, tape);
     if (rc) return rc;
     rc = sf_upload_receivers(c, rx, rz, nrec, st);
     if (rc) return rc;
@@ -913,7 +965,7 @@ extern "C" int sf_time_propagation(sf_ctx* c, int ani, float sx, float sz, float
     CK(cudaSetDevice(c->dev));
     cudaStream_t st = (cudaStream_t)stream;
     sf_shot s{sx, sz, 0, c->nxx};
-    int rc = sf_prepare_shots(c, &s, 1, true, false);
+    int rc = sf_prepare_shots(c, &s, 1, false);
     if (rc) return rc;
     const size_t npad = (size_t)c->nxx * c->nzz;
     // the whole-grid table is written straight into the caller's device buffer

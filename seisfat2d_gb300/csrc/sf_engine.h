@@ -167,21 +167,24 @@ unsigned sf_next_epoch(sf_ctx* c);
 int sf_check_flags(sf_ctx* c, cudaStream_t st);
 int sf_fwd_setup(sf_ctx* c);
 int sf_verify_divisors(sf_ctx* c);
-size_t sf_fwd_smem_bytes(int warps, bool comp, bool taped_iso);
+size_t sf_fwd_smem_bytes(int warps, bool comp, bool tape);
 // k_shots instantiation (one object file each, sf_shots_inst.cu)
-const void* sf_kshots_kernel(bool tape, bool ref, bool vti, bool interior, bool comp);
+const void* sf_kshots_kernel(bool tape, bool ref, bool interior, bool comp);
+const void* sf_kqp_kernel(bool ref, bool comp, bool fact);
 // whether the batch of hshots, G CTAs per shot, runs the interior-block body
 bool sf_interior_loops(sf_ctx* c, const void* kernel, size_t smem, int G);
 void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4]);
-int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool keep_tables, bool tape);
+int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool tape);
 int sf_launch_shots(sf_ctx* c, int ani, int nrec, float* d_picks, bool keep_tables, bool tape, int gang_warps,
                     cudaStream_t st);
 // The two halves of sf_launch_shots: configure (gang shape, buffers, shot
 // table upload; host work and allocation) and enqueue (counter reset and the
 // launch; stream work only, capturable).
-int sf_fwd_configure(sf_ctx* c, int ani, int nrec, bool keep_tables, bool tape, int gang_warps, cudaStream_t st,
-                     FwdLaunch* L);
+int sf_fwd_configure(sf_ctx* c, int nrec, bool per_shot_T, bool tape, int gang_warps, cudaStream_t st,
+                     FwdLaunch* L, const float* Sshots);
 int sf_fwd_enqueue(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st);
+int sf_fwd_launch(sf_ctx* c, FwdLaunch& L, float* d_picks, unsigned epoch, cudaStream_t st);
+int sf_qp_launch(sf_ctx* c, bool fact, cudaStream_t st);
 int sf_adj_configure(sf_ctx* c, cudaStream_t st, AdjLaunch* A);
 int sf_adj_enqueue(sf_ctx* c, AdjLaunch& A, const float* d_pg, float* d_grad, unsigned epoch, cudaStream_t st);
 int sf_residual_enqueue(sf_ctx* c, const float* d_picks, const float* d_obs, float* d_pg, double* d_misfit,

@@ -1,7 +1,9 @@
-// Whole-shot forward kernel: one CTA solves one shot window at a time (init,
-// 4 sweeps, optional qP pass + second solve, receiver picks) and pulls the
-// next shot from a device work counter. The same kernel with one shot and one
-// CTA is the per-shot drop-in solver.
+// Whole-shot forward kernel: a gang of CTAs solves one shot window at a time
+// (init, 4 sweeps, receiver picks) and takes the shots k, k+NG, ... of its
+// gang. The same kernel with one shot and one CTA is the per-shot drop-in
+// solver. An anisotropic batch (eikonal_ani.cu:33-45) is three launches: the
+// solve of every shot on S, the qP pass over every shot's window (k_qp, a
+// map over cells), and the solve of every shot on its own qP slowness.
 #pragma once
 #include "sf_sweep.cuh"
 
@@ -18,11 +20,12 @@ struct ShotDev {
     int pad_;
     long long t_off;      // traveltime window offset (floats) when tables are kept
     long long tape_off;   // tape offset (entries)
-    long long q_off;      // qP derivative factors offset (window cells), anisotropic taped batches
+    long long q_off;      // window cells of the shots before it (qP slowness and derivative factors)
 };
 
 struct FwdParams {
     const float* S;       // padded slowness, column stride nzz
+    const float* Sshots;  // per-shot slowness windows at q_off (column stride nzz) instead of S, or nullptr
     int nzz, nxx, nb;
     Consts kc;
     const ShotDev* shots;
@@ -39,14 +42,6 @@ struct FwdParams {
     unsigned epoch;       // launch number (tags: epoch << 10 | shot-solve number)
     unsigned long long wait_ns;  // time limit of the bounded waits
     int stall_handoff;    // test of the timeout path: consumers wait for a tag no producer writes
-    // anisotropy
-    int ani;
-    const uint16_t* cij[6];
-    float mm[12];
-    float* Sq;            // qP slowness, Sq + gang * sq_per_gang
-    long long sq_per_gang;
-    float* vfac;          // taped: dSq/dS, dSq/dC11, dSq/dC13 per shot window cell (3 x vfac_total)
-    long long vfac_total;
     // tape
     uint8_t* tcode;
     float* tc1;
@@ -175,12 +170,11 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
 
 // Persistent gangs of G CTAs: gang k solves shots k, k+NG, ... (shots are
 // sorted widest window first). The grid never exceeds what the device can
-// hold at once, so every gang's CTAs are resident together. VTI (with TAPE):
-// anisotropic shots whose second (qP) solve is taped, with the qP pass
-// writing its derivative factors. INTERIOR: the strip loops' bounds-test-free
-// body for interior blocks (see run_strip). COMP: compensated arithmetic
-// (node_update_comp; the 3x3 initial values are the FP64 ones rounded once).
-template <bool TAPE, bool REF, bool VTI, bool INTERIOR, bool COMP = false>
+// hold at once, so every gang's CTAs are resident together. INTERIOR: the
+// strip loops' bounds-test-free body for interior blocks (see run_strip).
+// COMP: compensated arithmetic (node_update_comp; the 3x3 initial values are
+// the FP64 ones rounded once).
+template <bool TAPE, bool REF, bool INTERIOR, bool COMP = false>
 // (kMaxWarps * 32, 1): with the block size alone as the bound ptxas caps the
 // kernel at 64 registers and spills the strip loop's state to local memory.
 __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? kMaxWarpsTapedInterior : kMaxWarps)) * 32, 1)
@@ -190,11 +184,10 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
     unsigned char* rings = smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15));
-    constexpr size_t kRingStride = ring_bytes<COMP>(fwd_ring_slots<TAPE, VTI>());
+    constexpr size_t kRingStride = ring_bytes<COMP>(FwdBlock<TAPE>::RING);
     const int tid = threadIdx.x;
     const GangPos gp = gang_pos(p.G);
     const int nzz = p.nzz;
-    const int nstrips = (nzz + 31) >> 5;
     unsigned* bar = p.bar + gp.gang;
     unsigned nbar = 0;
     if (tid == 0) {
@@ -202,81 +195,19 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
         cs->wait_ns = p.wait_ns ? p.wait_ns : kSpinNs;
     }
     __syncthreads();
-    const int nsolves = p.ani ? 2 : 1;
     int it = 0;
 #pragma unroll 1
     for (int b = gp.gang; b < p.nshots; b += p.NG, it++) {
         const ShotDev sh = p.shots[b];
-        const int ncols = sh.ncols;
         float* T = (p.t_per_gang > 0) ? p.Tpool + (size_t)gp.gang * p.t_per_gang : p.Tpool + sh.t_off;
         float* Tl = !COMP ? nullptr
                           : (p.t_per_gang > 0) ? p.Tlpool + (size_t)gp.gang * p.t_per_gang : p.Tlpool + sh.t_off;
-        const float* Sw = p.S + (size_t)sh.c0 * nzz;
-        const unsigned tag = (p.epoch << 10) | (unsigned)((it * nsolves) & 1023);
+        // the shot's slowness window: columns c0.. of S, or its own qP slowness
+        const float* Sw = p.Sshots ? p.Sshots + sh.q_off : p.S + (size_t)sh.c0 * nzz;
+        const unsigned tag = (p.epoch << 10) | (unsigned)(it & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE && !VTI, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings, kRingStride);
-        // taped isotropic batches never set ani: their kernels carry no qP pass
-        if ((!TAPE || VTI) && p.ani) {
-            // get_quasi_slowness (eikonal_ani.cu:47-111) on the window, rows of this
-            // warp's strips, once the whole first solve is done
-            gang_barrier(bar, (++nbar) * p.G, cs, p.err);
-            float* Sq = p.Sq + (size_t)gp.gang * p.sq_per_gang;
-            const int sloc = sh.sIdx - sh.c0, nb = p.nb, lane = tid & 31;
-            for (int k = gp.slot; k < nstrips; k += gp.slots) {  // the rows of this warp's strips
-                const int i = 32 * k + lane;
-                if (i >= nzz) continue;
-                for (int j = 0; j < ncols; j++) {
-                    const size_t idx = (size_t)i + (size_t)j * nzz;
-                    const size_t g = (size_t)i + (size_t)(sh.c0 + j) * nzz;
-                    float s = p.S[g];
-                    float out = s;
-                    float fS = 1.0f, f11 = 0.0f, f13 = 0.0f;
-                    if (i >= nb && i < nzz - nb && j >= nb && j < ncols - nb && !(i == sh.sIdz && j == sloc)) {
-                        const float* Tc = T + idx;
-                        const float c11 = decode_c(p.cij[0][g], p.mm[0], p.mm[1]);
-                        const float c13 = decode_c(p.cij[1][g], p.mm[2], p.mm[3]);
-                        const float c15 = decode_c(p.cij[2][g], p.mm[4], p.mm[5]);
-                        const float c33 = decode_c(p.cij[3][g], p.mm[6], p.mm[7]);
-                        const float c35 = decode_c(p.cij[4][g], p.mm[8], p.mm[9]);
-                        const float c55 = decode_c(p.cij[5][g], p.mm[10], p.mm[11]);
-                        // central differences; of the pairs in the compensated arithmetic
-                        float dzr, dxr;
-                        if (COMP) {
-                            const float* Lc = Tl + idx;
-                            dzr = ff_diff(Tc[1], Lc[1], Tc[-1], Lc[-1]);
-                            dxr = ff_diff(Tc[nzz], Lc[nzz], Tc[-(long)nzz], Lc[-(long)nzz]);
-                        } else {
-                            dzr = fsub(Tc[1], Tc[-1]);
-                            dxr = fsub(Tc[nzz], Tc[-(long)nzz]);
-                        }
-                        out = qp_slowness<REF>(dzr, dxr, s, p.kc.dx, p.kc.dz, c11, c13, c15, c33, c35, c55);
-                        if (VTI) qp_factors(dzr, dxr, s, p.kc.dx, p.kc.dz, c11, c13, c15, c33, c35, c55, fS, f11, f13);
-                    }
-                    Sq[idx] = out;
-                    if (VTI) {
-                        float* f = p.vfac + sh.q_off + idx;
-                        f[0] = fS;
-                        f[p.vfac_total] = f11;
-                        f[2 * p.vfac_total] = f13;
-                    }
-                }
-            }
-            gang_barrier(bar, (++nbar) * p.G, cs, p.err);
-            if (tid < 9) {
-                // second time_init reads the qP field (window-local columns)
-                const int a = tid % 3, bb = tid / 3;
-                const int zi = sh.sIdz + a - 1, xl = sloc + bb - 1;
-                const float s = Sq[zi + (size_t)xl * nzz];
-                if (REF)
-                    cs->init[tid] = src_value_f32(s, zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz);
-                else
-                    cs->init[tid] = __double2float_rn(
-                        __dmul_rn((double)s, src_dist(zi, xl + sh.c0, p.nb, p.kc.dx, p.kc.dz, sh.sx, sh.sz)));
-            }
-            __syncthreads();
-            solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sq, nzz, T, Tl, tag + 1u, cs, rings, kRingStride);
-        }
+        solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings, kRingStride);
         // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {
             gang_barrier(bar, (++nbar) * p.G, cs, p.err);
@@ -284,13 +215,87 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
                 int i, j;
                 float xd, zd;
                 float v = __int_as_float(0x7fc00000);
-                if (pick_geom(p.rx[r], p.rz[r], p.kc.dx, p.kc.dz, p.nb, nzz, ncols, sh.c0, i, j, xd, zd))
+                if (pick_geom(p.rx[r], p.rz[r], p.kc.dx, p.kc.dz, p.nb, nzz, sh.ncols, sh.c0, i, j, xd, zd))
                     v = pick_value(T, nzz, i, j, xd, zd);
                 p.picks[(size_t)sh.orig * p.nrec + r] = v;
             }
         }
         // the gang's buffers are reused by its next shot
         gang_barrier(bar, (++nbar) * p.G, cs, p.err);
+    }
+}
+
+// The qP pass of an anisotropic batch, get_quasi_slowness
+// (eikonal_ani.cu:47-111), on every shot's window once the first solves are
+// done: the qP slowness of each window cell from the central differences of
+// the window's traveltimes (of their pairs in the compensated arithmetic)
+// and the decoded stiffness; the window's edge cells (nb of them) and the
+// source node keep S. FACT (taped batches): also the derivative factors dSq/dS,
+// dSq/dC11, dSq/dC13 of each cell. A map over cells: blockIdx.y strides over
+// the shots, the x dimension over a shot's window.
+struct QpParams {
+    const float* S;       // padded slowness, column stride nzz
+    int nzz, nb;
+    Consts kc;
+    const ShotDev* shots;
+    int nshots;
+    const float* Tpool;   // per-shot traveltime windows at t_off
+    const float* Tlpool;  // their lo parts (compensated)
+    const uint16_t* cij[6];
+    float mm[12];
+    float* Sq;            // per-shot qP slowness windows at q_off
+    float* vfac;          // FACT: dSq/dS, dSq/dC11, dSq/dC13 per window cell (3 x vfac_total)
+    long long vfac_total;
+};
+
+template <bool REF, bool COMP, bool FACT>
+__global__ void __launch_bounds__(256) k_qp(QpParams p)
+{
+    const int nzz = p.nzz, nb = p.nb;
+#pragma unroll 1
+    for (int b = blockIdx.y; b < p.nshots; b += gridDim.y) {
+        const ShotDev sh = p.shots[b];
+        const int ncols = sh.ncols, sloc = sh.sIdx - sh.c0;
+        const float* T = p.Tpool + sh.t_off;
+        const float* Tl = COMP ? p.Tlpool + sh.t_off : nullptr;
+        float* Sq = p.Sq + sh.q_off;
+        const size_t ncell = (size_t)nzz * ncols;
+#pragma unroll 1
+        for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < ncell; idx += (size_t)gridDim.x * blockDim.x) {
+            const int i = (int)(idx % nzz), j = (int)(idx / nzz);
+            const size_t g = (size_t)i + (size_t)(sh.c0 + j) * nzz;
+            const float s = p.S[g];
+            float out = s;
+            float fS = 1.0f, f11 = 0.0f, f13 = 0.0f;
+            if (i >= nb && i < nzz - nb && j >= nb && j < ncols - nb && !(i == sh.sIdz && j == sloc)) {
+                const float* Tc = T + idx;
+                const float c11 = decode_c(p.cij[0][g], p.mm[0], p.mm[1]);
+                const float c13 = decode_c(p.cij[1][g], p.mm[2], p.mm[3]);
+                const float c15 = decode_c(p.cij[2][g], p.mm[4], p.mm[5]);
+                const float c33 = decode_c(p.cij[3][g], p.mm[6], p.mm[7]);
+                const float c35 = decode_c(p.cij[4][g], p.mm[8], p.mm[9]);
+                const float c55 = decode_c(p.cij[5][g], p.mm[10], p.mm[11]);
+                // central differences; of the pairs in the compensated arithmetic
+                float dzr, dxr;
+                if (COMP) {
+                    const float* Lc = Tl + idx;
+                    dzr = ff_diff(Tc[1], Lc[1], Tc[-1], Lc[-1]);
+                    dxr = ff_diff(Tc[nzz], Lc[nzz], Tc[-(long)nzz], Lc[-(long)nzz]);
+                } else {
+                    dzr = fsub(Tc[1], Tc[-1]);
+                    dxr = fsub(Tc[nzz], Tc[-(long)nzz]);
+                }
+                out = qp_slowness<REF>(dzr, dxr, s, p.kc.dx, p.kc.dz, c11, c13, c15, c33, c35, c55);
+                if (FACT) qp_factors(dzr, dxr, s, p.kc.dx, p.kc.dz, c11, c13, c15, c33, c35, c55, fS, f11, f13);
+            }
+            Sq[idx] = out;
+            if (FACT) {
+                float* f = p.vfac + sh.q_off + idx;
+                f[0] = fS;
+                f[p.vfac_total] = f11;
+                f[2 * p.vfac_total] = f13;
+            }
+        }
     }
 }
 

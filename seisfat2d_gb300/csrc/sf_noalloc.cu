@@ -62,7 +62,7 @@ int noalloc_setup(int dev, unsigned char** addr)
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SF_ERR_CUDA;
-        if (cudaFuncSetAttribute(sf_kshots_kernel(false, true, false, true, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(sf_kshots_kernel(false, true, true, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sf_fwd_smem_bytes(kMaxWarps, false, false)) != cudaSuccess)
             return SF_ERR_CUDA;
         // the tagged pairs must not start with a valid-looking tag
@@ -190,7 +190,7 @@ extern "C" int sf_time_propagation_noalloc(const float* S, int nx, int nz, float
     p.epoch = epoch;
     const int warps = 8;
     void* args[] = {&p};
-    if (cudaLaunchKernel(sf_kshots_kernel(false, true, false, true, false), dim3(1), dim3(warps * 32), args,
+    if (cudaLaunchKernel(sf_kshots_kernel(false, true, true, false), dim3(1), dim3(warps * 32), args,
                          sf_fwd_smem_bytes(warps, false, false), st) != cudaSuccess)
         return SF_ERR_CUDA;
     int err = 0;

@@ -76,7 +76,7 @@ extern "C" int sf_kernel_times(sf_ctx* c, float* ms, int n)
 
 static int plan_configure(sf_ctx* c, cudaStream_t st)
 {
-    int rc = sf_fwd_configure(c, 0, c->plan_nrec, false, true, c->gang_warps, st, &c->plan_f);
+    int rc = sf_fwd_configure(c, c->plan_nrec, false, true, c->gang_warps, st, &c->plan_f, nullptr);
     if (!rc) rc = sf_adj_configure(c, st, &c->plan_a);
     if (rc) {
         c->plan_valid = false;
@@ -97,7 +97,7 @@ extern "C" int sf_plan_batch(sf_ctx* c, const sf_shot* shots, int nshots, const 
     c->tape_valid = false;
     c->tables_valid = false;
     c->batch_ani = 0;
-    int rc = sf_prepare_shots(c, shots, nshots, false, true);
+    int rc = sf_prepare_shots(c, shots, nshots, true);
     if (!rc) rc = sf_upload_receivers(c, rx, rz, nrec, st);
     if (rc) return rc;
     c->batch_nshots = nshots;

@@ -79,11 +79,6 @@ constexpr size_t ring_bytes(int R)
 {
     return sizeof(float) * (size_t)R * ((COMP ? kSPc : kSP) + (COMP ? 2 : 1) * kTP);
 }
-// Ring slots per warp of a forward kernel: the taped isotropic kernels run
-// only taped strip loops, every other kernel plain ones (the anisotropic
-// taped kernels also for their first solve).
-template <bool TAPE, bool VTI>
-constexpr int fwd_ring_slots() { return (TAPE && !VTI) ? FwdBlock<true>::RING : FwdBlock<false>::RING; }
 
 // Per-CTA shared state (static part), followed by the CTA's warp rings in
 // dynamic shared memory.
