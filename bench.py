@@ -568,7 +568,9 @@ def measure(cfg, a, env, arith, full, steps, warmup):
     kname = "k_shots_tape" if fa else ("k_shots_ani" if ani else "k_shots")
     if arith == "compensated":
         kname += "_comp"  # its own capture (the lo parts add window traffic); absent ones give no traffic
-    stages = {"forward": {"kernel": "sf::k_shots<tape>" if fa else "sf::k_shots", "ms": kt["forward"],
+    fkern = "sf::k_shots<tape>" if fa else ("sf::k_shots, sf::k_qp, sf::k_shots (solve on S, qP pass, solve on the qP slowness)"
+                                            if ani else "sf::k_shots")
+    stages = {"forward": {"kernel": fkern, "ms": kt["forward"],
                           "algorithmic_bytes": fwd_bpc * cells, "traffic_file": f"{kname}_cfg{cfg}.txt"}}
     if fa and "gather" in kt:
         stages["adjoint"] = {"kernel": "sf::k_adjoint", "ms": kt["adjoint"],
@@ -625,7 +627,7 @@ def measure(cfg, a, env, arith, full, steps, warmup):
                      "step": {"algorithmic_bytes": step_bytes,
                               "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
                               "frac": step_bytes / (ms / 1e3) / 1e9 / peak}},
-        "gpu_launches": steps * ((4 if "gather" in kt else 3) if fa else 1),
+        "gpu_launches": steps * ((4 if "gather" in kt else 3) if fa else (3 if ani else 1)),
         "clocks": clk.summary(),
         "wall_s_timed": wall,
     }

@@ -783,9 +783,8 @@ int sf_qp_launch(sf_ctx* c, bool fact, cudaStream_t st)
     q.vfac = fact ? c->d_vfac : nullptr;
     q.vfac_total = c->batch_q_cells;
     const bool comp = c->arith == SF_ARITH_COMPENSATED, ref = c->arith == SF_ARITH_REFERENCE;
-    // x: enough CTAs of 256 threads for the widest window, grid-strided; y: the shots
-    const long long cells = (long long)c->nzz * c->batch_maxcols;
-    const unsigned gx = (unsigned)std::min<long long>((cells + 255) / 256, 2048);
+    // x: the widest window's columns (grid-strided past 2048); y: the shots
+    const unsigned gx = (unsigned)std::min(c->batch_maxcols, 2048);
     const unsigned gy = (unsigned)std::min(q.nshots, 65535);
     void* args[] = {&q};
     CK(cudaLaunchKernel(sf_kqp_kernel(ref, comp, fact), dim3(gx, gy), dim3(256), args, 0, st));

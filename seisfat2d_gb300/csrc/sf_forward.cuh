@@ -232,7 +232,8 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
 // and the decoded stiffness; the window's edge cells (nb of them) and the
 // source node keep S. FACT (taped batches): also the derivative factors dSq/dS,
 // dSq/dC11, dSq/dC13 of each cell. A map over cells: blockIdx.y strides over
-// the shots, the x dimension over a shot's window.
+// the shots, blockIdx.x over a window's columns, the threads over a column's
+// rows (coalesced, z fastest).
 struct QpParams {
     const float* S;       // padded slowness, column stride nzz
     int nzz, nb;
@@ -259,10 +260,11 @@ __global__ void __launch_bounds__(256) k_qp(QpParams p)
         const float* T = p.Tpool + sh.t_off;
         const float* Tl = COMP ? p.Tlpool + sh.t_off : nullptr;
         float* Sq = p.Sq + sh.q_off;
-        const size_t ncell = (size_t)nzz * ncols;
 #pragma unroll 1
-        for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < ncell; idx += (size_t)gridDim.x * blockDim.x) {
-            const int i = (int)(idx % nzz), j = (int)(idx / nzz);
+        for (int j = blockIdx.x; j < ncols; j += gridDim.x)
+#pragma unroll 1
+        for (int i = threadIdx.x; i < nzz; i += blockDim.x) {
+            const size_t idx = (size_t)i + (size_t)j * nzz;
             const size_t g = (size_t)i + (size_t)(sh.c0 + j) * nzz;
             const float s = p.S[g];
             float out = s;
