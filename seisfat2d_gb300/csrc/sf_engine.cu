@@ -787,7 +787,7 @@ int sf_qp_launch(sf_ctx* c, bool fact, cudaStream_t st)
     const unsigned gx = (unsigned)std::min(c->batch_maxcols, 2048);
     const unsigned gy = (unsigned)std::min(q.nshots, 65535);
     void* args[] = {&q};
-    CK(cudaLaunchKernel(sf_kqp_kernel(ref, comp, fact), dim3(gx, gy), dim3(256), args, 0, st));
+    CK(cudaLaunchKernel(sf_kqp_kernel(ref, comp, fact), dim3(gx, gy), dim3(128), args, 0, st));
     return SF_OK;
 }
 
