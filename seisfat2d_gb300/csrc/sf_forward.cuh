@@ -104,8 +104,7 @@ __device__ __forceinline__ GangPos gang_pos(int G)
 // arithmetic, lo parts in Tl, two handoff pairs per column.
 template <bool TAPE, bool REF, bool INTERIOR, bool COMP>
 __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPos& gp, const float* Sw,
-                             int ldS, float* T, float* Tl, unsigned tag, CtaShared* cs, unsigned char* rings,
-                             size_t ring_stride)
+                             int ldS, float* T, float* Tl, unsigned tag, CtaShared* cs, unsigned char* rings)
 {
     const int nzz = p.nzz, ncols = sh.ncols;
     const int nstrips = (nzz + 31) >> 5;
@@ -123,7 +122,7 @@ __device__ void solve_window(const FwdParams& p, const ShotDev& sh, const GangPo
     a.sIdx = sh.sIdx - sh.c0;
     a.kc = p.kc;
     a.init = cs->init;
-    a.ring = rings + (size_t)gp.warp * ring_stride;
+    a.ring = rings + (size_t)gp.warp * ring_bytes<COMP>(FwdBlock<TAPE>::RING);
     a.sh = cs;
     a.err = p.err;
     a.tcode = nullptr;
@@ -184,7 +183,6 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaShared* cs = reinterpret_cast<CtaShared*>(smem_raw);
     unsigned char* rings = smem_raw + ((sizeof(CtaShared) + 15) & ~size_t(15));
-    constexpr size_t kRingStride = ring_bytes<COMP>(FwdBlock<TAPE>::RING);
     const int tid = threadIdx.x;
     const GangPos gp = gang_pos(p.G);
     const int nzz = p.nzz;
@@ -207,7 +205,7 @@ __global__ void __launch_bounds__((COMP ? kMaxWarpsComp : ((TAPE && INTERIOR) ? 
         const unsigned tag = (p.epoch << 10) | (unsigned)(it & 1023);
         init_block<REF>(p, sh, Sw, cs->init);
         __syncthreads();
-        solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings, kRingStride);
+        solve_window<TAPE, REF, INTERIOR, COMP>(p, sh, gp, Sw, nzz, T, Tl, tag, cs, rings);
         // receivers (modeling.cu:161-194), spread over the gang once the field is final
         if (p.nrec > 0 && p.picks) {
             gang_barrier(bar, (++nbar) * p.G, cs, p.err);
