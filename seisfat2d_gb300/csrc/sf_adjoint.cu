@@ -63,6 +63,7 @@ static void cubic_weights(double t, double w[4])
 // a shot's window is decided per shot from its padded column.
 static int prepare_seed(sf_ctx* c, cudaStream_t st)
 {
+    if (c->seed_gen == c->recv_gen && c->seed_nrec == c->batch_nrec) return SF_OK;  // same receivers
     const int nrec = c->batch_nrec, nzz = c->nzz, nb = c->nb;
     const float dx = c->dx, dz = c->dz;
     std::vector<int> rec_jg(std::max(nrec, 1), -1000000);
@@ -122,6 +123,8 @@ static int prepare_seed(sf_ctx* c, cudaStream_t st)
                            cudaMemcpyHostToDevice, st));
     c->seed_nodes = nn;
     c->seed_entries = ne;
+    c->seed_gen = c->recv_gen;
+    c->seed_nrec = nrec;
     return SF_OK;
 }
 
@@ -130,6 +133,8 @@ static int prepare_seed(sf_ctx* c, cudaStream_t st)
 // order, with what the gather needs of each.
 static int prepare_gather(sf_ctx* c, cudaStream_t st)
 {
+    if (c->gather_gen == c->shots_gen) return SF_OK;  // same shot table
+
     const int ns = (int)c->hshots.size();
     const int nblk = (c->nxx + kGT - 1) / kGT;
     std::vector<int> ptr(nblk + 1, 0);
@@ -164,6 +169,7 @@ static int prepare_gather(sf_ctx* c, cudaStream_t st)
     if (!c->h_gshots.empty())
         CK(cudaMemcpyAsync(c->d_gshots, c->h_gshots.data(), c->h_gshots.size() * sizeof(GatherShot),
                            cudaMemcpyHostToDevice, st));
+    c->gather_gen = c->shots_gen;
     return SF_OK;
 }
 

@@ -560,6 +560,10 @@ void sf_skip_cells(int ncols, int nzz, int si[4], int sj[4])
 int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool tape)
 {
     c->plan_valid = false;  // the planned batch's tables are replaced
+    // a new generation unless the table comes out the same as before (an
+    // early error return leaves it new)
+    const std::vector<ShotDev> prev = c->hshots;
+    const unsigned long long prev_gen = c->shots_gen++;
     c->hshots.resize(nshots);
     std::vector<int> order(nshots);
     std::vector<std::pair<int, std::array<int, 8>>> skip_cache;
@@ -617,6 +621,9 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool tape)
     c->batch_maxcols = maxcols;
     c->tables_index.assign(nshots, 0);
     for (int q = 0; q < nshots; q++) c->tables_index[c->hshots[q].orig] = q;
+    if (prev.size() == c->hshots.size() &&
+        std::memcmp(prev.data(), c->hshots.data(), prev.size() * sizeof(ShotDev)) == 0)
+        c->shots_gen = prev_gen;
     return SF_OK;
 }
 
@@ -845,6 +852,7 @@ int sf_upload_receivers(sf_ctx* c, const float* rx, const float* rz, int nrec, c
         return SF_OK;  // unchanged receivers stay on the device
     c->h_rx.assign(rx, rx + nrec);
     c->h_rz.assign(rz, rz + nrec);
+    c->recv_gen++;
     CK(cudaMemcpyAsync(c->d_rx, c->h_rx.data(), nrec * sizeof(float), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->d_rz, c->h_rz.data(), nrec * sizeof(float), cudaMemcpyHostToDevice, st));
     return SF_OK;

@@ -116,6 +116,11 @@ struct sf_ctx {
     int seed_nodes = 0, seed_entries = 0;
     std::vector<int> h_seed_pack;
     std::vector<float> h_seed_w;
+    // the gather's shot lists and the seed table are rebuilt only when the
+    // batch's shots or receivers changed (generations of each)
+    unsigned long long shots_gen = 1, recv_gen = 1;
+    unsigned long long gather_gen = 0, seed_gen = 0;
+    int seed_nrec = -1;
 
     // model update (sf_smooth_model, sf_update_slowness)
     float* d_skern = nullptr; size_t cap_skern = 0;
