@@ -565,8 +565,6 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool tape)
     const std::vector<ShotDev> prev = c->hshots;
     const unsigned long long prev_gen = c->shots_gen++;
     c->hshots.resize(nshots);
-    std::vector<int> order(nshots);
-    std::vector<std::pair<int, std::array<int, 8>>> skip_cache;
     long long toff = 0, tape_off = 0, q_off = 0;
     const int nstrips = (c->nzz + 31) / 32;
     int maxcols = 0;
@@ -590,19 +588,15 @@ int sf_prepare_shots(sf_ctx* c, const sf_shot* shots, int nshots, bool tape)
         const int sloc = d.sIdx - d.c0;
         if (d.sIdz < 1 || d.sIdz > c->nzz - 2 || sloc < 1 || sloc > d.ncols - 2)
             return sf_fail(c, SF_ERR_RANGE, "shot " + std::to_string(b) + ": source outside its window");
-        bool found = false;
-        for (auto& e : skip_cache)
-            if (e.first == d.ncols) {
-                for (int q = 0; q < 4; q++) { d.skip_i[q] = e.second[q]; d.skip_j[q] = e.second[4 + q]; }
-                found = true;
-                break;
-            }
-        if (!found) {
-            sf_skip_cells(d.ncols, c->nzz, d.skip_i, d.skip_j);
+        // the skipped cells depend on the window width alone (nzz is the
+        // context's): computed once per width for the context's lifetime
+        auto it = c->skip_cache.find(d.ncols);
+        if (it == c->skip_cache.end()) {
             std::array<int, 8> v;
-            for (int q = 0; q < 4; q++) { v[q] = d.skip_i[q]; v[4 + q] = d.skip_j[q]; }
-            skip_cache.push_back({d.ncols, v});
+            sf_skip_cells(d.ncols, c->nzz, v.data(), v.data() + 4);
+            it = c->skip_cache.emplace(d.ncols, v).first;
         }
+        for (int q = 0; q < 4; q++) { d.skip_i[q] = it->second[q]; d.skip_j[q] = it->second[4 + q]; }
         d.orig = b;
         d.t_off = toff;  // per-shot traveltime windows (tables, anisotropic batches)
         toff += (long long)c->nzz * d.ncols;

@@ -2,6 +2,7 @@
 #pragma once
 #include <array>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/seisfat2d.h"
@@ -71,6 +72,7 @@ struct sf_ctx {
 
     // batch state
     std::vector<sf::ShotDev> hshots;  // sorted widest first
+    std::unordered_map<int, std::array<int, 8>> skip_cache;  // window width -> skipped cells (sf_skip_cells)
     std::vector<int> tables_index;    // caller index -> hshots index
     long long batch_T_floats = 0, batch_tape_entries = 0;
     long long batch_q_cells = 0;      // window cells of all shots (qP derivative factors)
