@@ -105,7 +105,14 @@ int sf_compute_seismogram(sf_ctx* ctx, const float* T_dev, const float* rx, cons
 
 /* Batched forward: the shot loop of modeling_main.cpp:21-29 (and the
  * traveltime-table loops of migration.cu:116-171) in one persistent launch.
- * shots/rx/rz are host arrays; picks is nshots x nrec (shot-major). */
+ * shots/rx/rz are host arrays; picks is nshots x nrec (shot-major).
+ * ani = 1: three launches (eikonal_ani.cu:33-45): the solve of every shot on
+ * S, the qP pass over every shot's window, the solve of every shot on its
+ * qP slowness. Every shot then keeps its traveltime window and its qP
+ * slowness window on the device (nzz x ncols floats each, a second
+ * traveltime window in the compensated arithmetic, three factor windows
+ * with SF_KEEP_TAPE), so device memory grows with the batch: split batches
+ * whose windows exceed it (SF_ERR_CUDA when an allocation fails). */
 int sf_batch_forward(sf_ctx* ctx, int ani, const sf_shot* shots, int nshots, const float* rx,
                      const float* rz, int nrec, float* picks, int picks_mem, int flags,
                      void* stream);
